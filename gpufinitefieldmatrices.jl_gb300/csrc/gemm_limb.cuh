@@ -1,0 +1,382 @@
+// gemm_limb.cuh -- exact modular GEMM on the tcgen05 tensor cores.
+//
+// Representation.  A residue x in [0, N), N < 2^26, is centred to
+// c in (-N/2, N/2] and written in L balanced base-2^7 digits
+//     c = sum_{i<L} d_i 2^(7i),   d_i in [-64, 63],
+// each digit held exactly in fp16.  For A (m x k) and B (k x n):
+//     A*B = sum_s 2^(7s) C_s,   C_s = sum_{i+j=s} A_i B_j,   s = 0 .. 2L-2.
+//
+// Tensor-core mapping.  The L digit tiles of B for one 64-column output tile
+// are stacked along N into one operand B' = [B_0; B_1; ...; B_{L-1}] (64L
+// rows).  One tcgen05.mma of A_i (128 x 16) with B' (64L x 16) produces
+// [A_i B_0 | A_i B_1 | ... ] and is issued with its accumulator at TMEM
+// column 64*i, so the block A_i B_j lands in columns 64*(i+j): the shift-s
+// accumulator.  The 2L-1 shift accumulators (448 columns for L = 4) live side
+// by side in TMEM and every mma of the main loop has N = 64L (256 for L = 4).
+//
+// Exactness.  |d_i d_j| <= 2^12 and a shift accumulator sums at most L digit
+// products per k, so after Kc <= 4096/L values of k every partial sum is an
+// integer of magnitude <= 2^24 and the fp32 accumulation is exact.  The K loop
+// is therefore cut into chunks of Kc; after each chunk the epilogue warps
+// drain the accumulators, convert them to int32 and add
+// sum_s C_s * (2^(7s) mod N) into int64 registers; the final value is reduced
+// mod N with Barrett's method and stored.
+//
+// Warp roles (320 threads): warp 0 issues TMA loads, warp 1 allocates TMEM
+// and one lane issues the mma's, warps 2..9 are the epilogue (two warps per
+// 32-lane TMEM quadrant, each owning 32 of the 64 output columns).  Every
+// wait is bounded; on timeout a kernel records the failure in the library's
+// error word and returns without storing.
+#pragma once
+
+#include "gffm_common.cuh"
+#include "limb_host.h"
+
+namespace limb {
+
+constexpr int BM = 128;            // output rows per tile (tcgen05 M)
+constexpr int BN = 64;             // output columns per tile
+constexpr int BK = 64;             // k per pipeline stage (one 128-byte swizzle row of fp16)
+constexpr int A_TILE = BM * BK * 2;
+constexpr int B_TILE = BN * BK * 2;
+constexpr int NUM_EPI_WARPS = 8;
+constexpr int NUM_THREADS = 64 + 32 * NUM_EPI_WARPS;
+constexpr int MAX_SHIFTS = 7;
+constexpr int TILE_GROUP = 16;     // output-tile rows per raster group (L2 reuse)
+
+enum Epi { EPI_STORE_F64 = 0, EPI_STORE_F32 = 1, EPI_SUB_I32 = 2, EPI_STORE_I32 = 3 };
+
+template <int L>
+struct Cfg {
+    static constexpr int STAGE_BYTES = L * (A_TILE + B_TILE);
+    static constexpr int STAGES = (L == 4) ? 2 : (L == 3 ? 3 : (L == 2 ? 4 : 8));
+    static constexpr int NSHIFT = 2 * L - 1;
+    static constexpr int TMEM_COLS = (64 * NSHIFT <= 64) ? 64 : (64 * NSHIFT <= 128 ? 128 : (64 * NSHIFT <= 256 ? 256 : 512));
+    static constexpr int CHUNK_KB = 64 / L;  // Kc = 4096 / L
+    static constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024;
+};
+
+struct Params {
+    int m, n;              // true output size
+    int kblocks;           // padded K / BK
+    int Mpad, Npad;        // rows per digit plane of the A / B digit arrays
+    int mtiles, ntiles;
+    int chunk_kb;          // k-blocks per exact chunk
+    int64_t N;
+    uint64_t minv;         // floor((2^64-1)/N)
+    int64_t bias;          // multiple of N, >= 2^60
+    int32_t W[MAX_SHIFTS]; // 2^(7s) mod N
+    void *C;
+    int64_t ldc;
+    int *err;
+};
+
+__device__ __forceinline__ void tile_coords(int t, int mtiles, int ntiles, int &tm, int &tn) {
+    int group = t / (TILE_GROUP * ntiles);
+    int first_m = group * TILE_GROUP;
+    int gsz = mtiles - first_m < TILE_GROUP ? mtiles - first_m : TILE_GROUP;
+    int local = t - group * TILE_GROUP * ntiles;
+    tm = first_m + local % gsz;
+    tn = local / gsz;
+}
+
+__device__ __forceinline__ int64_t reduce_signed(int64_t acc, const Params &p) {
+    // acc + bias is in [0, 2^62); bias = 0 mod N
+    return (int64_t)gffm_dev::barrett64((uint64_t)(acc + p.bias), (uint64_t)p.N, p.minv);
+}
+
+template <int L, int EPI>
+__global__ void __launch_bounds__(NUM_THREADS, 1)
+    k_gemm_limb(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, Params p) {
+    using C_ = Cfg<L>;
+    extern __shared__ uint8_t dsmem_raw[];
+    __shared__ uint64_t full_bar[C_::STAGES];
+    __shared__ uint64_t empty_bar[C_::STAGES];
+    __shared__ uint64_t acc_full_bar, acc_empty_bar, drain_bar;
+    __shared__ uint32_t tmem_base_s;
+    __shared__ int abort_sh;
+    volatile int &abort_s = abort_sh;
+
+    uint8_t *smem = (uint8_t *)(((uintptr_t)dsmem_raw + 1023) & ~(uintptr_t)1023);
+    const int warp = threadIdx.x >> 5;
+    const int lane = threadIdx.x & 31;
+    const int ntiles_total = p.mtiles * p.ntiles;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < C_::STAGES; s++) {
+            gffm_dev::mbar_init(&full_bar[s], 1);
+            gffm_dev::mbar_init(&empty_bar[s], 1);
+        }
+        gffm_dev::mbar_init(&acc_full_bar, 1);
+        gffm_dev::mbar_init(&acc_empty_bar, NUM_EPI_WARPS);
+        gffm_dev::mbar_init(&drain_bar, 1);
+        abort_s = 0;
+        gffm_dev::fence_mbar_init();
+        gffm_dev::prefetch_tmap(&tmA);
+        gffm_dev::prefetch_tmap(&tmB);
+    }
+    if (warp == 1) gffm_dev::tmem_alloc(&tmem_base_s, C_::TMEM_COLS);
+    gffm_dev::tc_fence_before();
+    __syncthreads();
+    gffm_dev::tc_fence_after();
+    const uint32_t tmem = tmem_base_s;
+
+    if (warp == 0) {
+        // ---------------- TMA producer ----------------
+        if (lane == 0) {
+            int stage = 0;
+            uint32_t phase = 0;
+            uint32_t issued_parity_mask = 0, issued_mask = 0;
+            for (int t = blockIdx.x; t < ntiles_total && !abort_s; t += gridDim.x) {
+                int tm, tn;
+                tile_coords(t, p.mtiles, p.ntiles, tm, tn);
+                for (int kb = 0; kb < p.kblocks; kb++) {
+                    if (!gffm_dev::mbar_wait(&empty_bar[stage], phase ^ 1)) {
+                        atomicOr(p.err, 1);
+                        abort_s = 1;
+                        break;
+                    }
+                    if (abort_s) break;
+                    uint8_t *sa = smem + stage * C_::STAGE_BYTES;
+                    uint8_t *sb = sa + L * A_TILE;
+                    gffm_dev::mbar_arrive_expect_tx(&full_bar[stage], C_::STAGE_BYTES);
+#pragma unroll
+                    for (int l = 0; l < L; l++)
+                        gffm_dev::tma_load_2d(sa + l * A_TILE, &tmA, &full_bar[stage], kb * BK, l * p.Mpad + tm * BM);
+#pragma unroll
+                    for (int l = 0; l < L; l++)
+                        gffm_dev::tma_load_2d(sb + l * B_TILE, &tmB, &full_bar[stage], kb * BK, l * p.Npad + tn * BN);
+                    issued_mask |= 1u << stage;
+                    issued_parity_mask = (issued_parity_mask & ~(1u << stage)) | (phase << stage);
+                    if (++stage == C_::STAGES) {
+                        stage = 0;
+                        phase ^= 1;
+                    }
+                }
+            }
+            if (abort_s) {
+                // let copies already in flight land before the CTA exits (bounded)
+                for (int s = 0; s < C_::STAGES; s++)
+                    if (issued_mask & (1u << s)) gffm_dev::mbar_wait(&full_bar[s], (issued_parity_mask >> s) & 1);
+            }
+        }
+    } else if (warp == 1) {
+        // ---------------- MMA issuer ----------------
+        if (lane == 0) {
+            int stage = 0;
+            uint32_t phase = 0, acc_phase = 0;
+            bool issued_any = false;
+            const uint32_t idesc_full = gffm_dev::idesc_f16_f32(BM, BN * L);
+            const uint32_t idesc_lo = gffm_dev::idesc_f16_f32(BM, BN * (L > 1 ? L - 1 : 1));
+            const uint32_t idesc_one = gffm_dev::idesc_f16_f32(BM, BN);
+            for (int t = blockIdx.x; t < ntiles_total && !abort_s; t += gridDim.x) {
+                for (int kb0 = 0; kb0 < p.kblocks && !abort_s; kb0 += p.chunk_kb) {
+                    int kb1 = kb0 + p.chunk_kb < p.kblocks ? kb0 + p.chunk_kb : p.kblocks;
+                    if (!gffm_dev::mbar_wait(&acc_empty_bar, acc_phase ^ 1)) {
+                        atomicOr(p.err, 2);
+                        abort_s = 1;
+                        break;
+                    }
+                    gffm_dev::tc_fence_after();
+                    for (int kb = kb0; kb < kb1; kb++) {
+                        if (!gffm_dev::mbar_wait(&full_bar[stage], phase)) {
+                            atomicOr(p.err, 4);
+                            abort_s = 1;
+                            break;
+                        }
+                        gffm_dev::tc_fence_after();
+                        const uint32_t sa = gffm_dev::smem_u32(smem + stage * C_::STAGE_BYTES);
+                        const uint32_t sb = sa + L * A_TILE;
+#pragma unroll
+                        for (int kk = 0; kk < BK / 16; kk++) {
+                            const uint64_t bdesc = gffm_dev::umma_desc_sw128(sb + kk * 32);
+                            if (kb == kb0 && kk == 0) {
+                                // first k-step of a chunk: initialise every shift accumulator once
+                                gffm_dev::mma_f16(tmem, gffm_dev::umma_desc_sw128(sa + kk * 32), bdesc, idesc_full, 0);
+#pragma unroll
+                                for (int i = 1; i < L; i++) {
+                                    const uint64_t adesc = gffm_dev::umma_desc_sw128(sa + i * A_TILE + kk * 32);
+                                    gffm_dev::mma_f16(tmem + 64 * i, adesc, bdesc, idesc_lo, 1);
+                                    gffm_dev::mma_f16(tmem + 64 * (i + L - 1), adesc,
+                                                      gffm_dev::umma_desc_sw128(sb + (L - 1) * B_TILE + kk * 32),
+                                                      idesc_one, 0);
+                                }
+                            } else {
+#pragma unroll
+                                for (int i = 0; i < L; i++)
+                                    gffm_dev::mma_f16(tmem + 64 * i, gffm_dev::umma_desc_sw128(sa + i * A_TILE + kk * 32),
+                                                      bdesc, idesc_full, 1);
+                            }
+                        }
+                        issued_any = true;
+                        gffm_dev::mma_commit(&empty_bar[stage]);  // frees the stage once these mma's finish
+                        if (++stage == C_::STAGES) {
+                            stage = 0;
+                            phase ^= 1;
+                        }
+                    }
+                    if (abort_s) break;
+                    gffm_dev::mma_commit(&acc_full_bar);
+                    acc_phase ^= 1;
+                }
+            }
+            if (abort_s && issued_any) {
+                // wait (bounded) until every mma issued so far has completed
+                gffm_dev::mma_commit(&drain_bar);
+                gffm_dev::mbar_wait(&drain_bar, 0);
+            }
+        }
+    } else {
+        // ---------------- epilogue ----------------
+        const int ew = warp - 2;
+        const int quad = warp & 3;       // TMEM lane quadrant this warp may access
+        const int half = ew >> 2;        // which 32 of the 64 tile columns
+        uint32_t acc_phase = 0;
+        for (int t = blockIdx.x; t < ntiles_total; t += gridDim.x) {
+            int tm, tn;
+            tile_coords(t, p.mtiles, p.ntiles, tm, tn);
+            int64_t acc[32];
+#pragma unroll
+            for (int j = 0; j < 32; j++) acc[j] = 0;
+            bool ok = true;
+            int chunk = 0;
+            for (int kb0 = 0; kb0 < p.kblocks; kb0 += p.chunk_kb, chunk++) {
+                if (!gffm_dev::mbar_wait(&acc_full_bar, acc_phase)) {
+                    atomicOr(p.err, 8);
+                    abort_s = 1;
+                    ok = false;
+                    break;
+                }
+                gffm_dev::tc_fence_after();
+#pragma unroll
+                for (int s = 0; s < C_::NSHIFT; s++) {
+                    uint32_t v[32];
+                    gffm_dev::tmem_ld_32x32b_x32(tmem + ((uint32_t)(quad * 32) << 16) + 64 * s + 32 * half, v);
+                    gffm_dev::tmem_ld_wait();
+                    const int w = p.W[s];
+#pragma unroll
+                    for (int j = 0; j < 32; j++) acc[j] += (int64_t)__float2int_rz(__uint_as_float(v[j])) * w;
+                }
+                gffm_dev::tc_fence_before();
+                __syncwarp();
+                if (lane == 0) gffm_dev::mbar_arrive(&acc_empty_bar);
+                acc_phase ^= 1;
+                if ((chunk & 63) == 63) {
+#pragma unroll
+                    for (int j = 0; j < 32; j++) acc[j] = reduce_signed(acc[j], p);
+                }
+            }
+            if (!ok || abort_s) break;
+            const int64_t row = (int64_t)tm * BM + quad * 32 + lane;
+            const int64_t col0 = (int64_t)tn * BN + half * 32;
+            if (row < p.m) {
+#pragma unroll
+                for (int j = 0; j < 32; j++) {
+                    const int64_t col = col0 + j;
+                    if (col < p.n) {
+                        const int64_t r = reduce_signed(acc[j], p);
+                        const int64_t off = row + col * p.ldc;
+                        if (EPI == EPI_STORE_F64) {
+                            ((double *)p.C)[off] = (double)r;
+                        } else if (EPI == EPI_STORE_F32) {
+                            ((float *)p.C)[off] = (float)r;
+                        } else if (EPI == EPI_STORE_I32) {
+                            ((int32_t *)p.C)[off] = (int32_t)r;
+                        } else {
+                            int32_t *cp = (int32_t *)p.C + off;
+                            int64_t v = (int64_t)*cp - r;
+                            *cp = (int32_t)(v < 0 ? v + p.N : v);
+                        }
+                    }
+                }
+            }
+        }
+    }
+
+    gffm_dev::tc_fence_before();
+    __syncthreads();
+    gffm_dev::tc_fence_after();
+    if (warp == 1) gffm_dev::tmem_dealloc(tmem, C_::TMEM_COLS);
+}
+
+// ---------------------------------------------------------------------------
+// Digit split kernels
+// ---------------------------------------------------------------------------
+struct ModN {
+    int64_t n;
+    uint64_t minv;
+};
+
+// residue of an integer-valued element, centred into (-N/2, N/2]
+template <typename T>
+__device__ __forceinline__ int32_t centred(T v, const ModN &M) {
+    int64_t x = (int64_t)v;
+    int64_t r;
+    if (x >= 0 && x < M.n) {
+        r = x;
+    } else if (x >= 0) {
+        r = (int64_t)gffm_dev::barrett64((uint64_t)x, (uint64_t)M.n, M.minv);
+    } else {
+        uint64_t q = gffm_dev::barrett64((uint64_t)(-x), (uint64_t)M.n, M.minv);
+        r = q ? M.n - (int64_t)q : 0;
+    }
+    if (2 * r > M.n) r -= M.n;
+    return (int32_t)r;
+}
+
+template <int L>
+__device__ __forceinline__ void digits(int32_t c, __half (&d)[L]) {
+#pragma unroll
+    for (int i = 0; i < L; i++) {
+        int32_t di = ((c + 64) & 127) - 64;
+        d[i] = __int2half_rn(di);
+        c = (c - di) >> 7;
+    }
+}
+
+// A (m x k, column-major, lda) -> digit planes D[l][r][kk] (K-major, Mpad x Kpad per plane)
+template <typename T, int L>
+__global__ void __launch_bounds__(256) k_split_a(const T *__restrict__ A, int64_t lda, int m, int k, __half *__restrict__ D,
+                                                 int Mpad, int Kpad, ModN M) {
+    __shared__ int32_t tile[32][33];
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    const int64_t r0 = (int64_t)blockIdx.y * 32, k0 = (int64_t)blockIdx.x * 32;
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        int64_t kk = k0 + ty + 8 * i, r = r0 + tx;
+        tile[ty + 8 * i][tx] = (r < m && kk < k) ? centred(A[r + kk * lda], M) : 0;
+    }
+    __syncthreads();
+    const size_t plane = (size_t)Mpad * Kpad;
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        int64_t r = r0 + ty + 8 * i, kk = k0 + tx;
+        __half d[L];
+        digits<L>(tile[tx][ty + 8 * i], d);
+#pragma unroll
+        for (int l = 0; l < L; l++) D[l * plane + (size_t)r * Kpad + kk] = d[l];
+    }
+}
+
+// B (k x n, column-major, ldb) -> digit planes D[l][c][kk] (K-major, Npad x Kpad per plane)
+template <typename T, int L>
+__global__ void __launch_bounds__(256) k_split_b(const T *__restrict__ B, int64_t ldb, int k, int n, __half *__restrict__ D,
+                                                 int Npad, int Kpad, ModN M) {
+    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;  // pair index
+    const int64_t pairs_per_col = Kpad / 2;
+    const int64_t total = pairs_per_col * Npad;
+    if (idx >= total) return;
+    const int64_t c = idx / pairs_per_col;
+    const int64_t kk = (idx - c * pairs_per_col) * 2;
+    int32_t v0 = (c < n && kk < k) ? centred(B[kk + c * ldb], M) : 0;
+    int32_t v1 = (c < n && kk + 1 < k) ? centred(B[kk + 1 + c * ldb], M) : 0;
+    __half d0[L], d1[L];
+    digits<L>(v0, d0);
+    digits<L>(v1, d1);
+    const size_t plane = (size_t)Npad * Kpad;
+#pragma unroll
+    for (int l = 0; l < L; l++)
+        *reinterpret_cast<__half2 *>(D + l * plane + (size_t)c * Kpad + kk) = __halves2half2(d0[l], d1[l]);
+}
+
+}  // namespace limb

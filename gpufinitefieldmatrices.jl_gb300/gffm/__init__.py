@@ -1,0 +1,16 @@
+"""gffm -- GB300-native drop-in for the hot path of GPUFiniteFieldMatrices.jl.
+
+Host-side mirror of the reference's CuModMatrix / KaratsubaMatrix interface
+over the C ABI of libgffm (include/gffm.h).  Every operation runs a CUDA
+kernel of libgffm; there is no CPU fallback.
+"""
+from ._lib import GFFMError, load as load_library, lib_path  # noqa: F401
+from .build import build  # noqa: F401
+from .cumod import (  # noqa: F401
+    TILE_WIDTH, DEFAULT_TYPE, CuModArray, CuModMatrix, CuModVector, wrap, zeros, eye, rand, similar, copy,
+    add_, sub_, elementwise_multiply_, scalar_add_, scalar_sub_, rscalar_sub_, scalar_mul_, negate_,
+    mod_, mod_elements_, fill_, zero_, copy_, change_modulus, change_modulus_no_alloc_,
+    mul_, stripe_mul_, mat_mul_gpu_type, mat_mul_type_inplace_, find_max_stripe_ops,
+    CuModArraySizeMismatchException, CuModArrayModulusMismatchException, CuModMatrixNotSquareException,
+    CuModMatrixModulusNotPrimeException,
+)

@@ -1,0 +1,149 @@
+/*
+ * gffm.h -- C ABI of libgffm, the GB300 (sm_103a) implementation of the hot
+ * path of GPUFiniteFieldMatrices.jl: exact modular matrix multiply for moduli
+ * N < 2^26, PLUQ / LU / RREF over prime fields, and the two-digit Karatsuba
+ * matrix type.
+ *
+ * Conventions (they mirror the reference's CuModArray, src/CuModMatrix/
+ * CuModMatrix.jl:42-122):
+ *   - matrices are column-major device buffers with an explicit leading
+ *     dimension (the reference pads every dimension by 32, so a CuModMatrix of
+ *     size (m, n) has ld = m + 32; any ld >= m is accepted);
+ *   - elements are residues stored as double (Float64) or float (Float32);
+ *   - sizes are the true (unpadded) sizes;
+ *   - every call is asynchronous on `stream` (a cudaStream_t, NULL = legacy
+ *     default stream) unless its comment says it synchronizes;
+ *   - every call returns a gffm_status; the message of the last failure on the
+ *     calling thread is available from gffm_last_error_string();
+ *   - argument and overflow checks happen on the host before any launch and
+ *     raise the errors the reference throws (size / modulus mismatch, "cannot
+ *     perform a single multiplication" ...).
+ * The library never frees caller memory.  Calls that take a workspace accept
+ * NULL, in which case they allocate stream-ordered scratch (cudaMallocAsync)
+ * and release it on the same stream.
+ */
+#ifndef GFFM_H
+#define GFFM_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define GFFM_API __attribute__((visibility("default")))
+#else
+#define GFFM_API
+#endif
+
+typedef void *gffm_stream_t; /* cudaStream_t */
+
+enum gffm_status {
+    GFFM_OK = 0,
+    GFFM_ERR_ARG = 1,         /* null pointer, negative size, ld too small */
+    GFFM_ERR_SIZE = 2,        /* CuModArraySizeMismatchException / DimensionMismatch */
+    GFFM_ERR_MODULUS = 3,     /* modulus out of the supported range */
+    GFFM_ERR_STRIPE = 4,      /* "cannot perform a single multiplication" (stripe_mul.jl:200-202) */
+    GFFM_ERR_WORKSPACE = 5,   /* caller workspace too small */
+    GFFM_ERR_CUDA = 6,        /* a CUDA runtime / driver call failed */
+    GFFM_ERR_TIMEOUT = 7,     /* a device-side wait gave up (kernel returned early) */
+    GFFM_ERR_BOUNDS = 8,      /* the reference would index out of bounds */
+    GFFM_ERR_NOT_PRIME = 9,   /* CuModMatrixModulusNotPrimeException */
+    GFFM_ERR_UNSUPPORTED = 10 /* no sm_103 device, or an unsupported configuration */
+};
+
+/* ---- library ---------------------------------------------------------- */
+
+/* Version string of the library (no reference counterpart). */
+GFFM_API const char *gffm_version(void);
+
+/* Message of the last failed call on this thread (no reference counterpart;
+ * replaces the text of the Julia exceptions, CuModMatrix.jl:5-31). */
+GFFM_API const char *gffm_last_error_string(void);
+
+/* Synchronizes `stream` and reports (then clears) a device-side failure
+ * recorded by any kernel of the library since the last call: GFFM_OK or
+ * GFFM_ERR_TIMEOUT.  (No reference counterpart.) */
+GFFM_API int gffm_device_status(gffm_stream_t stream);
+
+/* find_max_stripe_ops(type, N) (src/CuModMatrix/kernel_mul/stripe_mul.jl:13-27):
+ * the number of products that can be summed exactly in the element type
+ * before a reduction.  bits = 53 (Float64), 24 (Float32), 11 (Float16). */
+GFFM_API int gffm_find_max_stripe_ops(int bits, int64_t N, int64_t *out);
+
+/* ---- elementwise modular kernels (src/CuModMatrix/kernel_ops/*.jl) ----
+ * All act on `len` contiguous elements -- the whole padded data array, as the
+ * reference's grid-stride kernels do -- with Julia mod semantics (result in
+ * [0, N)).  In-place use (C == A or C == B) is allowed. */
+
+/* add!(C, A, B; mod_N) -> k_add_matrix! (add_ops.jl:3-11,23-30) */
+GFFM_API int gffm_add_f64(double *C, const double *A, const double *B, int64_t len, int64_t N, gffm_stream_t stream);
+GFFM_API int gffm_add_f32(float *C, const float *A, const float *B, int64_t len, int64_t N, gffm_stream_t stream);
+/* sub!(C, A, B; mod_N) -> k_sub_matrix! (sub_ops.jl:3-11,33-40) */
+GFFM_API int gffm_sub_f64(double *C, const double *A, const double *B, int64_t len, int64_t N, gffm_stream_t stream);
+GFFM_API int gffm_sub_f32(float *C, const float *A, const float *B, int64_t len, int64_t N, gffm_stream_t stream);
+/* elementwise_multiply!(C, A, B, mod_N) -> k_mul_matrix! (mul_ops.jl:13-21,23-30) */
+GFFM_API int gffm_mul_elementwise_f64(double *C, const double *A, const double *B, int64_t len, int64_t N, gffm_stream_t stream);
+GFFM_API int gffm_mul_elementwise_f32(float *C, const float *A, const float *B, int64_t len, int64_t N, gffm_stream_t stream);
+/* scalar_add!(C, A, s, mod_N) -> k_add_scalar! (add_ops.jl:13-21,32-40) */
+GFFM_API int gffm_scalar_add_f64(double *C, const double *A, double s, int64_t len, int64_t N, gffm_stream_t stream);
+GFFM_API int gffm_scalar_add_f32(float *C, const float *A, float s, int64_t len, int64_t N, gffm_stream_t stream);
+/* scalar_sub!(C, A, s, mod_N) -> k_sub_scalar! (sub_ops.jl:13-21,42-50) */
+GFFM_API int gffm_scalar_sub_f64(double *C, const double *A, double s, int64_t len, int64_t N, gffm_stream_t stream);
+GFFM_API int gffm_scalar_sub_f32(float *C, const float *A, float s, int64_t len, int64_t N, gffm_stream_t stream);
+/* rscalar_sub!(C, A, s, mod_N), negate! = rscalar_sub!(B, A, 0) -> k_rsub_scalar! (sub_ops.jl:23-31,52-60) */
+GFFM_API int gffm_rscalar_sub_f64(double *C, const double *A, double s, int64_t len, int64_t N, gffm_stream_t stream);
+GFFM_API int gffm_rscalar_sub_f32(float *C, const float *A, float s, int64_t len, int64_t N, gffm_stream_t stream);
+/* mul!(C, A, s, mod_N) -> k_mul_scalar! (mul_ops.jl:3-11,32-40) */
+GFFM_API int gffm_scalar_mul_f64(double *C, const double *A, double s, int64_t len, int64_t N, gffm_stream_t stream);
+GFFM_API int gffm_scalar_mul_f32(float *C, const float *A, float s, int64_t len, int64_t N, gffm_stream_t stream);
+/* mod!(C, A, N) / mod_elements! -> k_mod! (mod_ops.jl:3-11,13-21) */
+GFFM_API int gffm_mod_f64(double *C, const double *A, int64_t len, int64_t N, gffm_stream_t stream);
+GFFM_API int gffm_mod_f32(float *C, const float *A, int64_t len, int64_t N, gffm_stream_t stream);
+
+/* ---- plain modular GEMM / GEMV: the reference's own method ---------------
+ * C = A*B mod N with A (m x k, lda), B (k x n, ldb), C (m x n, ldc).
+ * Products are summed exactly in the element type in K-stripes of
+ * `stripe` columns (0 = find_max_stripe_ops(type, N), the reference's bound)
+ * and reduced mod N after every stripe, as stripe_mul! does
+ * (src/CuModMatrix/kernel_mul/stripe_mul.jl:175-244, called by mul!,
+ * CuModMatrix.jl:767-787, and *, kernel_ops/mul_ops.jl:54-58); the stripes
+ * are reduced in registers instead of by full-matrix mod! passes.  Only the
+ * m x n region of C is written.  GFFM_ERR_STRIPE when the stripe bound is
+ * below one product.  C must not alias A or B. */
+GFFM_API int gffm_matmul_plain_f64(int64_t m, int64_t n, int64_t k, const double *A, int64_t lda, const double *B,
+                          int64_t ldb, double *C, int64_t ldc, int64_t N, int64_t stripe, gffm_stream_t stream);
+GFFM_API int gffm_matmul_plain_f32(int64_t m, int64_t n, int64_t k, const float *A, int64_t lda, const float *B,
+                          int64_t ldb, float *C, int64_t ldc, int64_t N, int64_t stripe, gffm_stream_t stream);
+/* z = A*x mod N (stripe_mul! vector form, stripe_mul.jl:82-168; mul!(z, A, x),
+ * CuModMatrix.jl:816-836).  Vectors are contiguous. */
+GFFM_API int gffm_matvec_plain_f64(int64_t m, int64_t k, const double *A, int64_t lda, const double *x, double *z,
+                          int64_t N, int64_t stripe, gffm_stream_t stream);
+GFFM_API int gffm_matvec_plain_f32(int64_t m, int64_t k, const float *A, int64_t lda, const float *x, float *z,
+                          int64_t N, int64_t stripe, gffm_stream_t stream);
+
+/* ---- limb tensor-core modular GEMM ---------------------------------------
+ * Same contract as gffm_matmul_plain_* (replaces stripe_mul! / mul! / * /
+ * mat_mul_gpu_type / mat_mul_type_inplace!, mat_mul_gpu_direct.jl:8-85, for
+ * 2 <= N < 2^26) but exact for every k: residues are centred, split into
+ * balanced base-2^7 digits held in fp16, multiplied on the tcgen05 tensor
+ * cores with fp32 accumulation (exact: every partial sum is an integer below
+ * 2^24), and recombined and reduced mod N in the epilogue.  Inputs may hold
+ * any integer value (they are reduced mod N first), so a modulus override
+ * (mat_mul_gpu_type(A, B, mod_N)) is a different N on the same buffers.
+ * Workspace: gffm_matmul_limb_workspace_size bytes, or NULL. */
+GFFM_API int gffm_matmul_limb_workspace_size(int64_t m, int64_t n, int64_t k, int64_t N, size_t *bytes);
+GFFM_API int gffm_matmul_limb_f64(int64_t m, int64_t n, int64_t k, const double *A, int64_t lda, const double *B,
+                         int64_t ldb, double *C, int64_t ldc, int64_t N, void *workspace, size_t workspace_bytes,
+                         gffm_stream_t stream);
+GFFM_API int gffm_matmul_limb_f32(int64_t m, int64_t n, int64_t k, const float *A, int64_t lda, const float *B,
+                         int64_t ldb, float *C, int64_t ldc, int64_t N, void *workspace, size_t workspace_bytes,
+                         gffm_stream_t stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GFFM_H */

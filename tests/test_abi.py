@@ -1,0 +1,63 @@
+"""CPU tests of the C ABI: the library loads, exports every symbol the header
+declares, and rejects bad arguments on the host before touching a device."""
+import ctypes
+import os
+import re
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "gffm.h")
+
+
+@pytest.fixture(scope="module")
+def lib():
+    import gffm
+    gffm.build()
+    return gffm.load_library()
+
+
+def declared_symbols():
+    text = open(HEADER).read()
+    return sorted(set(re.findall(r"GFFM_API\s+[\w\s\*]*?\b(gffm_\w+)\s*\(", text)))
+
+
+def test_header_declares_entry_points():
+    syms = declared_symbols()
+    assert "gffm_matmul_limb_f64" in syms and "gffm_matmul_plain_f64" in syms
+    assert len(syms) >= 20
+
+
+def test_library_exports_every_declared_symbol(lib):
+    missing = [s for s in declared_symbols() if not hasattr(lib, s)]
+    assert missing == []
+
+
+def test_python_binding_covers_header():
+    from gffm import _lib
+    assert sorted(_lib.SIGNATURES) == declared_symbols()
+
+
+def test_version_and_stripe_bound(lib):
+    assert lib.gffm_version().startswith(b"gffm-gb300")
+    out = ctypes.c_int64(0)
+    assert lib.gffm_find_max_stripe_ops(53, 67108859, ctypes.byref(out)) == 0 and out.value == 1
+    assert lib.gffm_find_max_stripe_ops(53, 65521, ctypes.byref(out)) == 0 and out.value == 2098175
+    assert lib.gffm_find_max_stripe_ops(53, 33554393, ctypes.byref(out)) == 0 and out.value == 7
+
+
+def test_host_side_argument_errors(lib):
+    # negative size / bad modulus are refused before any device work
+    st = lib.gffm_matmul_limb_f64(-1, 4, 4, None, 4, None, 4, None, 4, 7, None, 0, None)
+    assert st == 1
+    st = lib.gffm_matmul_limb_f64(4, 4, 4, None, 4, None, 4, None, 4, 2 ** 26, None, 0, None)
+    assert st == 3 and b"2^26" in lib.gffm_last_error_string()
+    st = lib.gffm_matmul_plain_f64(4, 4, 4, None, 4, None, 4, None, 4, 2 ** 30, 0, None)
+    assert st == 4 and b"cannot perform a single multiplication" in lib.gffm_last_error_string()
+    st = lib.gffm_matmul_plain_f32(4, 4, 4, None, 4, None, 4, None, 4, 2 ** 13, 0, None)
+    assert st == 4
+    st = lib.gffm_matmul_plain_f64(4, 4, 4, None, 2, None, 4, None, 4, 7, 0, None)
+    assert st == 1
+    ws = ctypes.c_size_t(0)
+    assert lib.gffm_matmul_limb_workspace_size(8192, 8192, 8192, 67108859, ctypes.byref(ws)) == 0
+    assert ws.value == 4 * (8192 + 8192) * 8192 * 2

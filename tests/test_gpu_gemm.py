@@ -1,0 +1,257 @@
+"""GPU parity tests: modular GEMM (limb tensor-core and plain paths), GEMV and
+the elementwise kernels, against the oracle and the reference's known-answer
+vectors.  Bar: bit-exact equality on every output element."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+HERE = os.path.dirname(os.path.abspath(__file__))
+P26 = 67108859
+P25 = 33554393
+
+
+def kat(op):
+    with open(os.path.join(HERE, "golden", "reference_kat.json")) as f:
+        return [c for c in json.load(f)["cases"] if c["op"] == op]
+
+
+def status_ok(gffm):
+    assert gffm.load_library().gffm_device_status(None) == 0
+
+
+def as_int(M):
+    return np.rint(M.Array()).astype(np.int64)
+
+
+@pytest.mark.parametrize("case", kat("matmul") + kat("matmul_override"), ids=lambda c: c["src"])
+@pytest.mark.parametrize("method", ["limb", "plain"])
+def test_kat_matmul(gffm, case, method):
+    Ns = case.get("N_storage", case["N"])
+    A = gffm.CuModMatrix(case["A"], Ns, elem_type=torch.float64)
+    B = gffm.CuModMatrix(case["B"], Ns, elem_type=torch.float64)
+    C = gffm.mat_mul_gpu_type(A, B, case["N"] if "N_storage" in case else -1, method=method)
+    assert as_int(C).tolist() == case["expected"]
+    if "N_storage" not in case:
+        C2 = A * B
+        assert as_int(C2).tolist() == case["expected"]
+    status_ok(gffm)
+
+
+@pytest.mark.parametrize("elem", ["f32", "f64"])
+def test_kat_elementwise(gffm, elem):
+    dt = torch.float32 if elem == "f32" else torch.float64
+    ops = {"add": gffm.add_, "sub": gffm.sub_, "elementwise_mul": gffm.elementwise_multiply_}
+    for op, fn in ops.items():
+        for c in kat(op):
+            A = gffm.CuModMatrix(c["A"], 10 ** 6, mod=False, elem_type=dt)
+            B = gffm.CuModMatrix(c["B"], 10 ** 6, mod=False, elem_type=dt)
+            C = gffm.zeros(dt, *A.size, c["N"])
+            fn(C, A, B, mod_N=c["N"]) if op != "elementwise_mul" else fn(C, A, B, c["N"])
+            assert as_int(C).tolist() == c["expected"], (op, c["src"])
+    sc = {"scalar_add": gffm.scalar_add_, "scalar_sub": gffm.scalar_sub_, "scalar_mul": gffm.scalar_mul_}
+    for op, fn in sc.items():
+        for c in kat(op):
+            A = gffm.CuModMatrix(c["A"], 10 ** 6, mod=False, elem_type=dt)
+            C = gffm.zeros(dt, *A.size, c["N"])
+            fn(C, A, c["s"], c["N"])
+            assert as_int(C).tolist() == c["expected"], (op, c["src"])
+    for c in kat("negate"):
+        A = gffm.CuModMatrix(c["A"], c["N"], elem_type=dt)
+        C = gffm.zeros(dt, *A.size, c["N"])
+        gffm.negate_(C, A)
+        assert as_int(C).tolist() == c["expected"]
+        assert as_int(-A).tolist() == c["expected"]
+    for c in kat("mod"):
+        A = gffm.CuModMatrix(c["A"], 10 ** 6, mod=False, elem_type=dt)
+        gffm.mod_elements_(A, c["N"])
+        assert as_int(A).tolist() == c["expected"]
+    for c in kat("fill"):
+        F = gffm.zeros(dt, *c["shape"], c["N"])
+        gffm.fill_(F, c["s"])
+        assert as_int(F).tolist() == c["expected"]
+    status_ok(gffm)
+
+
+def test_operators_match_reference_formulas(gffm):
+    A_data = np.array([[1, 2, 3], [4, 5, 6], [7, 8, 9]])
+    B_data = np.array([[9, 8, 7], [6, 5, 4], [3, 2, 1]])
+    A = gffm.CuModMatrix(A_data, 11)
+    B = gffm.CuModMatrix(B_data, 11)
+    assert (as_int(A + B) == (A_data + B_data) % 11).all()
+    assert (as_int(A - B) == (A_data - B_data) % 11).all()
+    assert (as_int(A * B) == (A_data @ B_data) % 11).all()
+    assert (as_int(3 + A) == (3 + A_data) % 11).all()
+    assert (as_int(A - 3) == (A_data - 3) % 11).all()
+    assert (as_int(3 * A) == (3 * A_data) % 11).all()
+    assert (as_int(A * -1) == (-A_data) % 11).all()
+    G_data = np.array([[1, 2, 3], [0, 1, 4], [5, 6, 0]])
+    G = gffm.CuModMatrix(G_data, 11)
+    assert (as_int(G ** 2) == (G_data @ G_data) % 11).all()
+    assert (as_int(G ** 0) == np.eye(3, dtype=np.int64)).all()
+    status_ok(gffm)
+
+
+# moduli at each digit-count boundary of the limb path, plus the benchmark primes
+LIMB_MODULI = [2, 7, 127, 128, 16255, 16256, 65521, 2080639, 2080640, P25, P26, 2 ** 26 - 1]
+SHAPES = [(1, 1, 1), (5, 7, 3), (129, 65, 100), (130, 200, 1025), (64, 64, 4160), (300, 70, 1344)]
+
+
+def patterns(rng, N, m, n, k):
+    yield "uniform", rng.integers(0, N, size=(m, k)), rng.integers(0, N, size=(k, n))
+    # largest centred magnitudes: every digit near +-64, partial sums at the exactness bound
+    hi = (N - 1) // 2 if N > 2 else 1
+    lo = (N + 1) // 2 if N > 2 else 1
+    yield "all_hi", np.full((m, k), hi), np.full((k, n), hi)
+    yield "hi_lo", np.full((m, k), hi), np.full((k, n), lo)
+    yield "mixed", np.where(rng.random((m, k)) < 0.5, hi, lo), np.where(rng.random((k, n)) < 0.5, lo, hi)
+
+
+@pytest.mark.parametrize("N", LIMB_MODULI)
+@pytest.mark.parametrize("shape", SHAPES, ids=lambda s: "x".join(map(str, s)))
+def test_limb_gemm_matches_oracle(gffm, N, shape):
+    rng = np.random.default_rng(N * 7 + shape[2])
+    m, n, k = shape
+    for name, A, B in patterns(rng, N, m, n, k):
+        Ag = gffm.CuModMatrix(A, N, elem_type=torch.float64)
+        Bg = gffm.CuModMatrix(B, N, elem_type=torch.float64)
+        C = gffm.mat_mul_gpu_type(Ag, Bg, method="limb")
+        want = oracle.matmul(A, B, N)
+        got = as_int(C)
+        assert np.array_equal(got, want), "%s: %d mismatches" % (name, int((got != want).sum()))
+    status_ok(gffm)
+
+
+@pytest.mark.parametrize("N", [11, 2 ** 11, 11 ** 3, 4093])
+def test_limb_gemm_f32_storage(gffm, N):
+    rng = np.random.default_rng(N)
+    A = rng.integers(0, N, size=(100, 100))
+    B = rng.integers(0, N, size=(100, 100))
+    A[4, 4] = N - 5
+    B[94, 94] = N - 23 if N > 23 else 0
+    Ag = gffm.CuModMatrix(A, N, elem_type=torch.float32)
+    Bg = gffm.CuModMatrix(B, N, elem_type=torch.float32)
+    C = gffm.zeros(torch.float32, 100, 100, N)
+    gffm.mul_(C, Ag, Bg, method="limb")
+    assert np.array_equal(as_int(C), oracle.matmul(A, B, N))
+    status_ok(gffm)
+
+
+@pytest.mark.parametrize("N,elem", [(2 ** 11, "f32"), (11 ** 3, "f32"), (65521, "f64"), (P25, "f64"), (P26, "f64")])
+def test_plain_gemm_matches_oracle(gffm, N, elem):
+    # stripe_mul_test.jl:2-50 pattern: random entries with injected large residues
+    dt = torch.float32 if elem == "f32" else torch.float64
+    rng = np.random.default_rng(N)
+    for (m, n, k) in [(100, 100, 100), (77, 130, 257)]:
+        A = rng.integers(0, N, size=(m, k))
+        B = rng.integers(0, N, size=(k, n))
+        A[4, 4] = N - 5
+        B[min(94, k - 1), min(94, n - 1)] = N - 23
+        Ag = gffm.CuModMatrix(A, N, elem_type=dt)
+        Bg = gffm.CuModMatrix(B, N, elem_type=dt)
+        C = gffm.zeros(dt, m, n, N)
+        gffm.stripe_mul_(C, Ag, Bg)
+        assert np.array_equal(as_int(C), oracle.matmul(A, B, N))
+    status_ok(gffm)
+
+
+@pytest.mark.parametrize("N,elem", [(11 ** 3, "f32"), (7 ** 4, "f32"), (65521, "f64"), (P26, "f64")])
+def test_plain_matvec_matches_oracle(gffm, N, elem):
+    dt = torch.float32 if elem == "f32" else torch.float64
+    rng = np.random.default_rng(N + 1)
+    m, k = 3003, 1000
+    A = rng.integers(0, N, size=(m, k))
+    x = rng.integers(0, N, size=(k,))
+    A[4, 4] = N - 5
+    z = gffm.zeros(dt, m, N)
+    gffm.mul_(z, gffm.CuModMatrix(A, N, elem_type=dt), gffm.CuModVector(x, N, elem_type=dt))
+    want = oracle.matmul(A, x.reshape(-1, 1), N).reshape(-1)
+    assert np.array_equal(np.rint(z.Array()).astype(np.int64), want)
+    status_ok(gffm)
+
+
+def test_limb_and_plain_agree_medium(gffm):
+    rng = np.random.default_rng(99)
+    m = n = k = 640
+    A = rng.integers(0, P26, size=(m, k))
+    B = rng.integers(0, P26, size=(k, n))
+    Ag = gffm.CuModMatrix(A, P26, elem_type=torch.float64)
+    Bg = gffm.CuModMatrix(B, P26, elem_type=torch.float64)
+    C1 = gffm.mat_mul_gpu_type(Ag, Bg, method="limb")
+    C2 = gffm.mat_mul_gpu_type(Ag, Bg, method="plain")
+    assert np.array_equal(as_int(C1), as_int(C2))
+    assert np.array_equal(as_int(C1), oracle.matmul(A, B, P26))
+    status_ok(gffm)
+
+
+def test_limb_gemm_8192_cube_properties(gffm):
+    """8192^3 mod p26 (the benchmark size): Freivalds' check C x = A (B x) on two
+    random vectors, plus exact oracle values for sampled rows and columns."""
+    n = 8192
+    g = torch.Generator(device="cuda")
+    g.manual_seed(1234)
+    A = gffm.rand(torch.float64, n, n, P26, generator=g)
+    B = gffm.rand(torch.float64, n, n, P26, generator=g)
+    C = gffm.mat_mul_gpu_type(A, B, method="limb")
+    torch.cuda.synchronize()
+    Ah, Bh, Ch = as_int(A), as_int(B), as_int(C)
+    rng = np.random.default_rng(5)
+    for _ in range(2):
+        x = rng.integers(0, P26, size=(n, 1))
+        lhs = oracle.matmul(Ch, x, P26)
+        rhs = oracle.matmul(Ah, oracle.matmul(Bh, x, P26), P26)
+        assert np.array_equal(lhs, rhs)
+    rows = rng.integers(0, n, size=4)
+    cols = rng.integers(0, n, size=4)
+    assert np.array_equal(Ch[rows, :], oracle.matmul(Ah[rows, :], Bh, P26))
+    assert np.array_equal(Ch[:, cols], oracle.matmul(Ah, Bh[:, cols], P26))
+    status_ok(gffm)
+
+
+def test_limb_gemm_caller_workspace_and_ld(gffm):
+    """Caller-provided workspace and leading dimensions larger than the padding."""
+    import ctypes
+    rng = np.random.default_rng(3)
+    m, n, k, N = 100, 90, 333, 65521
+    A = rng.integers(0, N, size=(m, k))
+    B = rng.integers(0, N, size=(k, n))
+    lda, ldb, ldc = m + 40, k + 8, m + 3
+    Ad = torch.zeros((k, lda), dtype=torch.float64, device="cuda")
+    Bd = torch.zeros((n, ldb), dtype=torch.float64, device="cuda")
+    Cd = torch.full((n, ldc), -1.0, dtype=torch.float64, device="cuda")
+    Ad[:, :m] = torch.from_numpy(A.T.astype(np.float64)).cuda()
+    Bd[:, :k] = torch.from_numpy(B.T.astype(np.float64)).cuda()
+    L = gffm.load_library()
+    ws = ctypes.c_size_t(0)
+    assert L.gffm_matmul_limb_workspace_size(m, n, k, N, ctypes.byref(ws)) == 0
+    buf = torch.empty(ws.value, dtype=torch.uint8, device="cuda")
+    st = L.gffm_matmul_limb_f64(m, n, k, Ad.data_ptr(), lda, Bd.data_ptr(), ldb, Cd.data_ptr(), ldc, N,
+                                buf.data_ptr(), ws.value, None)
+    assert st == 0
+    torch.cuda.synchronize()
+    got = Cd.cpu().numpy().T
+    assert np.array_equal(np.rint(got[:m, :]).astype(np.int64), oracle.matmul(A, B, N))
+    assert (got[m:, :] == -1.0).all()           # rows past m untouched
+    small = torch.empty(16, dtype=torch.uint8, device="cuda")
+    assert L.gffm_matmul_limb_f64(m, n, k, Ad.data_ptr(), lda, Bd.data_ptr(), ldb, Cd.data_ptr(), ldc, N,
+                                  small.data_ptr(), 16, None) == 5
+    status_ok(gffm)
+
+
+def test_empty_and_degenerate(gffm):
+    N = P26
+    A = gffm.zeros(torch.float64, 5, 0, N)
+    B = gffm.zeros(torch.float64, 0, 7, N)
+    C = gffm.zeros(torch.float64, 5, 7, N)
+    gffm.fill_(C, 3)
+    gffm.mul_(C, A, B, method="limb")
+    assert (as_int(C) == 0).all()
+    Z = gffm.zeros(torch.float64, 0, 4, N)
+    gffm.mul_(gffm.zeros(torch.float64, 0, 3, N), Z, gffm.zeros(torch.float64, 4, 3, N), method="limb")
+    status_ok(gffm)
