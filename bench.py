@@ -1,0 +1,441 @@
+"""Benchmark: bit-exact modular GEMM 8192 x 8192 x 8192 mod 67108859 (the largest
+prime below 2^26) on one GB300, through the library's C ABI.
+
+A step is one C = A*B mod p of two resident Float64 CuModMatrix operands on
+the limb tensor-core path (digit split of A and B + the tcgen05 GEMM with its
+fused recombination / Barrett epilogue).  Operands are 2 x 541 MB, larger than
+the 129 MB L2, so no flush is needed between steps.
+
+Printed JSON line (one, from rank 0):
+  value        whole-job Gop/s (2*m*n*k per step, all ranks)
+  e2e          the same metric through the C ABI with host buffers: every step
+               copies A and B from pinned host memory and C back
+  roofline     the tcgen05 GEMM kernel's tensor FLOP/s (digit products) vs the
+               measured dense bf16/fp16 peak; traffic from the committed ncu summary
+  plain_fp64   the plain path (the reference's Float64 method) on the same GPU
+  pluq         PLUQ timings when the elimination is built (see --pluq)
+  cpu_baseline the oracle (exact C restatement) on the host cores, bounded sample
+--impl reference times the reference's CPU path (the oracle port; the Julia
+reference cannot run here) on the same workload and metric.
+"""
+import argparse
+import ctypes
+import json
+import os
+import re
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG_DIR = os.path.join(ROOT, "gpufinitefieldmatrices.jl_gb300")
+for _p in (ROOT, PKG_DIR):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+P26 = 67108859
+M = N = K = 8192
+METRIC = "bit-exact mod-p GEMM Gop/s & PLUQ time: limb tensor-core vs plain FP64, same GB300"
+WORKLOAD = "modular GEMM 8192x8192x8192 mod 67108859, Float64 CuModMatrix operands, limb tensor-core path"
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=60)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--no-plain", action="store_true", help="skip the plain FP64 comparison")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--pluq", type=int, default=-1, help="PLUQ size to time (-1: default when available, 0: skip)")
+    ap.add_argument("--size", type=int, default=8192, help="m = n = k (8192 is the benchmark workload)")
+    return ap.parse_args()
+
+
+# ---------------------------------------------------------------------------
+# clocks sampled during the timed region
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.thread.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return d.get("bf16_tflops"), d.get("hbm_gbs"), "measured"
+    except (OSError, ValueError):
+        return 1900.0, 6800.0, "fallback"
+
+
+def profiled_traffic():
+    """dram bytes per launch of the limb GEMM kernel, from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "limb_gemm_8192_mod_p26.md")
+    try:
+        txt = open(path).read()
+    except OSError:
+        return None
+    m = re.search(r"dram_bytes_per_launch:\s*([0-9.eE+]+)", txt)
+    return float(m.group(1)) if m else None
+
+
+# ---------------------------------------------------------------------------
+# CPU side (oracle): cpu_baseline and the reference arm
+# ---------------------------------------------------------------------------
+def cpu_sample(target_s=12.0):
+    """Time the oracle's exact matmul on a row sample of the 8192^3 workload with
+    every host thread; returns (Gop/s, threads, description)."""
+    import numpy as np
+    import oracle
+    threads = os.cpu_count() or 1
+    rng = np.random.default_rng(7)
+    B = np.asfortranarray(rng.integers(0, P26, size=(K, N)))
+    rows = 16
+    while True:
+        A = np.asfortranarray(rng.integers(0, P26, size=(rows, K)))
+        t0 = time.perf_counter()
+        oracle.matmul(A, B, P26, threads)
+        dt = time.perf_counter() - t0
+        if dt >= target_s / 4 or rows >= M:
+            break
+        rows = min(M, rows * max(2, int(target_s / 4 / max(dt, 1e-3))))
+    gops = 2.0 * rows * N * K / dt / 1e9
+    return gops, threads, "%d x %d x %d row slice of the workload (exact Int128-free uint64 C, OpenMP)" % (rows, N, K)
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    import numpy as np
+    import oracle
+    oracle.build()
+    threads = os.cpu_count() or 1
+    rng = np.random.default_rng(11)
+    B = np.asfortranarray(rng.integers(0, P26, size=(K, N)))
+    # calibrate one step to ~2 s of CPU work
+    rows = 8
+    while True:
+        A = np.asfortranarray(rng.integers(0, P26, size=(rows, K)))
+        t0 = time.perf_counter()
+        oracle.matmul(A, B, P26, threads)
+        dt = time.perf_counter() - t0
+        if dt > 1.0 or rows >= 1024:
+            break
+        rows *= 2
+    A = np.asfortranarray(rng.integers(0, P26, size=(rows, K)))
+    for _ in range(args.warmup):
+        oracle.matmul(A, B, P26, threads)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        oracle.matmul(A, B, P26, threads)
+    dt = time.perf_counter() - t0
+    gops = 2.0 * rows * N * K * args.steps / dt / 1e9
+    sample = "each step: %d x %d x %d row slice of the 8192^3 workload" % (rows, N, K)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(gops, 3), "unit": "Gop/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(dt / args.steps * 1e3, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "m": M, "n": N, "k": K, "modulus": P26},
+        "cpu_baseline": {"value": round(gops, 3), "unit": "Gop/s", "cores": threads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": round(gops, 3), "unit": "Gop/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "GPUFiniteFieldMatrices.jl is Julia (CUDA.jl); no Julia toolchain exists on this box, so its CPU "
+                "path (Int64 matmul then mod) is stood in for by the exact C restatement in oracle/",
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+def run_ours(args):
+    import torch
+    import gffm
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    else:
+        torch.cuda.set_device(0)
+    gffm.build()
+    L = gffm.load_library()
+    dev = torch.device("cuda", local if world > 1 else 0)
+    stream = torch.cuda.current_stream()
+    sp = ctypes.c_void_p(stream.cuda_stream)
+
+    g = torch.Generator(device=dev)
+    g.manual_seed(1234 + rank)
+    A = gffm.rand(torch.float64, M, K, P26, generator=g)
+    B = gffm.rand(torch.float64, K, N, P26, generator=g)
+    C = gffm.zeros(torch.float64, M, N, P26)
+    ws = ctypes.c_size_t(0)
+    assert L.gffm_matmul_limb_workspace_size(M, N, K, P26, ctypes.byref(ws)) == 0
+    wbuf = torch.empty(ws.value, dtype=torch.uint8, device=dev)
+
+    def step(ev=None):
+        if ev is not None:
+            L.gffm_profile_next_kernel(ctypes.c_void_p(ev[0].cuda_event), ctypes.c_void_p(ev[1].cuda_event))
+        st = L.gffm_matmul_limb_f64(M, N, K, A.data.data_ptr(), A.ld, B.data.data_ptr(), B.ld, C.data.data_ptr(),
+                                    C.ld, P26, wbuf.data_ptr(), ws.value, sp)
+        if st != 0:
+            raise RuntimeError(L.gffm_last_error_string().decode())
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    for _ in range(max(args.warmup, 3)):
+        step()
+    torch.cuda.synchronize()
+    # correctness spot check of the warm-up output (Freivalds on one vector, exact on the host)
+    spot_ok = freivalds(A, B, C)
+
+    kev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    for a, b in kev:        # torch creates the CUDA event on its first record
+        a.record()
+        b.record()
+    clocks = ClockSampler(local if world > 1 else 0)
+    barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    time.sleep(0.3)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for i in range(args.steps):
+        step(kev[i])
+    e1.record()
+    torch.cuda.synchronize()
+    barrier()
+    clk = clocks.stop()
+    ms = e0.elapsed_time(e1)
+    kern_ms = [a.elapsed_time(b) for a, b in kev]
+    if dist is not None:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    ops_step = 2.0 * M * N * K
+    value = ops_step * args.steps * world / (ms / 1e3) / 1e9
+    st = L.gffm_device_status(sp)
+    if st != 0:
+        raise RuntimeError("device status %d" % st)
+
+    # roofline of the tcgen05 GEMM kernel: digit-product tensor FLOPs per launch
+    Ld = 4
+    Mp, Np, Kp = (M + 127) // 128 * 128, (N + 63) // 64 * 64, (K + 63) // 64 * 64
+    tflop = 2.0 * Ld * Ld * Mp * Np * Kp / 1e12
+    kavg = statistics.mean(kern_ms)
+    peak, hbm_peak, peak_kind = measured_peaks()
+    achieved = tflop / (kavg / 1e3)
+    roofline = {"bound": "tensor", "kernel": "limb::k_gemm_limb<4, EPI_STORE_F64>", "achieved": round(achieved, 1),
+                "peak": peak, "unit": "TFLOP/s", "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
+                "traffic": profiled_traffic(), "kernel_ms": round(kavg, 4),
+                "algorithmic": "16 fp16 digit-pair products per modular MAC: 2*16*8192^3 FLOP per launch"}
+
+    out = {
+        "metric": METRIC, "value": round(value, 1), "unit": "Gop/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 4), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f16", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "m": M, "n": N, "k": K, "modulus": P26, "digits": Ld,
+                   "l2": "inputs larger than L2 (2 x 541 MB Float64 operands); no flush",
+                   "parallelism": "replicas x%d" % world},
+        "clocks": clk, "gpu_launches": 3 * args.steps, "roofline": roofline, "spot_check_ok": spot_ok,
+    }
+
+    if not args.no_e2e:
+        out["e2e"] = e2e_run(args, L, sp, dev, world, dist)
+    if not args.no_plain:
+        out["plain_fp64"] = plain_run(L, sp, dev)
+        out["plain_fp64"]["limb_speedup"] = round(value / world / out["plain_fp64"]["value"], 1)
+    if args.pluq != 0:
+        pl = pluq_run(args, L, sp, dev)
+        if pl is not None:
+            out["pluq"] = pl
+    if rank == 0 and not args.no_cpu:
+        gops, threads, desc = cpu_sample()
+        out["cpu_baseline"] = {"value": round(gops, 3), "unit": "Gop/s", "cores": threads, "kind": "port",
+                               "sample": desc}
+    if dist is not None:
+        dist.barrier()
+        dist.destroy_process_group()
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+
+
+def freivalds(A, B, C):
+    import numpy as np
+    import oracle
+    rng = np.random.default_rng(3)
+    x = rng.integers(0, P26, size=(K, 1))
+    Ah = np.rint(A.Array()).astype(np.int64)
+    Bh = np.rint(B.Array()).astype(np.int64)
+    Ch = np.rint(C.Array()).astype(np.int64)
+    return bool(np.array_equal(oracle.matmul(Ch, x, P26), oracle.matmul(Ah, oracle.matmul(Bh, x, P26), P26)))
+
+
+def e2e_run(args, L, sp, dev, world, dist):
+    """C = A*B mod p from pinned host Float64 buffers (padded CuModMatrix layout):
+    H2D of A and B, the C ABI call, D2H of C -- every step."""
+    import torch
+    pad = 32
+    shapeA = (K + pad, M + pad)
+    shapeB = (N + pad, K + pad)
+    shapeC = (N + pad, M + pad)
+    g = torch.Generator()
+    g.manual_seed(77)
+    hA = torch.zeros(shapeA, dtype=torch.float64).pin_memory()
+    hB = torch.zeros(shapeB, dtype=torch.float64).pin_memory()
+    hC = torch.zeros(shapeC, dtype=torch.float64).pin_memory()
+    hA[:K, :M] = torch.randint(0, P26, (K, M), generator=g).double()
+    hB[:N, :K] = torch.randint(0, P26, (N, K), generator=g).double()
+    dA = torch.empty(shapeA, dtype=torch.float64, device=dev)
+    dB = torch.empty(shapeB, dtype=torch.float64, device=dev)
+    dC = torch.zeros(shapeC, dtype=torch.float64, device=dev)
+    ws = ctypes.c_size_t(0)
+    L.gffm_matmul_limb_workspace_size(M, N, K, P26, ctypes.byref(ws))
+    wbuf = torch.empty(ws.value, dtype=torch.uint8, device=dev)
+
+    def step():
+        dA.copy_(hA, non_blocking=True)
+        dB.copy_(hB, non_blocking=True)
+        st = L.gffm_matmul_limb_f64(M, N, K, dA.data_ptr(), M + pad, dB.data_ptr(), K + pad, dC.data_ptr(), M + pad,
+                                    P26, wbuf.data_ptr(), ws.value, sp)
+        assert st == 0
+        hC.copy_(dC, non_blocking=True)
+
+    steps = max(5, args.steps // 6)
+    for _ in range(3):
+        step()
+    torch.cuda.synchronize()
+    if dist is not None:
+        dist.barrier()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(steps):
+        step()
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    if dist is not None:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    h2d = hA.numel() * 8 + hB.numel() * 8
+    d2h = hC.numel() * 8
+    return {"value": round(2.0 * M * N * K * steps * world / (ms / 1e3) / 1e9, 1), "unit": "Gop/s",
+            "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "steps": steps,
+            "ms_per_step": round(ms / steps, 3), "gpu_launches": 3 * steps}
+
+
+def plain_run(L, sp, dev):
+    """The plain path (the reference's Float64 method, stripe width 1 at this modulus)
+    on a k-slice of the same workload; its time is linear in k."""
+    import torch
+    import gffm
+    ks = 512
+    g = torch.Generator(device=dev)
+    g.manual_seed(99)
+    A = gffm.rand(torch.float64, M, ks, P26, generator=g)
+    B = gffm.rand(torch.float64, ks, N, P26, generator=g)
+    C = gffm.zeros(torch.float64, M, N, P26)
+
+    def run():
+        st = L.gffm_matmul_plain_f64(M, N, ks, A.data.data_ptr(), A.ld, B.data.data_ptr(), B.ld, C.data.data_ptr(),
+                                     C.ld, P26, 0, sp)
+        assert st == 0
+
+    run()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(2):
+        run()
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / 2
+    return {"value": round(2.0 * M * N * ks / (ms / 1e3) / 1e9, 2), "unit": "Gop/s",
+            "sample": "8192 x 8192 x %d k-slice (time is linear in k)" % ks, "ms": round(ms, 2),
+            "stripe": 1}
+
+
+def pluq_run(args, L, sp, dev):
+    try:
+        import gffm
+        from gffm import elimination  # noqa: F401
+    except ImportError:
+        return None
+    return elimination.bench_pluq(args.pluq, sp, dev)
+
+
+def main():
+    global M, N, K, WORKLOAD
+    args = parse_args()
+    if args.size != 8192:
+        M = N = K = args.size
+        WORKLOAD = WORKLOAD.replace("8192x8192x8192", "%dx%dx%d" % (M, N, K))
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -22,6 +22,17 @@ int check_device();                             // GFFM_OK on an sm_103 device
 int *device_error_flag();                       // device address of the error word
 cudaStream_t as_stream(gffm_stream_t s);
 
+// Events armed by gffm_profile_next_kernel: record around the next main kernel.
+struct ProfileHook {
+    cudaEvent_t start = nullptr, stop = nullptr;
+    void before(cudaStream_t s) { if (start) cudaEventRecord(start, s); }
+    void after(cudaStream_t s) {
+        if (stop) cudaEventRecord(stop, s);
+        start = stop = nullptr;
+    }
+};
+ProfileHook &profile_hook();
+
 // Scratch allocation: caller buffer, or stream-ordered allocation released by ~Scratch.
 struct Scratch {
     void *ptr = nullptr;

@@ -28,6 +28,9 @@ int cuda_error(cudaError_t e, const char *what) {
 
 cudaStream_t as_stream(gffm_stream_t s) { return reinterpret_cast<cudaStream_t>(s); }
 
+static thread_local ProfileHook tl_hook;
+ProfileHook &profile_hook() { return tl_hook; }
+
 namespace {
 constexpr int kMaxDevices = 64;
 struct DevInfo {
@@ -140,6 +143,12 @@ int gffm_device_status(gffm_stream_t stream) {
         GFFM_CUDA(cudaMemcpy(flag, &zero, sizeof(int), cudaMemcpyHostToDevice));
         return gffm::set_error(GFFM_ERR_TIMEOUT, "a device-side wait gave up (code %d); results are invalid", h);
     }
+    return GFFM_OK;
+}
+
+int gffm_profile_next_kernel(void *start_event, void *stop_event) {
+    gffm::profile_hook().start = static_cast<cudaEvent_t>(start_event);
+    gffm::profile_hook().stop = static_cast<cudaEvent_t>(stop_event);
     return GFFM_OK;
 }
 

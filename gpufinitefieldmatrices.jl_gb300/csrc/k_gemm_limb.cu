@@ -102,7 +102,9 @@ template <int L, int EPI>
 static int launch_gemm_L(const CUtensorMap &ta, const CUtensorMap &tb, const Params &p, int grid, cudaStream_t s) {
     auto kern = k_gemm_limb<L, EPI>;
     GFFM_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, Cfg<L>::SMEM_BYTES));
+    gffm::profile_hook().before(s);
     kern<<<grid, NUM_THREADS, Cfg<L>::SMEM_BYTES, s>>>(ta, tb, p);
+    gffm::profile_hook().after(s);
     GFFM_LAUNCH_CHECK("k_gemm_limb");
     return GFFM_OK;
 }

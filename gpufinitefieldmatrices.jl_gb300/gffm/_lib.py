@@ -23,6 +23,7 @@ SIGNATURES = {
     "gffm_version": (ctypes.c_char_p, []),
     "gffm_last_error_string": (ctypes.c_char_p, []),
     "gffm_device_status": (_INT, [_P]),
+    "gffm_profile_next_kernel": (_INT, [_P, _P]),
     "gffm_find_max_stripe_ops": (_INT, [_INT, _I64, _PI64]),
     "gffm_matmul_plain_f64": (_INT, [_I64, _I64, _I64, _P, _I64, _P, _I64, _P, _I64, _I64, _I64, _P]),
     "gffm_matmul_plain_f32": (_INT, [_I64, _I64, _I64, _P, _I64, _P, _I64, _P, _I64, _I64, _I64, _P]),

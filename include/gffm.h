@@ -68,6 +68,13 @@ GFFM_API const char *gffm_last_error_string(void);
  * GFFM_ERR_TIMEOUT.  (No reference counterpart.) */
 GFFM_API int gffm_device_status(gffm_stream_t stream);
 
+/* Kernel timing hook (no reference counterpart): the next call on this thread
+ * that launches the library's main tensor-core kernel (the limb GEMM, or a
+ * trailing update of the elimination) records `start_event` just before and
+ * `stop_event` just after that kernel, on the call's stream.  The events are
+ * cudaEvent_t handles created by the caller; the hook is then cleared. */
+GFFM_API int gffm_profile_next_kernel(void *start_event, void *stop_event);
+
 /* find_max_stripe_ops(type, N) (src/CuModMatrix/kernel_mul/stripe_mul.jl:13-27):
  * the number of products that can be summed exactly in the element type
  * before a reduction.  bits = 53 (Float64), 24 (Float32), 11 (Float16). */

@@ -104,17 +104,57 @@ void or_matmul(int64_t m, int64_t n, int64_t k,
         if (chunk < 1) chunk = 1;
         uint32_t *At = (uint32_t *)malloc(sizeof(uint32_t) * (size_t)m * (size_t)k);
         uint32_t *Bt = (uint32_t *)malloc(sizeof(uint32_t) * (size_t)n * (size_t)k);
-        for (int64_t p = 0; p < k; p++)
-            for (int64_t i = 0; i < m; i++) At[i * k + p] = (uint32_t)or_modi(A[i + p * lda], N);
-        for (int64_t j = 0; j < n; j++)
-            for (int64_t p = 0; p < k; p++) Bt[j * k + p] = (uint32_t)or_modi(B[p + j * ldb], N);
 #ifdef _OPENMP
         if (nthreads > 0) omp_set_num_threads(nthreads);
+#endif
+        /* operands as uint32 residues, both k-contiguous (A transposed, B as is) */
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static)
+#endif
+        for (int64_t i = 0; i < m; i++)
+            for (int64_t p = 0; p < k; p++) {
+                int64_t v = A[i + p * lda];
+                At[i * k + p] = (uint32_t)((v >= 0 && v < N) ? v : or_modi(v, N));
+            }
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static)
+#endif
+        for (int64_t j = 0; j < n; j++)
+            for (int64_t p = 0; p < k; p++) {
+                int64_t v = B[p + j * ldb];
+                Bt[j * k + p] = (uint32_t)((v >= 0 && v < N) ? v : or_modi(v, N));
+            }
+        /* 4 rows x 1 column per inner loop: each b[p] load feeds four products */
+#ifdef _OPENMP
 #pragma omp parallel for schedule(dynamic, 4)
 #endif
         for (int64_t j = 0; j < n; j++) {
             const uint32_t *b = Bt + j * k;
-            for (int64_t i = 0; i < m; i++) {
+            int64_t i = 0;
+            for (; i + 4 <= m; i += 4) {
+                const uint32_t *a0 = At + i * k, *a1 = a0 + k, *a2 = a1 + k, *a3 = a2 + k;
+                uint64_t r0 = 0, r1 = 0, r2 = 0, r3 = 0;
+                for (int64_t p0 = 0; p0 < k; p0 += (int64_t)chunk) {
+                    int64_t p1 = p0 + (int64_t)chunk < k ? p0 + (int64_t)chunk : k;
+                    uint64_t s0 = 0, s1 = 0, s2 = 0, s3 = 0;
+                    for (int64_t p = p0; p < p1; p++) {
+                        uint64_t bv = b[p];
+                        s0 += (uint64_t)a0[p] * bv;
+                        s1 += (uint64_t)a1[p] * bv;
+                        s2 += (uint64_t)a2[p] * bv;
+                        s3 += (uint64_t)a3[p] * bv;
+                    }
+                    r0 = (r0 + s0 % (uint64_t)N) % (uint64_t)N;
+                    r1 = (r1 + s1 % (uint64_t)N) % (uint64_t)N;
+                    r2 = (r2 + s2 % (uint64_t)N) % (uint64_t)N;
+                    r3 = (r3 + s3 % (uint64_t)N) % (uint64_t)N;
+                }
+                C[i + j * ldc] = (int64_t)r0;
+                C[i + 1 + j * ldc] = (int64_t)r1;
+                C[i + 2 + j * ldc] = (int64_t)r2;
+                C[i + 3 + j * ldc] = (int64_t)r3;
+            }
+            for (; i < m; i++) {
                 const uint32_t *a = At + i * k;
                 uint64_t res = 0;
                 for (int64_t p0 = 0; p0 < k; p0 += (int64_t)chunk) {
