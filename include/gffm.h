@@ -149,6 +149,28 @@ GFFM_API int gffm_matmul_limb_f32(int64_t m, int64_t n, int64_t k, const float *
                          int64_t ldb, float *C, int64_t ldc, int64_t N, void *workspace, size_t workspace_bytes,
                          gffm_stream_t stream);
 
+/* ---- limb GEMM without allocation -----------------------------------------
+ * No counterpart in the reference.  For callers that cannot allocate device
+ * memory when they multiply: a process whose HBM is already reserved by
+ * another allocator (a framework pool holding nearly the whole device) would
+ * get an out-of-memory error from the workspace allocation, and a pipeline
+ * that must not stall cannot accept the device-wide synchronization of
+ * cudaMalloc/cudaFree.  This variant of gffm_matmul_limb_f64 takes inputs and
+ * outputs only; its digit-plane scratch is a fixed array of
+ * gffm_matmul_limb_static_max_bytes() bytes (32 MiB) that the library keeps
+ * on every GPU that loads it until the process exits.  It calls no
+ * allocator.  A product whose digit planes need more scratch than that
+ * (gffm_matmul_limb_workspace_size) is rejected with GFFM_ERR_WORKSPACE.
+ * The first call on a device looks up the array's device address; make that
+ * first call before any stream capture on that device.  All calls share the
+ * array: calls that run concurrently on the GPU (e.g. on two streams) race on
+ * it, calls on one stream are safe.  Every call rewrites the scratch it uses,
+ * so nothing in it needs to start at zero. */
+GFFM_API int gffm_matmul_limb_static_max_bytes(size_t *bytes);
+GFFM_API int gffm_matmul_limb_static_f64(int64_t m, int64_t n, int64_t k, const double *A, int64_t lda,
+                                         const double *B, int64_t ldb, double *C, int64_t ldc, int64_t N,
+                                         gffm_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif
