@@ -14,3 +14,7 @@ from .cumod import (  # noqa: F401
     CuModArraySizeMismatchException, CuModArrayModulusMismatchException, CuModMatrixNotSquareException,
     CuModMatrixModulusNotPrimeException,
 )
+from .elimination import (  # noqa: F401,E402
+    pluq_gpu_kernel, lu_gpu_type, rref_gpu_type, apply_col_perm_, apply_col_inv_perm_, apply_col_perm,
+    apply_row_perm_, apply_row_inv_perm_, apply_row_perm, perm_array_to_matrix,
+)

@@ -32,6 +32,17 @@ SIGNATURES = {
     "gffm_matmul_limb_workspace_size": (_INT, [_I64, _I64, _I64, _I64, _PSZ]),
     "gffm_matmul_limb_f64": (_INT, [_I64, _I64, _I64, _P, _I64, _P, _I64, _P, _I64, _I64, _P, _SZ, _P]),
     "gffm_matmul_limb_f32": (_INT, [_I64, _I64, _I64, _P, _I64, _P, _I64, _P, _I64, _I64, _P, _SZ, _P]),
+    "gffm_elim_workspace_size": (_INT, [_I64, _I64, _I64, _PSZ]),
+    "gffm_pluq_f64": (_INT, [_I64, _I64, _P, _I64, _P, _I64, _P, _I64, _I64, _I64, _P, _P, _P, _P, _P, _P, _SZ, _P]),
+    "gffm_pluq_f32": (_INT, [_I64, _I64, _P, _I64, _P, _I64, _P, _I64, _I64, _I64, _P, _P, _P, _P, _P, _P, _SZ, _P]),
+    "gffm_lu_f64": (_INT, [_I64, _I64, _P, _I64, _P, _I64, _P, _I64, _I64, _P, _P, _P, _SZ, _P]),
+    "gffm_lu_f32": (_INT, [_I64, _I64, _P, _I64, _P, _I64, _P, _I64, _I64, _P, _P, _P, _SZ, _P]),
+    "gffm_rref_f64": (_INT, [_I64, _I64, _P, _I64, _P, _I64, _I64, _P, _P, _P, _SZ, _P]),
+    "gffm_rref_f32": (_INT, [_I64, _I64, _P, _I64, _P, _I64, _I64, _P, _P, _P, _SZ, _P]),
+    "gffm_apply_row_swaps_f64": (_INT, [_P, _I64, _I64, _I64, _P, _I64, _INT, _P]),
+    "gffm_apply_row_swaps_f32": (_INT, [_P, _I64, _I64, _I64, _P, _I64, _INT, _P]),
+    "gffm_apply_col_swaps_f64": (_INT, [_P, _I64, _I64, _I64, _P, _I64, _INT, _P]),
+    "gffm_apply_col_swaps_f32": (_INT, [_P, _I64, _I64, _I64, _P, _I64, _INT, _P]),
     "gffm_matmul_limb_static_max_bytes": (_INT, [_PSZ]),
     "gffm_matmul_limb_static_f64": (_INT, [_I64, _I64, _I64, _P, _I64, _P, _I64, _P, _I64, _I64, _P]),
 }

@@ -149,6 +149,72 @@ GFFM_API int gffm_matmul_limb_f32(int64_t m, int64_t n, int64_t k, const float *
                          int64_t ldb, float *C, int64_t ldc, int64_t N, void *workspace, size_t workspace_bytes,
                          gffm_stream_t stream);
 
+/* ---- elimination over Z/N, 2 <= N < 2^26 -----------------------------------
+ * Blocked right-looking elimination with the reference's exact step
+ * semantics; the trailing updates run on the limb tensor-core GEMM.  These
+ * calls synchronize `stream` (they return host data).  Workspace:
+ * gffm_elim_workspace_size bytes (l_cols = padded width of L; 0 for RREF),
+ * or NULL.  U / R may alias A.  Arithmetic follows the reference's mod_inv
+ * (extended Euclid) for the pivot inverses, so composite N behaves as the
+ * reference's algorithm does. */
+GFFM_API int gffm_elim_workspace_size(int64_t m, int64_t n, int64_t l_cols, size_t *bytes);
+
+/* pluq_gpu_kernel(A) -> (U, L, Perm_rows, Perm_cols)
+ * (src/CuModMatrix/rref_lu_pluq/pluq_kernels.jl:46-157): pivot = largest
+ * residue of the column below the current row (lowest row on ties); a zero
+ * column is swapped with the last column and skipped; U is unit upper with the
+ * pivot rows scaled by the pivot inverse; L (m x l_cols, the reference's L is
+ * (m+32) x (m+32)) holds the pivot values at (row, col) and the eliminated
+ * entries below.  row_swaps / col_swaps receive the swap stacks as 1-based
+ * (i, j) pairs (capacity 2*m and 2*n int64), in order.  GFFM_ERR_BOUNDS where
+ * the reference would index L out of bounds. */
+GFFM_API int gffm_pluq_f64(int64_t m, int64_t n, const double *A, int64_t lda, double *U, int64_t ldu, double *L,
+                           int64_t ldl, int64_t l_cols, int64_t N, int64_t *row_swaps, int64_t *n_row_swaps,
+                           int64_t *col_swaps, int64_t *n_col_swaps, int64_t *rank, void *workspace,
+                           size_t workspace_bytes, gffm_stream_t stream);
+GFFM_API int gffm_pluq_f32(int64_t m, int64_t n, const float *A, int64_t lda, float *U, int64_t ldu, float *L,
+                           int64_t ldl, int64_t l_cols, int64_t N, int64_t *row_swaps, int64_t *n_row_swaps,
+                           int64_t *col_swaps, int64_t *n_col_swaps, int64_t *rank, void *workspace,
+                           size_t workspace_bytes, gffm_stream_t stream);
+
+/* lu_gpu_type(A) -> (U, L, Perm) (intended API, test/Experiments/rref_gpu_type.jl:60-103):
+ * the same pivot rule without column swaps -- a zero column is skipped and
+ * L's column index is the pivot count.  L is m x m; perm (host, m int64)
+ * receives the 1-based original row index of each row of U. */
+GFFM_API int gffm_lu_f64(int64_t m, int64_t n, const double *A, int64_t lda, double *U, int64_t ldu, double *L,
+                         int64_t ldl, int64_t N, int64_t *perm, int64_t *rank, void *workspace,
+                         size_t workspace_bytes, gffm_stream_t stream);
+GFFM_API int gffm_lu_f32(int64_t m, int64_t n, const float *A, int64_t lda, float *U, int64_t ldu, float *L,
+                         int64_t ldl, int64_t N, int64_t *perm, int64_t *rank, void *workspace,
+                         size_t workspace_bytes, gffm_stream_t stream);
+
+/* rref_gpu_type(A) (intended API, test/Experiments/rref_gpu_type.jl:8-51;
+ * called by test/CuModMatrix/benchmark_test.jl:144): the reduced row echelon
+ * form mod N into R (unique for prime N).  pivot_cols (host, capacity
+ * min(m, n) int64, may be NULL) receives the 1-based pivot columns. */
+GFFM_API int gffm_rref_f64(int64_t m, int64_t n, const double *A, int64_t lda, double *R, int64_t ldr, int64_t N,
+                           int64_t *rank, int64_t *pivot_cols, void *workspace, size_t workspace_bytes,
+                           gffm_stream_t stream);
+GFFM_API int gffm_rref_f32(int64_t m, int64_t n, const float *A, int64_t lda, float *R, int64_t ldr, int64_t N,
+                           int64_t *rank, int64_t *pivot_cols, void *workspace, size_t workspace_bytes,
+                           gffm_stream_t stream);
+
+/* ---- swap-stack permutations (src/CuModMatrix/rref_lu_pluq/permutations.jl) --
+ * A is nrows x ncols, column-major; `swaps` is a HOST array of nswaps 1-based
+ * (i, j) pairs (the reference's Vector{Tuple{Int,Int}}), applied in order, or
+ * in reverse order when `inverse` is non-zero.  Indices are checked on the
+ * host (GFFM_ERR_BOUNDS).
+ * apply_row_perm! / apply_row_inv_perm! (:73-89) */
+GFFM_API int gffm_apply_row_swaps_f64(double *A, int64_t lda, int64_t nrows, int64_t ncols, const int64_t *swaps,
+                                      int64_t nswaps, int inverse, gffm_stream_t stream);
+GFFM_API int gffm_apply_row_swaps_f32(float *A, int64_t lda, int64_t nrows, int64_t ncols, const int64_t *swaps,
+                                      int64_t nswaps, int inverse, gffm_stream_t stream);
+/* apply_col_perm! / apply_col_inv_perm! (:11-27) */
+GFFM_API int gffm_apply_col_swaps_f64(double *A, int64_t lda, int64_t nrows, int64_t ncols, const int64_t *swaps,
+                                      int64_t nswaps, int inverse, gffm_stream_t stream);
+GFFM_API int gffm_apply_col_swaps_f32(float *A, int64_t lda, int64_t nrows, int64_t ncols, const int64_t *swaps,
+                                      int64_t nswaps, int inverse, gffm_stream_t stream);
+
 /* ---- limb GEMM without allocation -----------------------------------------
  * No counterpart in the reference.  For callers that cannot allocate device
  * memory when they multiply: a process whose HBM is already reserved by

@@ -49,6 +49,8 @@ def lib():
         L.or_matmul.argtypes = [_i64, _i64, _i64, _p, _i64, _p, _i64, _p, _i64, _i64, ctypes.c_int]
         L.or_pluq.restype = ctypes.c_int
         L.or_pluq.argtypes = [_i64, _i64, _p, _i64, _p, _i64, _i64, _i64, _p, _p, _p, _p, _p]
+        L.or_lu.restype = ctypes.c_int
+        L.or_lu.argtypes = [_i64, _i64, _p, _i64, _p, _i64, _i64, _p, _p]
         L.or_rref.restype = ctypes.c_int
         L.or_rref.argtypes = [_i64, _i64, _p, _i64, _i64, _p, _p]
         L.or_karatsuba_matmul.restype = None
@@ -114,6 +116,17 @@ def pluq(A, N, l_cols=None):
     rows = [tuple(int(v) for v in rs[i]) for i in range(nr.value)]
     cols = [tuple(int(v) for v in cs[i]) for i in range(nc.value)]
     return U, L, rows, cols, rk.value
+
+
+def lu(A, N):
+    """lu_gpu_type semantics (no column swaps): returns (U, L (m x m), perm (1-based), rank)."""
+    U = _f(A).copy(order="F")
+    m, n = U.shape
+    L = np.zeros((m, m), dtype=np.int64, order="F")
+    perm = np.zeros(max(m, 1), dtype=np.int64)
+    rk = ctypes.c_int64(0)
+    lib().or_lu(m, n, _ptr(U), max(m, 1), _ptr(L), max(m, 1), int(N), _ptr(perm), ctypes.byref(rk))
+    return U, L, [int(p) + 1 for p in perm[:m]], rk.value
 
 
 def rref(A, N):

@@ -288,6 +288,59 @@ int or_pluq(int64_t m, int64_t n, int64_t *A, int64_t lda,
 }
 
 /* ---------------------------------------------------------------------- */
+/* LU: lu_gpu_type (intended API, test/Experiments/rref_gpu_type.jl:60-103)*/
+/* as the elimination above without column swaps: a zero column is        */
+/* skipped (col += 1), the pivot value and multipliers go to L's column    */
+/* `row` (the pivot count), and perm tracks the row order (0-based).       */
+/* ---------------------------------------------------------------------- */
+int or_lu(int64_t m, int64_t n, int64_t *A, int64_t lda, int64_t *L, int64_t ldl, int64_t N,
+          int64_t *perm, int64_t *rank) {
+    int64_t row = 0, col = 0;
+    for (int64_t i = 0; i < m; i++) perm[i] = i;
+    while (row < m && col < n) {
+        int64_t best = -1, bi = -1;
+        for (int64_t r = row; r < m; r++) {
+            int64_t v = A[r + col * lda];
+            if (v > best) { best = v; bi = r; }
+        }
+        if (best <= 0) { col++; continue; }
+        int64_t inv = or_mod_inv(best, N);
+        for (int64_t c = 0; c < n; c++) {
+            int64_t t = A[bi + c * lda];
+            A[bi + c * lda] = A[row + c * lda];
+            A[row + c * lda] = or_mulmod(t, inv, N);
+        }
+        if (bi != row) {
+            for (int64_t c = 0; c < m; c++) {
+                int64_t t = L[row + c * ldl];
+                L[row + c * ldl] = L[bi + c * ldl];
+                L[bi + c * ldl] = t;
+            }
+            int64_t t = perm[row]; perm[row] = perm[bi]; perm[bi] = t;
+        }
+        L[row + row * ldl] = best;
+        for (int64_t r = row + 1; r < m; r++) {
+            L[r + row * ldl] = A[r + col * lda];
+            A[r + col * lda] = 0;
+        }
+        for (int64_t c = col + 1; c < n; c++) {
+            int64_t s = A[row + c * lda];
+            if (s == 0) continue;
+            for (int64_t r = row + 1; r < m; r++) {
+                int64_t l = L[r + row * ldl];
+                if (l == 0) continue;
+                int64_t v = A[r + c * lda] + or_mulmod(N - l, s, N);
+                A[r + c * lda] = v >= N ? v - N : v;
+            }
+        }
+        row++;
+        col++;
+    }
+    *rank = row;
+    return 0;
+}
+
+/* ---------------------------------------------------------------------- */
 /* RREF: the reduced row echelon form over Z/p (p prime).  It is unique,   */
 /* so any pivot order gives the same matrix; this is plain Gauss-Jordan    */
 /* with the first non-zero entry as pivot.  (Intended API:                 */

@@ -167,3 +167,18 @@ def test_rref_properties():
         assert (R2 == R).all() and rank2 == rank
         _, rank3, _ = oracle.rref(np.vstack([A, R]), N)
         assert rank3 == rank
+
+
+def test_lu_oracle_equals_pluq_on_full_column_rank():
+    # without zero columns lu_gpu_type and pluq_gpu_kernel take the same steps
+    rng = np.random.default_rng(21)
+    for (m, n, N) in [(12, 12, 7), (20, 15, 65521), (9, 9, 67108859)]:
+        A = rng.integers(0, N, size=(m, n))
+        U, L, rs, cs, rk = oracle.pluq(A, N)
+        U2, L2, perm, rk2 = oracle.lu(A, N)
+        assert cs == [] and rk == rk2 == min(m, n)
+        assert (U == U2).all() and (L[:, :m] == L2).all()
+        ident = list(range(1, m + 1))
+        for (i, j) in rs:
+            ident[i - 1], ident[j - 1] = ident[j - 1], ident[i - 1]
+        assert perm == ident
