@@ -44,8 +44,6 @@ constexpr int NUM_THREADS = 64 + 32 * NUM_EPI_WARPS;
 constexpr int MAX_SHIFTS = 7;
 constexpr int TILE_GROUP = 16;     // output-tile rows per raster group (L2 reuse)
 
-enum Epi { EPI_STORE_F64 = 0, EPI_STORE_F32 = 1, EPI_SUB_I32 = 2, EPI_STORE_I32 = 3 };
-
 template <int L>
 struct Cfg {
     static constexpr int STAGE_BYTES = L * (A_TILE + B_TILE);
@@ -270,22 +268,32 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
             const int64_t row = (int64_t)tm * BM + quad * 32 + lane;
             const int64_t col0 = (int64_t)tn * BN + half * 32;
             if (row < p.m) {
+                if (EPI == EPI_SUB_I32) {
+                    // read-modify-write: issue all 32 loads before any store
+                    int32_t *cbase = (int32_t *)p.C + row + col0 * p.ldc;
+                    int32_t cv[32];
 #pragma unroll
-                for (int j = 0; j < 32; j++) {
-                    const int64_t col = col0 + j;
-                    if (col < p.n) {
-                        const int64_t r = reduce_signed(acc[j], p);
-                        const int64_t off = row + col * p.ldc;
-                        if (EPI == EPI_STORE_F64) {
-                            ((double *)p.C)[off] = (double)r;
-                        } else if (EPI == EPI_STORE_F32) {
-                            ((float *)p.C)[off] = (float)r;
-                        } else if (EPI == EPI_STORE_I32) {
-                            ((int32_t *)p.C)[off] = (int32_t)r;
-                        } else {
-                            int32_t *cp = (int32_t *)p.C + off;
-                            int64_t v = (int64_t)*cp - r;
-                            *cp = (int32_t)(v < 0 ? v + p.N : v);
+                    for (int j = 0; j < 32; j++) cv[j] = (col0 + j < p.n) ? __ldcg(cbase + j * p.ldc) : 0;
+#pragma unroll
+                    for (int j = 0; j < 32; j++) {
+                        if (col0 + j < p.n) {
+                            const int64_t v = (int64_t)cv[j] - reduce_signed(acc[j], p);
+                            cbase[j * p.ldc] = (int32_t)(v < 0 ? v + p.N : v);
+                        }
+                    }
+                } else {
+#pragma unroll
+                    for (int j = 0; j < 32; j++) {
+                        const int64_t col = col0 + j;
+                        if (col < p.n) {
+                            const int64_t r = reduce_signed(acc[j], p);
+                            const int64_t off = row + col * p.ldc;
+                            if (EPI == EPI_STORE_F64)
+                                ((double *)p.C)[off] = (double)r;
+                            else if (EPI == EPI_STORE_F32)
+                                ((float *)p.C)[off] = (float)r;
+                            else
+                                ((int32_t *)p.C)[off] = (int32_t)r;
                         }
                     }
                 }

@@ -7,30 +7,36 @@
 // in W (LAPACK style) and moved into L at the end.
 //
 // One panel = up to NB consecutive pivot columns starting at (R0, C0).  The
-// panel kernel is a cooperative grid: CTA b keeps rows [R0 + b*R, R0 + (b+1)*R)
-// of the panel in shared memory.  Per pivot step it
-//   1. finds its local maximum residue of the pivot column (lowest row on ties),
-//   2. publishes the key, that row and (if it owns it) the current pivot row
-//      into a parity-double-buffered global slot,
-//   3. meets the other CTAs at a counting grid barrier (bounded wait),
-//   4. picks the global winner, computes the inverse with the reference's
-//      extended Euclid, swaps / scales the two rows it owns, and eliminates its
-//      rows below the pivot:  W[i][j] = (W[i][j] + (N - l_i) * u_j) mod N.
+// panel kernel (elim_panel.cuh) is a cooperative grid: CTA b keeps rows
+// [R0 + b*R, R0 + (b+1)*R) of the panel in shared memory.  Per pivot step it
+//   1. publishes its candidate -- the largest residue of the pivot column in
+//      its rows (lowest row on ties), that row, and the value's inverse by the
+//      reference's extended Euclid -- in a parity-double-buffered global slot
+//      tagged with the step; its owner also publishes the current row r,
+//   2. polls the G tagged slots (the grid barrier, bounded wait) and loads
+//      every candidate row,
+//   3. picks the global winner, swaps / scales the two rows it owns, and
+//      eliminates its rows below the pivot: W[i][j] = (W[i][j] + (N - l_i) * u_j)
+//      mod N, finding its next candidate on the way.
 // Everything the reference does to columns outside the panel is deferred and
 // applied after the panel in the same order-independent form:
-//   - columns left of the panel: the panel's row swaps (L's multipliers only
-//     below the reference's L swap width 32*cld(m, 32); skipped columns always,
-//     then the pivot-row scaling),
-//   - trailing columns: the row swaps, a triangular solve for the panel rows
-//     (x_t = inv_t * (a_t - sum_{s<t} L[r_t, c_s] x_s), the reference's
-//     scaling and updates in closed form) and the update of the rows below,
-//     A22 -= L21 * U12 mod N, on the limb tensor-core GEMM.
+//   - columns left of the panel: the panel's row swaps (earlier multipliers and
+//     skipped columns), then the pivot-row scaling of the skipped columns,
+//   - trailing columns: the row swaps, the triangular solve for the panel rows
+//     U12 = L11^{-1} P A12 (x_t = inv_t * (a_t - sum_{s<t} L[r_t, c_s] x_s):
+//     the reference's scaling and updates in closed form; the panel kernel
+//     builds L11^{-1}) and the update of the rows below, A22 -= L21 * U12 mod N,
+//     both on the limb tensor-core GEMM.
+// W keeps every multiplier column permuted for this arithmetic; the
+// reference's narrower swap width for L (32*cld(m, 32) columns) is restored
+// when L is extracted.
 // A zero pivot column ends the panel when the panel already has pivots; at the
 // start of a panel it triggers the reference's swap with the last column
 // (PLUQ) or is skipped (LU / RREF).  Exact modular arithmetic makes every
 // pivot search see the same values as the unblocked reference, so the pivot
 // sequence, P, L, U, Q and the swap stacks are identical.
 #include "gffm_common.cuh"
+#include "elim_panel.cuh"
 #include "limb_host.h"
 
 #include <algorithm>
@@ -38,227 +44,7 @@
 
 namespace elim {
 
-constexpr int NB = 64;              // panel width (pivot columns per panel)
-constexpr int PANEL_THREADS = 256;
-
-enum PanelStatus { PS_DONE = 0, PS_ZERO_COL = 1, PS_TIMEOUT = 2, PS_BOUNDS = 3 };
 enum Mode { MODE_PLUQ = 0, MODE_LU = 1, MODE_RREF = 2 };
-
-struct ModP {
-    uint32_t n;
-    uint64_t minv;
-};
-
-__device__ __forceinline__ uint32_t mulmod(uint32_t a, uint32_t b, const ModP &M) {
-    return (uint32_t)gffm_dev::barrett64((uint64_t)a * b, M.n, M.minv);
-}
-
-// mod_inv(p, P), src/CuModMatrix/rref_lu_pluq/pluq_kernels.jl:11-31
-__device__ __forceinline__ uint32_t mod_inv_euclid(int64_t p, int64_t P) {
-    int64_t inv = 0, new_inv = 1, rem = P, new_rem = p;
-    while (new_rem != 0) {
-        int64_t q = (int64_t)((uint32_t)rem / (uint32_t)new_rem);  // both in [0, 2^26)
-        int64_t t = inv - q * new_inv;
-        inv = new_inv;
-        new_inv = t;
-        t = rem - q * new_rem;
-        rem = new_rem;
-        new_rem = t;
-    }
-    if (inv < 0) inv += P;
-    return (uint32_t)inv;
-}
-
-struct PanelArgs {
-    int32_t *W;
-    int64_t ldw;
-    int m, n;
-    int R0, C0, nbw;   // first pivot row / column, panel width
-    int R;             // rows per CTA
-    ModP M;
-    int lsw;           // L row swaps reach columns [0, lsw) only
-    int l_cols;        // L's padded width (PLUQ bound check), <= 0: no check
-    unsigned long long *cand_key;  // [2][G]
-    int32_t *cand_row;             // [2][G][NB]
-    int32_t *old_row;              // [2][NB]
-    unsigned int *bar;             // barrier counter, zero at launch
-    int32_t *piv_row, *piv_val, *piv_inv;  // [NB]
-    int *result;                           // [0] pivots, [1] status
-    int *err;
-};
-
-__global__ void __launch_bounds__(PANEL_THREADS) k_panel(PanelArgs a) {
-    extern __shared__ int32_t P[];  // R x NB
-    __shared__ int32_t piv[NB], oldr[NB], u[NB];
-    __shared__ unsigned long long red[PANEL_THREADS / 32];
-    __shared__ int s_stop, s_status;
-    __shared__ int32_t s_prow, s_pv, s_inv;
-    const int b = blockIdx.x, G = gridDim.x, tid = threadIdx.x;
-    const int lane = tid & 31, wid = tid >> 5;
-    const int rbeg = a.R0 + b * a.R;
-    const int rend = min(rbeg + a.R, a.m);
-    const int nr = max(rend - rbeg, 0);
-    const int nbw = a.nbw;
-
-    for (int e = tid; e < nr * NB; e += blockDim.x) {
-        int i = e / NB, j = e - (e / NB) * NB;
-        P[e] = (j < nbw) ? a.W[(int64_t)(rbeg + i) * a.ldw + a.C0 + j] : 0;
-    }
-    if (tid == 0) {
-        s_stop = 0;
-        s_status = PS_DONE;
-    }
-    __syncthreads();
-
-    const int tmax = min(nbw, a.m - a.R0);
-    int t = 0;
-    for (; t < tmax; t++) {
-        const int r = a.R0 + t;
-        const int par = t & 1;
-        // 1. local arg-max of column t over rows >= r (key: value, then lowest row)
-        unsigned long long best = 0;
-        for (int i = max(r - rbeg, 0) + tid; i < nr; i += blockDim.x) {
-            unsigned long long key = ((unsigned long long)(uint32_t)P[i * NB + t] << 32) |
-                                     (unsigned long long)(0xFFFFFFFFu - (uint32_t)(rbeg + i));
-            best = key > best ? key : best;
-        }
-        for (int o = 16; o; o >>= 1) {
-            unsigned long long v = __shfl_xor_sync(0xffffffffu, best, o);
-            best = v > best ? v : best;
-        }
-        if (lane == 0) red[wid] = best;
-        __syncthreads();
-        if (tid == 0) {
-            for (int w = 1; w < PANEL_THREADS / 32; w++) best = red[w] > best ? red[w] : best;
-            best = red[0] > best ? red[0] : best;
-            a.cand_key[par * G + b] = best;
-            s_prow = best ? (int)(0xFFFFFFFFu - (uint32_t)best) : -1;
-        }
-        __syncthreads();
-        // 2. publish the candidate row and, from its owner, the current row r
-        {
-            const int li = s_prow >= 0 ? s_prow - rbeg : -1;
-            int32_t *cr = a.cand_row + ((size_t)par * G + b) * NB;
-            if (li >= 0)
-                for (int j = tid; j < nbw; j += blockDim.x) cr[j] = P[li * NB + j];
-            if (r >= rbeg && r < rend)
-                for (int j = tid; j < nbw; j += blockDim.x) a.old_row[par * NB + j] = P[(r - rbeg) * NB + j];
-        }
-        __syncthreads();
-        // 3. grid barrier (bounded)
-        if (tid == 0) {
-            __threadfence();
-            atomicAdd(a.bar, 1u);
-            const unsigned int target = (unsigned int)(t + 1) * (unsigned int)G;
-            if (*(volatile unsigned int *)a.bar < target) {
-                const unsigned long long t0 = gffm_dev::globaltimer();
-                while (*(volatile unsigned int *)a.bar < target) {
-                    if (gffm_dev::globaltimer() - t0 > gffm_dev::kWaitLimitNs) {
-                        atomicOr(a.err, 16);
-                        s_stop = 1;
-                        s_status = PS_TIMEOUT;
-                        break;
-                    }
-                }
-            }
-            __threadfence();
-        }
-        __syncthreads();
-        if (s_stop) break;
-        // 4. the global pivot
-        unsigned long long wk = 0;
-        for (int g = tid; g < G; g += blockDim.x) {
-            unsigned long long v = *(volatile unsigned long long *)&a.cand_key[par * G + g];
-            wk = v > wk ? v : wk;
-        }
-        for (int o = 16; o; o >>= 1) {
-            unsigned long long v = __shfl_xor_sync(0xffffffffu, wk, o);
-            wk = v > wk ? v : wk;
-        }
-        if (lane == 0) red[wid] = wk;
-        __syncthreads();
-        if (tid == 0) {
-            for (int w = 0; w < PANEL_THREADS / 32; w++) wk = red[w] > wk ? red[w] : wk;
-            const uint32_t pv = (uint32_t)(wk >> 32);
-            if (pv == 0) {
-                s_stop = 1;
-                s_status = PS_ZERO_COL;
-            } else if (a.l_cols > 0 && a.C0 + t >= a.l_cols) {
-                s_stop = 1;
-                s_status = PS_BOUNDS;
-            } else {
-                s_pv = (int32_t)pv;
-                s_prow = (int)(0xFFFFFFFFu - (uint32_t)wk);
-            }
-        }
-        __syncthreads();
-        if (s_stop) break;
-        const int prow = s_prow;
-        const int bw = (prow - a.R0) / a.R;
-        {
-            const volatile int32_t *cr = a.cand_row + ((size_t)par * G + bw) * NB;
-            const volatile int32_t *orow = a.old_row + par * NB;
-            for (int j = tid; j < nbw; j += blockDim.x) {
-                piv[j] = cr[j];
-                oldr[j] = orow[j];
-            }
-        }
-        if (tid == 0) s_inv = (int32_t)mod_inv_euclid(s_pv, a.M.n);
-        __syncthreads();
-        const uint32_t inv = (uint32_t)s_inv;
-        for (int j = tid; j < nbw; j += blockDim.x) u[j] = (int32_t)mulmod((uint32_t)piv[j], inv, a.M);
-        __syncthreads();
-        // 5. swap_rows_and_mod restricted to the panel: row r <- pivot row * inv,
-        //    row prow <- old row r; multiplier columns (j < t) swap unscaled, only below lsw
-        if (r >= rbeg && r < rend) {
-            int32_t *pr = P + (r - rbeg) * NB;
-            for (int j = tid; j < nbw; j += blockDim.x) {
-                if (j >= t)
-                    pr[j] = u[j];
-                else if (a.C0 + j < a.lsw)
-                    pr[j] = piv[j];
-            }
-        }
-        if (prow != r && prow >= rbeg && prow < rend) {
-            int32_t *pp = P + (prow - rbeg) * NB;
-            for (int j = tid; j < nbw; j += blockDim.x) {
-                if (j >= t || a.C0 + j < a.lsw) pp[j] = oldr[j];
-            }
-        }
-        __syncthreads();
-        // 6. eliminate rows below the pivot (the multiplier stays in column t)
-        {
-            const int i0 = max(r + 1 - rbeg, 0);
-            const int ncol = nbw - t - 1;
-            if (ncol > 0 && i0 < nr) {
-                const int total = (nr - i0) * ncol;
-                for (int e = tid; e < total; e += blockDim.x) {
-                    const int i = i0 + e / ncol;
-                    const int j = t + 1 + e % ncol;
-                    const uint32_t l = (uint32_t)P[i * NB + t];
-                    if (l != 0) {
-                        const uint64_t v = (uint64_t)(uint32_t)P[i * NB + j] + (uint64_t)(a.M.n - l) * (uint32_t)u[j];
-                        P[i * NB + j] = (int32_t)gffm_dev::barrett64(v, a.M.n, a.M.minv);
-                    }
-                }
-            }
-        }
-        if (b == 0 && tid == 0) {
-            a.piv_row[t] = prow;
-            a.piv_val[t] = s_pv;
-            a.piv_inv[t] = (int32_t)inv;
-        }
-        __syncthreads();
-    }
-    for (int e = tid; e < nr * NB; e += blockDim.x) {
-        int i = e / NB, j = e - (e / NB) * NB;
-        if (j < nbw) a.W[(int64_t)(rbeg + i) * a.ldw + a.C0 + j] = P[e];
-    }
-    if (b == 0 && tid == 0) {
-        a.result[0] = t;
-        a.result[1] = s_status;
-    }
-}
 
 // A (column-major, any element type holding integers) -> W (row-major int32 residues)
 template <typename T>
@@ -291,25 +77,8 @@ __global__ void __launch_bounds__(256) k_to_rowmajor(const T *__restrict__ A, in
     }
 }
 
-// Apply the panel's row swaps (pivot s: rows R0+s <-> prow[s]), in order, to
-// columns [c_lo, c_hi); with inv != nullptr also scale the new pivot row.
-__global__ void __launch_bounds__(256) k_laswp(int32_t *W, int64_t ldw, int c_lo, int c_hi, int R0, int t,
-                                               const int32_t *prow, const int32_t *inv, ModP M) {
-    const int j = c_lo + blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= c_hi) return;
-    for (int s = 0; s < t; s++) {
-        const int r = R0 + s, p = prow[s];
-        if (p != r) {
-            int32_t x = W[(int64_t)r * ldw + j];
-            W[(int64_t)r * ldw + j] = W[(int64_t)p * ldw + j];
-            W[(int64_t)p * ldw + j] = x;
-        }
-        if (inv) W[(int64_t)r * ldw + j] = (int32_t)mulmod((uint32_t)W[(int64_t)r * ldw + j], (uint32_t)inv[s], M);
-    }
-}
-
 // Skipped (swapped-in, never eliminated) columns: the panel's row swaps for
-// columns at or beyond lo (those below lo were covered by k_laswp), then the
+// columns at or beyond lo (those below lo were covered by k_permute_rows), then the
 // scaling of every new pivot row, as swap_rows_and_mod does over all columns.
 __global__ void k_skipped(int32_t *W, int64_t ldw, const int32_t *qlist, int nq, int lo, int R0, int t,
                           const int32_t *prow, const int32_t *inv, ModP M) {
@@ -339,37 +108,6 @@ __global__ void k_colswap(int32_t *W, int64_t ldw, int m, int c1, int c2) {
     int32_t x = W[(int64_t)i * ldw + c1];
     W[(int64_t)i * ldw + c1] = W[(int64_t)i * ldw + c2];
     W[(int64_t)i * ldw + c2] = x;
-}
-
-// Rows R0..R0+t-1 of the trailing columns [cs, n):
-//   x_i = inv_i * (a_i - sum_{s<i} L11[i][s] x_s)  mod N,
-// L11[i][s] = W[R0+i][C0+s] (the multipliers of this panel).  Sums of up to NB
-// products below 2^52 are exact in 64 bits before one reduction.
-__global__ void __launch_bounds__(128) k_trsm(int32_t *W, int64_t ldw, int R0, int C0, int t, int cs, int n,
-                                              const int32_t *inv, ModP M) {
-    __shared__ uint32_t L11[NB][NB + 1];
-    __shared__ uint32_t sinv[NB];
-    for (int e = threadIdx.x; e < t * t; e += blockDim.x) {
-        int i = e / t, s = e % t;
-        L11[i][s] = (s < i) ? (M.n - (uint32_t)W[(int64_t)(R0 + i) * ldw + C0 + s]) % M.n : 0;
-    }
-    for (int e = threadIdx.x; e < t; e += blockDim.x) sinv[e] = (uint32_t)inv[e];
-    __syncthreads();
-    const int j = cs + blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= n) return;
-    uint32_t x[NB];
-#pragma unroll
-    for (int i = 0; i < NB; i++) {
-        if (i < t) {
-            uint64_t acc = (uint32_t)W[(int64_t)(R0 + i) * ldw + j];
-#pragma unroll
-            for (int s = 0; s < NB; s++)
-                if (s < i) acc += (uint64_t)L11[i][s] * x[s];
-            const uint32_t v = (uint32_t)gffm_dev::barrett64(acc, M.n, M.minv);
-            x[i] = mulmod(v, sinv[i], M);
-            W[(int64_t)(R0 + i) * ldw + j] = (int32_t)x[i];
-        }
-    }
 }
 
 // U (column-major) from W: multipliers below each pivot become 0.
@@ -471,14 +209,14 @@ __global__ void k_gather_cols(const int32_t *W, int64_t ldw, int row0, int rows,
 struct Work {
     int32_t *W;
     int64_t ldw;
-    unsigned long long *cand_key;
-    int32_t *cand_row, *old_row;
-    unsigned int *bar;
+    Rec *rec;
+    int32_t *old_row;
     int32_t *piv_row, *piv_val, *piv_inv;
     int *result;
     int32_t *colpiv, *lsrc, *lrow, *lpv, *pcol;  // [n], [lcols] x3, [min(m,n)]
     int32_t *gather;                             // m x NB
     int32_t *coef;                               // NB x NB
+    int32_t *linv;                               // NB x NB, inverse of the panel's L11
     int32_t *qlist;                              // [n] skipped columns
     __half *dA, *dB;                             // digit planes
     limb::Layout gl;
@@ -494,10 +232,10 @@ static void layout_ws(int64_t m, int64_t n, int64_t lcols, size_t *total, size_t
     *gl = limb::layout(std::max<int64_t>(n, 1), std::max<int64_t>(m, 1), NB, int64_t(1) << 25);
     size_t sizes[16] = {
         (size_t)std::max<int64_t>(m, 1) * ldw * 4,      // W
-        (size_t)2 * G * 8,                              // cand_key
-        (size_t)2 * G * NB * 4,                         // cand_row
+        (size_t)2 * MAX_PANEL_CTAS * sizeof(Rec),       // rec
+        (size_t)NB * NB * 4,                            // linv
         (size_t)2 * NB * 4,                             // old_row
-        256,                                            // bar
+        0,
         NB * 4, NB * 4, NB * 4,                         // piv_row/val/inv
         64,                                             // result
         (size_t)std::max<int64_t>(n, 1) * 4,            // colpiv
@@ -520,10 +258,9 @@ static void bind_ws(void *base, int64_t m, int64_t n, int64_t lcols, Work *w) {
     uint8_t *b = static_cast<uint8_t *>(base);
     w->W = (int32_t *)(b + off[0]);
     w->ldw = gffm::round_up(n > 0 ? n : 1, 32);
-    w->cand_key = (unsigned long long *)(b + off[1]);
-    w->cand_row = (int32_t *)(b + off[2]);
+    w->rec = (Rec *)(b + off[1]);
+    w->linv = (int32_t *)(b + off[2]);
     w->old_row = (int32_t *)(b + off[3]);
-    w->bar = (unsigned int *)(b + off[4]);
     w->piv_row = (int32_t *)(b + off[5]);
     w->piv_val = (int32_t *)(b + off[6]);
     w->piv_inv = (int32_t *)(b + off[7]);
@@ -550,14 +287,18 @@ size_t workspace_bytes(int64_t m, int64_t n, int64_t lcols) {
 struct Result {
     std::vector<int64_t> row_swaps, col_swaps;  // flattened 1-based pairs
     std::vector<int> piv_r, piv_c, piv_v;       // pivots in order
+    std::vector<int> swap_step;                 // pivot index of each recorded row swap
     std::vector<int> perm;                      // LU: final row order (0-based original index)
     int rank = 0;
 };
 
-// W -= L21 * U12 (or the RREF back update) on the limb GEMM, in row-major terms:
-// C (rows x cols, row-major, ldc) -= X (rows x k, row-major, ldx) * Y (k x cols, row-major, ldy)
-static int rowmajor_sub_gemm(Work &w, int64_t N, int32_t *C, int64_t ldc, const int32_t *X, int64_t ldx,
-                             const int32_t *Y, int64_t ldy, int64_t rows, int64_t cols, int64_t k, cudaStream_t s) {
+// Row-major products on the limb GEMM:
+// C (rows x cols, row-major, ldc) (-)= X (rows x k, row-major, ldx) * Y (k x cols, row-major, ldy),
+// epi = limb::EPI_SUB_I32 (C -= XY) or limb::EPI_STORE_I32 (C = XY; C may overlap Y, which is
+// split into digit planes before the product runs).
+static int rowmajor_gemm(Work &w, int64_t N, int32_t *C, int64_t ldc, const int32_t *X, int64_t ldx,
+                         const int32_t *Y, int64_t ldy, int64_t rows, int64_t cols, int64_t k, int epi,
+                         cudaStream_t s) {
     if (rows <= 0 || cols <= 0 || k <= 0) return GFFM_OK;
     // column-major view: C^T (cols x rows) -= Y^T (cols x k) * X^T (k x rows)
     limb::Layout g = limb::layout(cols, rows, k, N);
@@ -565,21 +306,24 @@ static int rowmajor_sub_gemm(Work &w, int64_t N, int32_t *C, int64_t ldc, const 
     if (st) return st;
     st = limb::split_b<int32_t>(X, ldx, k, rows, w.dB, g, N, s);
     if (st) return st;
-    return limb::gemm_digits(g, w.dA, w.dB, cols, rows, k, N, C, ldc, 2 /* EPI_SUB_I32 */, 0, s);
+    return limb::gemm_digits(g, w.dA, w.dB, cols, rows, k, N, C, ldc, epi, 0, s);
 }
 
-static int run_panel(Work &w, int m, int n, int R0, int C0, int nbw, const ModP &M, int lsw, int lcols_check,
+static int run_panel(Work &w, int m, int n, int R0, int C0, int nbw, const ModP &M, int lcols_check,
                      cudaStream_t s, int h_res[2], std::vector<int32_t> &h_prow, std::vector<int32_t> &h_pv) {
     using namespace gffm;
     const int rows = m - R0;
-    int sms = sm_count();
+    const int sms = sm_count();
+    // rows per CTA: at least 64, and at most 64 CTAs while the rows fit (the per-step
+    // exchange moves G candidate rows into every CTA)
     int R = 64;
-    while ((rows + R - 1) / R > sms || (rows + R - 1) / R > 150) R += 32;
-    if (R > 768)
-        return set_error(GFFM_ERR_UNSUPPORTED, "elimination panel: %d rows exceed the panel kernel's capacity", rows);
+    while ((rows + R - 1) / R > std::min(sms, 64) && R < 640) R += 32;
+    while ((rows + R - 1) / R > std::min(sms, MAX_PANEL_CTAS)) R += 32;
     const int G = std::max(1, (rows + R - 1) / R);
-    const size_t smem = (size_t)R * NB * 4;
-    GFFM_CUDA(cudaMemsetAsync(w.bar, 0, sizeof(unsigned int), s));
+    const size_t smem = ((size_t)R + G) * NB * 4;
+    if (smem > 200 * 1024)
+        return set_error(GFFM_ERR_UNSUPPORTED, "elimination panel: %d rows exceed the panel kernel's capacity", rows);
+    GFFM_CUDA(cudaMemsetAsync(w.rec, 0, (size_t)2 * G * sizeof(Rec), s));
     PanelArgs a;
     a.W = w.W;
     a.ldw = w.ldw;
@@ -590,18 +334,15 @@ static int run_panel(Work &w, int m, int n, int R0, int C0, int nbw, const ModP 
     a.nbw = nbw;
     a.R = R;
     a.M = M;
-    a.lsw = lsw;
     a.l_cols = lcols_check;
-    a.cand_key = w.cand_key;
-    a.cand_row = w.cand_row;
+    a.rec = w.rec;
     a.old_row = w.old_row;
-    a.bar = w.bar;
     a.piv_row = w.piv_row;
     a.piv_val = w.piv_val;
     a.piv_inv = w.piv_inv;
     a.result = w.result;
     a.err = device_error_flag();
-    if (smem > 48 * 1024) GFFM_CUDA(cudaFuncSetAttribute(k_panel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    GFFM_CUDA(cudaFuncSetAttribute(k_panel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     void *args[] = {&a};
     GFFM_CUDA(cudaLaunchCooperativeKernel((void *)k_panel, dim3(G), dim3(PANEL_THREADS), args, smem, s));
     GFFM_CUDA(cudaMemcpyAsync(h_res, w.result, 2 * sizeof(int), cudaMemcpyDeviceToHost, s));
@@ -615,7 +356,6 @@ static int run_panel(Work &w, int m, int n, int R0, int C0, int nbw, const ModP 
 static int forward(Work &w, int m, int n, int64_t N, int mode, int lcols, cudaStream_t s, Result &res) {
     using namespace gffm;
     ModP M{(uint32_t)N, ~uint64_t(0) / (uint64_t)N};
-    const int lsw = (mode == MODE_PLUQ) ? std::min<int64_t>(((int64_t)m + 31) / 32 * 32, lcols) : n;
     const int last = n - 1;
     std::vector<int> skipped;  // PLUQ: columns holding a swapped-in column that is never eliminated
     std::vector<int32_t> h_prow(NB), h_pv(NB);
@@ -625,7 +365,7 @@ static int forward(Work &w, int m, int n, int64_t N, int mode, int lcols, cudaSt
     for (int i = 0; i < m; i++) res.perm[i] = i;
     while (row < m && col < n) {
         const int nbw = std::min(NB, n - col);
-        int st = run_panel(w, m, n, row, col, nbw, M, lsw, mode == MODE_PLUQ ? lcols : 0, s, h_res, h_prow, h_pv);
+        int st = run_panel(w, m, n, row, col, nbw, M, mode == MODE_PLUQ ? lcols : 0, s, h_res, h_prow, h_pv);
         if (st) return st;
         const int t = h_res[0], status = h_res[1];
         if (status == PS_TIMEOUT) return set_error(GFFM_ERR_TIMEOUT, "elimination panel: a device-side wait gave up");
@@ -634,6 +374,7 @@ static int forward(Work &w, int m, int n, int64_t N, int mode, int lcols, cudaSt
             if (p != r) {
                 res.row_swaps.push_back(r + 1);
                 res.row_swaps.push_back(p + 1);
+                res.swap_step.push_back((int)res.piv_r.size());
                 std::swap(res.perm[r], res.perm[p]);
             }
             res.piv_r.push_back(r);
@@ -641,11 +382,33 @@ static int forward(Work &w, int m, int n, int64_t N, int mode, int lcols, cudaSt
             res.piv_v.push_back(h_pv[q]);
         }
         if (t > 0) {
-            // columns left of the panel: L multipliers (below lsw) and skipped columns
-            const int left_hi = std::min(col, lsw);
+            // the panel's row swaps composed into one permutation of the rows involved
+            PermArgs perm;
+            {
+                std::vector<int32_t> rows_inv;
+                for (int q = 0; q < t; q++) rows_inv.push_back(row + q);
+                for (int q = 0; q < t; q++)
+                    if (h_prow[q] >= row + t && std::find(rows_inv.begin(), rows_inv.end(), h_prow[q]) == rows_inv.end())
+                        rows_inv.push_back(h_prow[q]);
+                std::vector<int32_t> content(rows_inv.size());
+                for (size_t k = 0; k < rows_inv.size(); k++) content[k] = (int32_t)k;
+                auto pos = [&](int32_t rr) {
+                    return (int)(std::find(rows_inv.begin(), rows_inv.end(), rr) - rows_inv.begin());
+                };
+                for (int q = 0; q < t; q++) std::swap(content[pos(row + q)], content[pos(h_prow[q])]);
+                perm.K = (int)rows_inv.size();
+                for (int k = 0; k < perm.K; k++) {
+                    perm.rows[k] = rows_inv[k];
+                    perm.src[k] = content[k];
+                }
+            }
+            // columns left of the panel: multipliers of earlier pivots and skipped columns
+            // (W keeps every multiplier column permuted for the arithmetic; the reference's
+            // narrower L swap width is restored when L is extracted)
+            const int left_hi = col;
             if (left_hi > 0) {
-                k_laswp<<<(left_hi + 255) / 256, 256, 0, s>>>(w.W, w.ldw, 0, left_hi, row, t, w.piv_row, nullptr, M);
-                GFFM_LAUNCH_CHECK("k_laswp(left)");
+                k_permute_rows<<<(left_hi + 63) / 64, 64, 0, s>>>(w.W, w.ldw, 0, left_hi, perm);
+                GFFM_LAUNCH_CHECK("k_permute_rows(left)");
             }
             if (!skipped.empty()) {
                 // skipped columns hold A values: row swaps at every width, then the
@@ -658,14 +421,19 @@ static int forward(Work &w, int m, int n, int64_t N, int mode, int lcols, cudaSt
             // trailing columns: swaps, triangular solve, update of the rows below
             const int cs = col + nbw;
             if (cs < n) {
-                k_laswp<<<(n - cs + 255) / 256, 256, 0, s>>>(w.W, w.ldw, cs, n, row, t, w.piv_row, nullptr, M);
-                GFFM_LAUNCH_CHECK("k_laswp(trailing)");
-                k_trsm<<<(n - cs + 127) / 128, 128, 0, s>>>(w.W, w.ldw, row, col, t, cs, n, w.piv_inv, M);
-                GFFM_LAUNCH_CHECK("k_trsm");
+                k_permute_rows<<<(n - cs + 63) / 64, 64, 0, s>>>(w.W, w.ldw, cs, n, perm);
+                GFFM_LAUNCH_CHECK("k_permute_rows(trailing)");
+                // U12 = L11^{-1} P A12
+                k_linv<<<2, 1024, 0, s>>>(w.W, w.ldw, row, col, t, w.piv_inv, w.linv, M);
+                GFFM_LAUNCH_CHECK("k_linv");
+                st = rowmajor_gemm(w, N, w.W + (int64_t)row * w.ldw + cs, w.ldw, w.linv, NB,
+                                   w.W + (int64_t)row * w.ldw + cs, w.ldw, t, n - cs, t, limb::EPI_STORE_I32, s);
+                if (st) return st;
                 if (row + t < m) {
-                    st = rowmajor_sub_gemm(w, N, w.W + (int64_t)(row + t) * w.ldw + cs, w.ldw,
-                                           w.W + (int64_t)(row + t) * w.ldw + col, w.ldw,
-                                           w.W + (int64_t)row * w.ldw + cs, w.ldw, m - row - t, n - cs, t, s);
+                    st = rowmajor_gemm(w, N, w.W + (int64_t)(row + t) * w.ldw + cs, w.ldw,
+                                       w.W + (int64_t)(row + t) * w.ldw + col, w.ldw,
+                                       w.W + (int64_t)row * w.ldw + cs, w.ldw, m - row - t, n - cs, t,
+                                       limb::EPI_SUB_I32, s);
                     if (st) return st;
                 }
             }
@@ -715,8 +483,8 @@ static int backward(Work &w, int m, int n, int64_t N, const Result &res, cudaStr
         if (p0 > 0) {
             k_gather_cols<<<(p0 + 127) / 128, 128, 0, s>>>(w.W, w.ldw, 0, p0, nbp, w.pcol, w.gather);
             GFFM_LAUNCH_CHECK("k_gather_cols");
-            int st = rowmajor_sub_gemm(w, N, w.W + c0, w.ldw, w.gather, NB, w.W + (int64_t)p0 * w.ldw + c0, w.ldw,
-                                       p0, n - c0, nbp, s);
+            int st = rowmajor_gemm(w, N, w.W + c0, w.ldw, w.gather, NB, w.W + (int64_t)p0 * w.ldw + c0, w.ldw,
+                                   p0, n - c0, nbp, limb::EPI_SUB_I32, s);
             if (st) return st;
         }
         // the host vector pc must outlive the async copy
@@ -844,6 +612,24 @@ int pluq(int64_t m, int64_t n, const T *A, int64_t lda, T *U, int64_t ldu, T *L,
         if (L) {
             st = extract_l<T>(w, m, lcols, res, mode, L, ldl, s);
             if (st) return st;
+            if (mode == MODE_PLUQ) {
+                // The reference swaps L's rows only over columns 1..32*cld(rows, 32)
+                // (swap_rows launch, pluq_kernels.jl:254): a pivot column past that width
+                // keeps the row order of its own step.  W permuted every column, so undo
+                // the later swaps on those (rare) columns.
+                const int64_t lsw = std::min<int64_t>((m + 31) / 32 * 32, lcols);
+                std::vector<T> colbuf(m);
+                for (size_t q = 0; q < res.piv_c.size(); q++) {
+                    const int64_t c = res.piv_c[q];
+                    if (c < lsw || c >= lcols) continue;
+                    GFFM_CUDA(cudaMemcpy(colbuf.data(), L + c * ldl, m * sizeof(T), cudaMemcpyDeviceToHost));
+                    for (int64_t k = (int64_t)res.swap_step.size() - 1; k >= 0; k--) {
+                        if (res.swap_step[k] <= (int)q) break;
+                        std::swap(colbuf[res.row_swaps[2 * k] - 1], colbuf[res.row_swaps[2 * k + 1] - 1]);
+                    }
+                    GFFM_CUDA(cudaMemcpy(L + c * ldl, colbuf.data(), m * sizeof(T), cudaMemcpyHostToDevice));
+                }
+            }
         }
         if (mode == MODE_PLUQ) {
             std::copy(res.row_swaps.begin(), res.row_swaps.end(), row_swaps);

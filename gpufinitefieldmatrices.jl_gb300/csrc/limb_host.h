@@ -9,6 +9,9 @@
 
 namespace limb {
 
+// epilogue of the GEMM: store Float64 / Float32 / int32 residues, or C = (C - AB) mod N on int32
+enum Epi { EPI_STORE_F64 = 0, EPI_STORE_F32 = 1, EPI_SUB_I32 = 2, EPI_STORE_I32 = 3 };
+
 struct Layout {
     int L;                 // digits per residue
     int64_t Mpad, Npad, Kpad;

@@ -49,6 +49,10 @@ def make(kind, m, n, N, rng):
     if kind == "tall_low":             # rows below the pivot are zero early
         A = np.triu(rng.integers(0, N, size=(m, n)))
         return A
+    if kind == "wide_quirk":           # 32 leading zero columns: pivots land past L's row-swap width
+        A = rng.integers(0, N, size=(m, n))
+        A[:, :32] = 0
+        return A
     raise ValueError(kind)
 
 
@@ -59,6 +63,7 @@ CASES = [
     ("rank30", 96, 96, P26), ("rank70", 150, 140, 7), ("rank1", 40, 40, 5),
     ("zero_cols", 40, 40, 13), ("zero_cols", 100, 130, 65521), ("lead_zero", 70, 80, 7),
     ("ties", 70, 70, 3), ("ties", 130, 90, 11), ("zeros", 10, 12, 7), ("tall_low", 90, 90, P26),
+    ("wide_quirk", 3, 40, 7), ("wide_quirk", 5, 45, 11), ("wide_quirk", 4, 38, 65521),
 ]
 
 
@@ -67,8 +72,16 @@ def test_pluq_matches_oracle(gffm, case):
     kind, m, n, N = case
     rng = np.random.default_rng(m * 1000 + n + N % 997)
     A = make(kind, m, n, N, rng)
-    U0, L0, rs0, cs0, rk0 = oracle.pluq(A, N)
     Ag = gffm.CuModMatrix(A, N, elem_type=torch.float64)
+    try:
+        U0, L0, rs0, cs0, rk0 = oracle.pluq(A, N)
+    except IndexError:
+        # the reference indexes L past its padded width here (a BoundsError): so must we
+        with pytest.raises(gffm.GFFMError) as ei:
+            gffm.pluq_gpu_kernel(Ag)
+        assert ei.value.status == 8
+        status_ok(gffm)
+        return
     U, L, rs, cs = gffm.pluq_gpu_kernel(Ag)
     assert rs == rs0 and cs == cs0
     assert np.array_equal(as_int(U), U0)
