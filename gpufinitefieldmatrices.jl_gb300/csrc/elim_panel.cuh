@@ -6,8 +6,9 @@
 
 namespace elim {
 
-constexpr int NB = 64;              // panel width (pivot columns per panel)
-constexpr int PANEL_THREADS = 256;
+constexpr int NB = 128;             // panel width (pivot columns per panel)
+constexpr int CPL = NB / 32;        // panel columns per lane in the elimination
+constexpr int PANEL_THREADS = 512;
 constexpr int PANEL_WARPS = PANEL_THREADS / 32;
 constexpr int MAX_PANEL_CTAS = 160;
 constexpr int MAX_PERM_ROWS = 2 * NB;
@@ -23,37 +24,81 @@ __device__ __forceinline__ uint32_t mulmod(uint32_t a, uint32_t b, const ModP &M
     return (uint32_t)gffm_dev::barrett64((uint64_t)a * b, M.n, M.minv);
 }
 
-// floor(a / b) for 0 <= a < 2^26, b >= 1: float estimate, corrected to the exact quotient
+// floor(a / b) for 0 <= a < 2^26, 1 <= b <= a: float estimate, corrected to the
+// exact quotient (32-bit arithmetic; the remainder a - q*b stays below 2^27)
 __device__ __forceinline__ uint32_t udiv26(uint32_t a, uint32_t b) {
-    int64_t q = (int64_t)__fdividef((float)a, (float)b);
-    int64_t r = (int64_t)a - q * (int64_t)b;
+    int32_t q = (int32_t)__fdividef((float)a, (float)b);
+    int32_t r = (int32_t)a - q * (int32_t)b;
     while (r < 0) {
         q--;
-        r += b;
+        r += (int32_t)b;
     }
-    while (r >= (int64_t)b) {
+    while (r >= (int32_t)b) {
         q++;
-        r -= b;
+        r -= (int32_t)b;
     }
     return (uint32_t)q;
 }
 
 // mod_inv(p, P), src/CuModMatrix/rref_lu_pluq/pluq_kernels.jl:11-31: the same
 // extended Euclid sequence (exact quotients), so the same result for any P.
+// The Bezout coefficients stay below P < 2^26 in magnitude: 32-bit integers.
 __device__ __forceinline__ uint32_t mod_inv_euclid(uint32_t p, uint32_t P) {
-    int64_t inv = 0, new_inv = 1;
+    int32_t inv = 0, new_inv = 1;
     uint32_t rem = P, new_rem = p;
     while (new_rem != 0) {
         const uint32_t q = udiv26(rem, new_rem);
-        const int64_t t = inv - (int64_t)q * new_inv;
+        const int32_t t = inv - (int32_t)q * new_inv;
         inv = new_inv;
         new_inv = t;
         const uint32_t r2 = rem - q * new_rem;
         rem = new_rem;
         new_rem = r2;
     }
-    if (inv < 0) inv += P;
+    if (inv < 0) inv += (int32_t)P;
     return (uint32_t)inv;
+}
+
+// Montgomery arithmetic modulo an odd N < 2^26 with R = 2^32:
+// mont_mul(a, b) = a * b * R^{-1} mod N for a, b < N (t + m*N < 2^59).
+struct Mont {
+    uint32_t n, nprime;  // nprime = -N^{-1} mod 2^32
+    uint32_t r2;         // R^2 mod N
+    int prime;           // N is prime (then the inverse is v^(N-2))
+};
+__device__ __forceinline__ uint32_t mont_mul(uint32_t a, uint32_t b, const Mont &M) {
+    const uint64_t t = (uint64_t)a * b;
+    const uint32_t m = (uint32_t)t * M.nprime;
+    const uint32_t u = (uint32_t)((t + (uint64_t)m * M.n) >> 32);
+    return u >= M.n ? u - M.n : u;
+}
+// The inverse of v in [1, N): for prime N by Fermat (v^(N-2), square-and-multiply
+// in Montgomery form -- the unique inverse, equal to what the reference's Euclid
+// returns), otherwise the reference's extended Euclid itself.
+__device__ __forceinline__ uint32_t mod_inverse(uint32_t v, const Mont &M) {
+    if (!M.prime) return mod_inv_euclid(v, M.n);
+    const uint32_t e = M.n - 2;
+    const uint32_t vm = mont_mul(v, M.r2, M);
+    uint32_t x = vm;
+    for (int bit = 30 - __clz(e); bit >= 0; bit--) {
+        x = mont_mul(x, x, M);
+        if ((e >> bit) & 1u) x = mont_mul(x, vm, M);
+    }
+    return mont_mul(x, 1u, M);
+}
+
+// Shoup's modular multiplication by a fixed u in [0, N): u' = floor(u * 2^32 / N)
+// (possibly one less, from floor((2^64 - 1) / N)); then l * u mod N for l in
+// [0, N) takes 32-bit operations only.
+__device__ __forceinline__ uint32_t shoup_pre(uint32_t u, const ModP &M) {
+    return (uint32_t)(((uint64_t)u * M.minv) >> 32);
+}
+__device__ __forceinline__ uint32_t shoup_mul(uint32_t l, uint32_t u, uint32_t us, uint32_t n) {
+    const uint32_t q = __umulhi(l, us);
+    uint32_t r = l * u - q * n;  // exact: the true value lies in [0, 3n) < 2^28
+    if (r >= n) r -= n;
+    if (r >= n) r -= n;
+    return r;
 }
 
 // Pivot key: value (26 bits) | (0x3FFFFF - row) (22 bits) | step tag (16 bits).
@@ -80,12 +125,19 @@ struct PanelArgs {
     int R;             // rows per CTA
     ModP M;
     int l_cols;        // L's padded width (PLUQ bound check), <= 0: no check
+    Mont mont;         // for the pivot inverses
     Rec *rec;          // [2][G], keys zero at launch
     int32_t *old_row;  // [2][NB]
     int32_t *piv_row, *piv_val, *piv_inv;  // [NB]
     int *result;       // [0] pivots, [1] status
     int *err;
 };
+
+__device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long long *p) {
+    unsigned long long v;
+    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
 
 __device__ __forceinline__ unsigned long long warp_max_u64(unsigned long long v) {
     for (int o = 16; o; o >>= 1) {
@@ -98,16 +150,20 @@ __device__ __forceinline__ unsigned long long warp_max_u64(unsigned long long v)
 // Cooperative panel factorization.  CTA b owns rows [R0 + b*R, R0 + (b+1)*R)
 // of columns [C0, C0 + nbw) in shared memory.  Per pivot step the CTAs
 // exchange one record each (their best candidate row with its inverse, tagged
-// with the step) through a parity-double-buffered global slot; polling the G
-// tags is the grid barrier, and every CTA then holds every candidate row.
-__global__ void __launch_bounds__(PANEL_THREADS) k_panel(PanelArgs a) {
+// with the step) through a parity-double-buffered global slot: polling the G
+// tags is the grid barrier, then every CTA loads the winning row.  The next
+// pivot column is eliminated first, so the next candidate's inverse (warp 0)
+// overlaps the elimination of the remaining columns (the other warps).
+__global__ void __launch_bounds__(PANEL_THREADS, 1) k_panel(PanelArgs a) {
     extern __shared__ int32_t smem_dyn[];
-    int32_t *P = smem_dyn;                           // R x NB
-    int32_t *crow = smem_dyn + (size_t)a.R * NB;     // G x NB candidate rows
+    int32_t *P = smem_dyn;  // R x NB
     __shared__ unsigned long long keys[MAX_PANEL_CTAS];
     __shared__ uint32_t invs[MAX_PANEL_CTAS];
-    __shared__ int32_t oldr[NB], u[NB];
+    __shared__ __align__(16) int32_t piv[NB];
+    __shared__ __align__(16) int32_t oldr[NB];
+    __shared__ int32_t u[NB];
     __shared__ unsigned long long red[PANEL_WARPS];
+    __shared__ unsigned long long s_best;
     __shared__ int s_stop, s_status, s_prow, s_bw;
     __shared__ uint32_t s_pv, s_inv, s_cinv;
     const int b = blockIdx.x, G = gridDim.x, tid = threadIdx.x;
@@ -116,6 +172,7 @@ __global__ void __launch_bounds__(PANEL_THREADS) k_panel(PanelArgs a) {
     const int rend = min(rbeg + a.R, a.m);
     const int nr = max(rend - rbeg, 0);
     const int nbw = a.nbw;
+    const uint32_t n = a.M.n;
 
     for (int e = tid; e < nr * NB; e += blockDim.x) {
         const int i = e / NB, j = e - (e / NB) * NB;
@@ -126,14 +183,26 @@ __global__ void __launch_bounds__(PANEL_THREADS) k_panel(PanelArgs a) {
         s_status = PS_DONE;
     }
     __syncthreads();
-    // candidate for step 0: column 0 over all own rows
-    unsigned long long best = 0;
-    for (int i = tid; i < nr; i += blockDim.x) {
-        const unsigned long long k = pkey((uint32_t)P[i * NB], rbeg + i);
-        best = k > best ? k : best;
+    // candidate for step 0: column 0 over all own rows, and its inverse
+    {
+        unsigned long long best = 0;
+        for (int i = tid; i < nr; i += blockDim.x) {
+            const unsigned long long k = pkey((uint32_t)P[i * NB], rbeg + i);
+            best = k > best ? k : best;
+        }
+        best = warp_max_u64(best);
+        if (lane == 0) red[wid] = best;
+        __syncthreads();
+        if (wid == 0) {
+            best = lane < PANEL_WARPS ? red[lane] : 0ull;
+            best = warp_max_u64(best);
+            if (lane == 0) {
+                s_best = best;
+                s_cinv = pkey_val(best) ? mod_inverse(pkey_val(best), a.mont) : 0u;
+            }
+        }
+        __syncthreads();
     }
-    best = warp_max_u64(best);
-    if (lane == 0) red[wid] = best;
 
     const int tmax = min(nbw, a.m - a.R0);
     int t = 0;
@@ -142,32 +211,27 @@ __global__ void __launch_bounds__(PANEL_THREADS) k_panel(PanelArgs a) {
         const int par = t & 1;
         const unsigned long long tag = (unsigned long long)(t + 1);
         Rec *mine = a.rec + par * G + b;
-        __syncthreads();  // red[] complete, previous step done
-        // 1. publish: candidate row (and the current row r from its owner); thread 0
-        //    computes the candidate's inverse meanwhile, then writes inverse and tagged key
-        best = 0;
-        for (int w = 0; w < PANEL_WARPS; w++) best = red[w] > best ? red[w] : best;
-        if (best) {
-            const int li = pkey_row(best) - rbeg;
+        // 1. publish the candidate row (and the current row r from its owner), then
+        //    the inverse and the tagged key with release semantics
+        const unsigned long long best0 = s_best;
+        if (best0) {
+            const int li = pkey_row(best0) - rbeg;
             for (int j = tid; j < NB; j += blockDim.x) mine->row[j] = P[li * NB + j];
         }
         if (r >= rbeg && r < rend)
             for (int j = tid; j < NB; j += blockDim.x) a.old_row[par * NB + j] = P[(r - rbeg) * NB + j];
-        if (tid == 0) s_cinv = pkey_val(best) ? mod_inv_euclid(pkey_val(best), a.M.n) : 0;
         __syncthreads();
         if (tid == 0) {
             mine->inv = s_cinv;
-            __threadfence();
-            *(volatile unsigned long long *)&mine->key = best | tag;
+            asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(&mine->key), "l"(best0 | tag) : "memory");
         }
-        // 2. gather every record (this is the grid barrier)
-        const int owner = (r - a.R0) / a.R;
+        // 2. poll the G tagged keys (the grid barrier)
         for (int g = tid; g < G; g += blockDim.x) {
-            const volatile unsigned long long *kp = &a.rec[par * G + g].key;
-            unsigned long long k = *kp;
+            const unsigned long long *kp = &a.rec[par * G + g].key;
+            unsigned long long k = ld_acquire_u64(kp);
             if ((k & 0xFFFFull) != tag) {
                 const unsigned long long t0 = gffm_dev::globaltimer();
-                while (((k = *kp) & 0xFFFFull) != tag) {
+                while (((k = ld_acquire_u64(kp)) & 0xFFFFull) != tag) {
                     if (gffm_dev::globaltimer() - t0 > gffm_dev::kWaitLimitNs) {
                         atomicOr(a.err, 16);
                         s_stop = 1;
@@ -177,19 +241,8 @@ __global__ void __launch_bounds__(PANEL_THREADS) k_panel(PanelArgs a) {
                     }
                 }
             }
-            __threadfence();
             keys[g] = k & ~0xFFFFull;
             invs[g] = (uint32_t)__ldcg(&a.rec[par * G + g].inv);
-            const int4 *src = reinterpret_cast<const int4 *>(a.rec[par * G + g].row);
-            int4 *dst = reinterpret_cast<int4 *>(crow + (size_t)g * NB);
-#pragma unroll
-            for (int q = 0; q < NB / 4; q++) dst[q] = __ldcg(src + q);
-            if (g == owner) {
-                const int4 *os = reinterpret_cast<const int4 *>(a.old_row + par * NB);
-                int4 *od = reinterpret_cast<int4 *>(oldr);
-#pragma unroll
-                for (int q = 0; q < NB / 4; q++) od[q] = __ldcg(os + q);
-            }
         }
         __syncthreads();
         if (s_stop) break;
@@ -223,17 +276,34 @@ __global__ void __launch_bounds__(PANEL_THREADS) k_panel(PanelArgs a) {
                     s_prow = pkey_row(wk);
                     s_bw = wg;
                     s_inv = invs[wg];
+                    if (b == 0) {
+                        a.piv_row[t] = s_prow;
+                        a.piv_val[t] = (int32_t)pv;
+                        a.piv_inv[t] = (int32_t)s_inv;
+                    }
                 }
             }
         }
         __syncthreads();
         if (s_stop) break;
+        // 4. the winning row and the current row r
+        {
+            const int owner = (r - a.R0) / a.R;
+            if (tid < NB / 4)
+                reinterpret_cast<int4 *>(piv)[tid] =
+                    __ldcg(reinterpret_cast<const int4 *>(a.rec[par * G + s_bw].row) + tid);
+            else if (tid < NB / 2 && owner != b)
+                reinterpret_cast<int4 *>(oldr)[tid - NB / 4] =
+                    __ldcg(reinterpret_cast<const int4 *>(a.old_row + par * NB) + (tid - NB / 4));
+            else if (tid < NB / 2)
+                for (int q = 0; q < 4; q++) oldr[(tid - NB / 4) * 4 + q] = P[(r - rbeg) * NB + (tid - NB / 4) * 4 + q];
+        }
+        __syncthreads();
         const int prow = s_prow;
         const uint32_t inv = s_inv;
-        const int32_t *piv = crow + (size_t)s_bw * NB;
         for (int j = tid; j < NB; j += blockDim.x) u[j] = (int32_t)mulmod((uint32_t)piv[j], inv, a.M);
         __syncthreads();
-        // 4. swap_rows_and_mod restricted to the panel: row r <- pivot row (scaled from
+        // 5. swap_rows_and_mod restricted to the panel: row r <- pivot row (scaled from
         //    column t on), row prow <- old row r; the multiplier columns swap unscaled
         if (r >= rbeg && r < rend) {
             int32_t *pr = P + (r - rbeg) * NB;
@@ -244,38 +314,68 @@ __global__ void __launch_bounds__(PANEL_THREADS) k_panel(PanelArgs a) {
             for (int j = tid; j < nbw; j += blockDim.x) pp[j] = oldr[j];
         }
         __syncthreads();
-        // 5. eliminate the rows below the pivot (warps over rows, lanes over columns);
-        //    the multiplier stays in column t; column t+1 gives the next candidate
-        best = 0;
+        // 6. eliminate the rows below the pivot (the multiplier stays in column t).
+        //    a) the next pivot column, one thread per row, and the next candidate
+        const int i0 = max(r + 1 - rbeg, 0);
+        const int jb = t + 1;
         {
-            const int i0 = max(r + 1 - rbeg, 0);
-            const int jb = t + 1;
+            unsigned long long best = 0;
             if (jb < nbw) {
-                for (int i = i0 + wid; i < nr; i += PANEL_WARPS) {
-                    int32_t *pi = P + i * NB;
-                    const uint32_t l = (uint32_t)pi[t];
-                    for (int j = jb + lane; j < nbw; j += 32) {
-                        uint32_t x = (uint32_t)pi[j];
-                        if (l != 0) {
-                            x = (uint32_t)gffm_dev::barrett64((uint64_t)x + (uint64_t)(a.M.n - l) * (uint32_t)u[j],
-                                                              a.M.n, a.M.minv);
-                            pi[j] = (int32_t)x;
-                        }
-                        if (j == jb) {
-                            const unsigned long long k = pkey(x, rbeg + i);
-                            best = k > best ? k : best;
-                        }
+                const uint32_t ub = (uint32_t)u[jb], sb = shoup_pre(ub, a.M);
+                for (int i = i0 + tid; i < nr; i += blockDim.x) {
+                    const uint32_t l = (uint32_t)P[i * NB + t];
+                    uint32_t x = (uint32_t)P[i * NB + jb];
+                    const uint32_t d = shoup_mul(l, ub, sb, n);
+                    x = x >= d ? x - d : x + n - d;
+                    P[i * NB + jb] = (int32_t)x;
+                    const unsigned long long k = pkey(x, rbeg + i);
+                    best = k > best ? k : best;
+                }
+            }
+            best = warp_max_u64(best);
+            if (lane == 0) red[wid] = best;
+            __syncthreads();
+            if (wid == 0) {
+                best = lane < PANEL_WARPS ? red[lane] : 0ull;
+                best = warp_max_u64(best);
+                if (lane == 0) s_best = best;
+            }
+            __syncthreads();
+        }
+        //    b) warp 0: the inverse of the next candidate; warps 1..: columns jb+1..
+        if (wid == 0) {
+            if (lane == 0) {
+                const uint32_t v = pkey_val(s_best);
+                s_cinv = (jb < nbw && v) ? mod_inverse(v, a.mont) : 0u;
+            }
+        } else if (jb + 1 < nbw) {
+            uint32_t uc[CPL], us[CPL];
+#pragma unroll
+            for (int c = 0; c < CPL; c++) {
+                const int j = jb + 1 + lane + 32 * c;
+                uc[c] = j < nbw ? (uint32_t)u[j] : 0u;
+                us[c] = shoup_pre(uc[c], a.M);
+            }
+            for (int i = i0 + wid - 1; i < nr; i += PANEL_WARPS - 1) {
+                int32_t *pi = P + i * NB;
+                const uint32_t l = (uint32_t)pi[t];
+                uint32_t x[CPL];
+#pragma unroll
+                for (int c = 0; c < CPL; c++) {
+                    const int j = jb + 1 + lane + 32 * c;
+                    x[c] = j < nbw ? (uint32_t)pi[j] : 0u;
+                }
+#pragma unroll
+                for (int c = 0; c < CPL; c++) {
+                    const int j = jb + 1 + lane + 32 * c;
+                    if (j < nbw) {
+                        const uint32_t d = shoup_mul(l, uc[c], us[c], n);
+                        pi[j] = (int32_t)(x[c] >= d ? x[c] - d : x[c] + n - d);
                     }
                 }
             }
         }
-        if (b == 0 && tid == 0) {
-            a.piv_row[t] = prow;
-            a.piv_val[t] = (int32_t)s_pv;
-            a.piv_inv[t] = (int32_t)inv;
-        }
-        best = warp_max_u64(best);
-        if (lane == 0) red[wid] = best;
+        __syncthreads();
     }
     __syncthreads();
     for (int e = tid; e < nr * NB; e += blockDim.x) {
@@ -292,20 +392,25 @@ __global__ void __launch_bounds__(PANEL_THREADS) k_panel(PanelArgs a) {
 // pivot values on the diagonal and the multipliers W[R0+i][C0+s] below), one
 // warp per column j by forward substitution:
 //   X[i][j] = inv_i * (delta_ij - sum_{j<=s<i} L11[i][s] X[s][j]).
-// Lanes hold X[s][j] for s = lane, lane + 32; each dot product is a warp sum.
-// Output row-major, ld NB, zero above the diagonal.
+// Lanes hold X[s][j] for s = lane + 32c; each dot product is a warp sum.
+// Output row-major, ld NB, zero above the diagonal.  Dynamic shared memory:
+// NB x (NB + 1) words for L11.
+constexpr size_t LINV_SMEM = (size_t)NB * (NB + 1) * 4;
 __global__ void __launch_bounds__(1024) k_linv(const int32_t *W, int64_t ldw, int R0, int C0, int t,
                                                const int32_t *inv, int32_t *linv, ModP M) {
-    __shared__ uint32_t L11[NB][NB + 1];
+    extern __shared__ uint32_t L11s[];
+    auto L11 = [&](int i, int s) -> uint32_t & { return L11s[i * (NB + 1) + s]; };
     for (int e = threadIdx.x; e < NB * NB; e += blockDim.x) {
         const int i = e / NB, s = e % NB;
-        L11[i][s] = (s < i && i < t) ? (uint32_t)W[(int64_t)(R0 + i) * ldw + C0 + s] : 0;
+        L11(i, s) = (s < i && i < t) ? (uint32_t)W[(int64_t)(R0 + i) * ldw + C0 + s] : 0;
     }
     __syncthreads();
     const int lane = threadIdx.x & 31;
     const int j = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     if (j >= NB) return;
-    uint32_t x0 = 0, x1 = 0;  // X[lane][j], X[lane + 32][j]
+    uint32_t x[CPL];  // X[lane + 32c][j]
+#pragma unroll
+    for (int c = 0; c < CPL; c++) x[c] = 0;
     for (int i = 0; i < NB; i++) {
         uint32_t xi = 0;
         if (i < t && i >= j) {
@@ -313,19 +418,21 @@ __global__ void __launch_bounds__(1024) k_linv(const int32_t *W, int64_t ldw, in
                 xi = (uint32_t)inv[i];
             } else {
                 uint64_t part = 0;
-                if (lane >= j && lane < i) part += (uint64_t)L11[i][lane] * x0;
-                if (lane + 32 >= j && lane + 32 < i) part += (uint64_t)L11[i][lane + 32] * x1;
-                for (int o = 16; o; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
-                const uint32_t a = (uint32_t)gffm_dev::barrett64(part, M.n, M.minv);
+#pragma unroll
+                for (int c = 0; c < CPL; c++) {
+                    const int s = lane + 32 * c;
+                    if (s >= j && s < i) part += (uint64_t)L11(i, s) * x[c];
+                }
+                // reduce each lane's part first: the warp sum of 32 residues fits 32 bits
+                uint32_t p32 = (uint32_t)gffm_dev::barrett64(part, M.n, M.minv);
+                for (int o = 16; o; o >>= 1) p32 += __shfl_xor_sync(0xffffffffu, p32, o);
+                const uint32_t a = (uint32_t)gffm_dev::barrett64(p32, M.n, M.minv);
                 xi = mulmod(a ? M.n - a : 0, (uint32_t)inv[i], M);
             }
         }
-        if (lane == (i & 31)) {
-            if (i < 32)
-                x0 = xi;
-            else
-                x1 = xi;
-        }
+#pragma unroll
+        for (int c = 0; c < CPL; c++)
+            if (lane + 32 * c == i) x[c] = xi;
         if (lane == 0 && i < t) linv[i * NB + j] = (int32_t)xi;
     }
 }
@@ -338,15 +445,22 @@ struct PermArgs {
     int32_t src[MAX_PERM_ROWS];
 };
 
-__global__ void __launch_bounds__(64) k_permute_rows(int32_t *W, int64_t ldw, int c_lo, int c_hi,
-                                                     const __grid_constant__ PermArgs p) {
-    __shared__ int32_t buf[MAX_PERM_ROWS][64];
-    const int j = c_lo + blockIdx.x * 64 + threadIdx.x;
-    const bool ok = j < c_hi;
-    for (int k = 0; k < p.K; k++) buf[k][threadIdx.x] = ok ? W[(int64_t)p.rows[k] * ldw + j] : 0;
-    __syncthreads();
-    if (!ok) return;
-    for (int k = 0; k < p.K; k++) W[(int64_t)p.rows[k] * ldw + j] = buf[p.src[k]][threadIdx.x];
+// Two passes through a K x ncols scratch copy (both fully parallel and coalesced):
+// k_rows_gather: tmp[k][j] = W[rows[k]][c_lo + j];  k_rows_scatter: W[rows[k]][c_lo + j] = tmp[src[k]][j].
+__global__ void __launch_bounds__(256) k_rows_gather(const int32_t *__restrict__ W, int64_t ldw, int c_lo, int ncols,
+                                                     int32_t *__restrict__ tmp, const __grid_constant__ PermArgs p) {
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= (int64_t)p.K * ncols) return;
+    const int k = (int)(e / ncols), j = (int)(e - (int64_t)k * ncols);
+    tmp[e] = W[(int64_t)p.rows[k] * ldw + c_lo + j];
+}
+__global__ void __launch_bounds__(256) k_rows_scatter(int32_t *__restrict__ W, int64_t ldw, int c_lo, int ncols,
+                                                      const int32_t *__restrict__ tmp,
+                                                      const __grid_constant__ PermArgs p) {
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= (int64_t)p.K * ncols) return;
+    const int k = (int)(e / ncols), j = (int)(e - (int64_t)k * ncols);
+    W[(int64_t)p.rows[k] * ldw + c_lo + j] = tmp[(int64_t)p.src[k] * ncols + j];
 }
 
 }  // namespace elim

@@ -24,9 +24,9 @@
 //     skipped columns), then the pivot-row scaling of the skipped columns,
 //   - trailing columns: the row swaps, the triangular solve for the panel rows
 //     U12 = L11^{-1} P A12 (x_t = inv_t * (a_t - sum_{s<t} L[r_t, c_s] x_s):
-//     the reference's scaling and updates in closed form; the panel kernel
-//     builds L11^{-1}) and the update of the rows below, A22 -= L21 * U12 mod N,
-//     both on the limb tensor-core GEMM.
+//     the reference's scaling and updates in closed form; k_linv builds
+//     L11^{-1}) and the update of the rows below, A22 -= L21 * U12 mod N, both
+//     on the limb tensor-core GEMM.
 // W keeps every multiplier column permuted for this arithmetic; the
 // reference's narrower swap width for L (32*cld(m, 32) columns) is restored
 // when L is extracted.
@@ -45,6 +45,7 @@
 namespace elim {
 
 enum Mode { MODE_PLUQ = 0, MODE_LU = 1, MODE_RREF = 2 };
+constexpr int RB = 64;  // pivots per block of the RREF back substitution
 
 // A (column-major, any element type holding integers) -> W (row-major int32 residues)
 template <typename T>
@@ -78,7 +79,7 @@ __global__ void __launch_bounds__(256) k_to_rowmajor(const T *__restrict__ A, in
 }
 
 // Skipped (swapped-in, never eliminated) columns: the panel's row swaps for
-// columns at or beyond lo (those below lo were covered by k_permute_rows), then the
+// columns at or beyond lo (those below lo were covered by permute_rows), then the
 // scaling of every new pivot row, as swap_rows_and_mod does over all columns.
 __global__ void k_skipped(int32_t *W, int64_t ldw, const int32_t *qlist, int nq, int lo, int R0, int t,
                           const int32_t *prow, const int32_t *inv, ModP M) {
@@ -171,36 +172,36 @@ __global__ void k_zero_below(int32_t *W, int64_t ldw, int m, int n, const int32_
 // substitution per column j >= pcol[0]: R[k] = U[k] - sum_{i>k} V[k][i] R[i].
 __global__ void __launch_bounds__(128) k_rref_block(int32_t *W, int64_t ldw, int p0, int nbp, const int32_t *pcol,
                                                     const int32_t *coefbuf, int n, ModP M) {
-    __shared__ uint32_t coef[NB][NB + 1];
-    for (int e = threadIdx.x; e < NB * NB; e += blockDim.x) {
-        int k = e / NB, i = e % NB;
-        coef[k][i] = (k < nbp && i < nbp && i > k) ? (M.n - (uint32_t)coefbuf[k * NB + i]) % M.n : 0;
+    __shared__ uint32_t coef[RB][RB + 1];
+    for (int e = threadIdx.x; e < RB * RB; e += blockDim.x) {
+        int k = e / RB, i = e % RB;
+        coef[k][i] = (k < nbp && i < nbp && i > k) ? (M.n - (uint32_t)coefbuf[k * RB + i]) % M.n : 0;
     }
     __syncthreads();
     const int j = pcol[0] + blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= n) return;
-    uint32_t y[NB];
+    uint32_t y[RB];
 #pragma unroll
-    for (int kk = NB - 1; kk >= 0; kk--) {
+    for (int kk = RB - 1; kk >= 0; kk--) {
         y[kk] = 0;
         if (kk < nbp) {
             uint64_t acc = (uint32_t)W[(int64_t)(p0 + kk) * ldw + j];
 #pragma unroll
-            for (int i = NB - 1; i > kk; i--) acc += (uint64_t)coef[kk][i] * y[i];
+            for (int i = RB - 1; i > kk; i--) acc += (uint64_t)coef[kk][i] * y[i];
             y[kk] = (uint32_t)gffm_dev::barrett64(acc, M.n, M.minv);
         }
     }
 #pragma unroll
-    for (int kk = 0; kk < NB; kk++)
+    for (int kk = 0; kk < RB; kk++)
         if (kk < nbp) W[(int64_t)(p0 + kk) * ldw + j] = (int32_t)y[kk];
 }
 
-// out[k][i] = W[row0 + k][pcol[i]] for k < rows (row-major, ld NB; zero past nbp)
+// out[k][i] = W[row0 + k][pcol[i]] for k < rows (row-major, ld RB; zero past nbp)
 __global__ void k_gather_cols(const int32_t *W, int64_t ldw, int row0, int rows, int nbp, const int32_t *pcol,
                               int32_t *out) {
     const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= rows) return;
-    for (int i = 0; i < NB; i++) out[k * NB + i] = i < nbp ? W[(row0 + k) * ldw + pcol[i]] : 0;
+    for (int i = 0; i < RB; i++) out[k * RB + i] = i < nbp ? W[(row0 + k) * ldw + pcol[i]] : 0;
 }
 
 // ---------------------------------------------------------------------------
@@ -217,6 +218,7 @@ struct Work {
     int32_t *gather;                             // m x NB
     int32_t *coef;                               // NB x NB
     int32_t *linv;                               // NB x NB, inverse of the panel's L11
+    int32_t *ptmp;                               // MAX_PERM_ROWS x n row-permutation scratch
     int32_t *qlist;                              // [n] skipped columns
     __half *dA, *dB;                             // digit planes
     limb::Layout gl;
@@ -235,7 +237,7 @@ static void layout_ws(int64_t m, int64_t n, int64_t lcols, size_t *total, size_t
         (size_t)2 * MAX_PANEL_CTAS * sizeof(Rec),       // rec
         (size_t)NB * NB * 4,                            // linv
         (size_t)2 * NB * 4,                             // old_row
-        0,
+        (size_t)MAX_PERM_ROWS * std::max<int64_t>(n, 1) * 4,  // ptmp (row permutation scratch)
         NB * 4, NB * 4, NB * 4,                         // piv_row/val/inv
         64,                                             // result
         (size_t)std::max<int64_t>(n, 1) * 4,            // colpiv
@@ -261,6 +263,7 @@ static void bind_ws(void *base, int64_t m, int64_t n, int64_t lcols, Work *w) {
     w->rec = (Rec *)(b + off[1]);
     w->linv = (int32_t *)(b + off[2]);
     w->old_row = (int32_t *)(b + off[3]);
+    w->ptmp = (int32_t *)(b + off[4]);
     w->piv_row = (int32_t *)(b + off[5]);
     w->piv_val = (int32_t *)(b + off[6]);
     w->piv_inv = (int32_t *)(b + off[7]);
@@ -309,6 +312,69 @@ static int rowmajor_gemm(Work &w, int64_t N, int32_t *C, int64_t ldc, const int3
     return limb::gemm_digits(g, w.dA, w.dB, cols, rows, k, N, C, ldc, epi, 0, s);
 }
 
+// Apply a composed row permutation to columns [c_lo, c_hi) of W.
+static int permute_rows(Work &w, const PermArgs &perm, int c_lo, int c_hi, cudaStream_t s) {
+    const int ncols = c_hi - c_lo;
+    if (ncols <= 0 || perm.K == 0) return GFFM_OK;
+    const int64_t total = (int64_t)perm.K * ncols;
+    const unsigned blocks = (unsigned)((total + 255) / 256);
+    k_rows_gather<<<blocks, 256, 0, s>>>(w.W, w.ldw, c_lo, ncols, w.ptmp, perm);
+    GFFM_LAUNCH_CHECK("k_rows_gather");
+    k_rows_scatter<<<blocks, 256, 0, s>>>(w.W, w.ldw, c_lo, ncols, w.ptmp, perm);
+    GFFM_LAUNCH_CHECK("k_rows_scatter");
+    return GFFM_OK;
+}
+
+// deterministic Miller-Rabin for 32-bit n (bases 2, 7, 61)
+static bool is_prime_u32(uint32_t n) {
+    if (n < 2) return false;
+    for (uint32_t p : {2u, 3u, 5u, 7u, 11u, 13u, 61u})
+        if (n % p == 0) return n == p;
+    uint32_t d = n - 1;
+    int s = 0;
+    while ((d & 1) == 0) {
+        d >>= 1;
+        s++;
+    }
+    auto powm = [n](uint64_t b, uint32_t e) {
+        uint64_t r = 1;
+        b %= n;
+        while (e) {
+            if (e & 1) r = r * b % n;
+            b = b * b % n;
+            e >>= 1;
+        }
+        return r;
+    };
+    for (uint32_t a : {2u, 7u, 61u}) {
+        uint64_t x = powm(a, d);
+        if (x == 1 || x == n - 1) continue;
+        bool comp = true;
+        for (int i = 1; i < s; i++) {
+            x = x * x % n;
+            if (x == n - 1) {
+                comp = false;
+                break;
+            }
+        }
+        if (comp) return false;
+    }
+    return true;
+}
+
+static Mont make_mont(uint32_t n) {
+    Mont M{};
+    M.n = n;
+    M.prime = (n & 1u) && is_prime_u32(n);
+    if (n & 1u) {
+        uint32_t inv = n;  // Newton iteration for n^{-1} mod 2^32
+        for (int i = 0; i < 5; i++) inv *= 2u - n * inv;
+        M.nprime = 0u - inv;
+        M.r2 = (uint32_t)(((unsigned __int128)1 << 64) % n);
+    }
+    return M;
+}
+
 static int run_panel(Work &w, int m, int n, int R0, int C0, int nbw, const ModP &M, int lcols_check,
                      cudaStream_t s, int h_res[2], std::vector<int32_t> &h_prow, std::vector<int32_t> &h_pv) {
     using namespace gffm;
@@ -317,10 +383,10 @@ static int run_panel(Work &w, int m, int n, int R0, int C0, int nbw, const ModP 
     // rows per CTA: at least 64, and at most 64 CTAs while the rows fit (the per-step
     // exchange moves G candidate rows into every CTA)
     int R = 64;
-    while ((rows + R - 1) / R > std::min(sms, 64) && R < 640) R += 32;
+    while ((rows + R - 1) / R > std::min(sms, 128) && R < 640) R += 32;
     while ((rows + R - 1) / R > std::min(sms, MAX_PANEL_CTAS)) R += 32;
     const int G = std::max(1, (rows + R - 1) / R);
-    const size_t smem = ((size_t)R + G) * NB * 4;
+    const size_t smem = (size_t)R * NB * 4;
     if (smem > 200 * 1024)
         return set_error(GFFM_ERR_UNSUPPORTED, "elimination panel: %d rows exceed the panel kernel's capacity", rows);
     GFFM_CUDA(cudaMemsetAsync(w.rec, 0, (size_t)2 * G * sizeof(Rec), s));
@@ -335,6 +401,7 @@ static int run_panel(Work &w, int m, int n, int R0, int C0, int nbw, const ModP 
     a.R = R;
     a.M = M;
     a.l_cols = lcols_check;
+    a.mont = make_mont(M.n);
     a.rec = w.rec;
     a.old_row = w.old_row;
     a.piv_row = w.piv_row;
@@ -407,8 +474,8 @@ static int forward(Work &w, int m, int n, int64_t N, int mode, int lcols, cudaSt
             // narrower L swap width is restored when L is extracted)
             const int left_hi = col;
             if (left_hi > 0) {
-                k_permute_rows<<<(left_hi + 63) / 64, 64, 0, s>>>(w.W, w.ldw, 0, left_hi, perm);
-                GFFM_LAUNCH_CHECK("k_permute_rows(left)");
+                st = permute_rows(w, perm, 0, left_hi, s);
+                if (st) return st;
             }
             if (!skipped.empty()) {
                 // skipped columns hold A values: row swaps at every width, then the
@@ -421,10 +488,11 @@ static int forward(Work &w, int m, int n, int64_t N, int mode, int lcols, cudaSt
             // trailing columns: swaps, triangular solve, update of the rows below
             const int cs = col + nbw;
             if (cs < n) {
-                k_permute_rows<<<(n - cs + 63) / 64, 64, 0, s>>>(w.W, w.ldw, cs, n, perm);
-                GFFM_LAUNCH_CHECK("k_permute_rows(trailing)");
+                st = permute_rows(w, perm, cs, n, s);
+                if (st) return st;
                 // U12 = L11^{-1} P A12
-                k_linv<<<2, 1024, 0, s>>>(w.W, w.ldw, row, col, t, w.piv_inv, w.linv, M);
+                GFFM_CUDA(cudaFuncSetAttribute(k_linv, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)LINV_SMEM));
+                k_linv<<<NB / 32, 1024, LINV_SMEM, s>>>(w.W, w.ldw, row, col, t, w.piv_inv, w.linv, M);
                 GFFM_LAUNCH_CHECK("k_linv");
                 st = rowmajor_gemm(w, N, w.W + (int64_t)row * w.ldw + cs, w.ldw, w.linv, NB,
                                    w.W + (int64_t)row * w.ldw + cs, w.ldw, t, n - cs, t, limb::EPI_STORE_I32, s);
@@ -469,8 +537,8 @@ static int backward(Work &w, int m, int n, int64_t N, const Result &res, cudaStr
     using namespace gffm;
     ModP M{(uint32_t)N, ~uint64_t(0) / (uint64_t)N};
     const int r = res.rank;
-    for (int end = r; end > 0; end -= NB) {
-        const int p0 = std::max(0, end - NB);
+    for (int end = r; end > 0; end -= RB) {
+        const int p0 = std::max(0, end - RB);
         const int nbp = end - p0;
         std::vector<int32_t> pc(nbp);
         for (int i = 0; i < nbp; i++) pc[i] = res.piv_c[p0 + i];
@@ -483,7 +551,7 @@ static int backward(Work &w, int m, int n, int64_t N, const Result &res, cudaStr
         if (p0 > 0) {
             k_gather_cols<<<(p0 + 127) / 128, 128, 0, s>>>(w.W, w.ldw, 0, p0, nbp, w.pcol, w.gather);
             GFFM_LAUNCH_CHECK("k_gather_cols");
-            int st = rowmajor_gemm(w, N, w.W + c0, w.ldw, w.gather, NB, w.W + (int64_t)p0 * w.ldw + c0, w.ldw,
+            int st = rowmajor_gemm(w, N, w.W + c0, w.ldw, w.gather, RB, w.W + (int64_t)p0 * w.ldw + c0, w.ldw,
                                    p0, n - c0, nbp, limb::EPI_SUB_I32, s);
             if (st) return st;
         }

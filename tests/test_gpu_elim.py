@@ -59,7 +59,8 @@ def make(kind, m, n, N, rng):
 CASES = [
     ("uniform", 1, 1, 7), ("uniform", 5, 5, 7), ("uniform", 33, 20, 3), ("uniform", 64, 64, 65521),
     ("uniform", 65, 65, P26), ("uniform", 130, 129, 2080639), ("uniform", 200, 300, P25), ("uniform", 300, 100, 11),
-    ("uniform", 257, 257, 2 ** 20), ("uniform", 100, 100, 1000),
+    ("uniform", 257, 257, 2 ** 20), ("uniform", 100, 100, 1000), ("uniform", 90, 90, 255255),
+    ("uniform", 20, 20, 2), ("uniform", 150, 150, 3),
     ("rank30", 96, 96, P26), ("rank70", 150, 140, 7), ("rank1", 40, 40, 5),
     ("zero_cols", 40, 40, 13), ("zero_cols", 100, 130, 65521), ("lead_zero", 70, 80, 7),
     ("ties", 70, 70, 3), ("ties", 130, 90, 11), ("zeros", 10, 12, 7), ("tall_low", 90, 90, P26),
