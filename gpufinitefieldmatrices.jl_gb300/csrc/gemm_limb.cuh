@@ -66,6 +66,7 @@ struct Params {
     int32_t W[MAX_SHIFTS]; // 2^(7s) mod N
     void *C;
     int64_t ldc;
+    const double *X, *Y;   // EPI_KSUB_F64 subtrahends
     int *err;
 };
 
@@ -251,15 +252,29 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
                     uint32_t v[32];
                     gffm_dev::tmem_ld_32x32b_x32(tmem + ((uint32_t)(quad * 32) << 16) + 64 * s + 32 * half, v);
                     gffm_dev::tmem_ld_wait();
-                    const int w = p.W[s];
+                    if (EPI == EPI_EXACT_I64) {
+                        // exact chunk value sum_s C_s 2^(7s), in [0, 2^62) for raw digits: wrapping
+                        // 64-bit sums are exact once every shift has been added
 #pragma unroll
-                    for (int j = 0; j < 32; j++) acc[j] += (int64_t)__float2int_rz(__uint_as_float(v[j])) * w;
+                        for (int j = 0; j < 32; j++)
+                            acc[j] = (int64_t)((uint64_t)acc[j] +
+                                               ((uint64_t)(int64_t)__float2int_rz(__uint_as_float(v[j])) << (7 * s)));
+                    } else {
+                        const int w = p.W[s];
+#pragma unroll
+                        for (int j = 0; j < 32; j++) acc[j] += (int64_t)__float2int_rz(__uint_as_float(v[j])) * w;
+                    }
                 }
                 gffm_dev::tc_fence_before();
                 __syncwarp();
                 if (lane == 0) gffm_dev::mbar_arrive(&acc_empty_bar);
                 acc_phase ^= 1;
-                if ((chunk & 63) == 63) {
+                if (EPI == EPI_EXACT_I64) {
+                    // acc < N < 2^52 before the chunk, so acc + chunk < 2^63: one Barrett step
+#pragma unroll
+                    for (int j = 0; j < 32; j++)
+                        acc[j] = (int64_t)gffm_dev::barrett64((uint64_t)acc[j], (uint64_t)p.N, p.minv);
+                } else if ((chunk & 63) == 63) {
 #pragma unroll
                     for (int j = 0; j < 32; j++) acc[j] = reduce_signed(acc[j], p);
                 }
@@ -279,6 +294,27 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
                         if (col0 + j < p.n) {
                             const int64_t v = (int64_t)cv[j] - reduce_signed(acc[j], p);
                             cbase[j * p.ldc] = (int32_t)(v < 0 ? v + p.N : v);
+                        }
+                    }
+                } else if (EPI == EPI_EXACT_I64) {
+                    int64_t *cbase = (int64_t *)p.C + row + col0 * p.ldc;
+#pragma unroll
+                    for (int j = 0; j < 32; j++)
+                        if (col0 + j < p.n) cbase[j * p.ldc] = acc[j];
+                } else if (EPI == EPI_KSUB_F64) {
+                    // C = (AB - X - Y) mod N: all subtrahend loads before any store
+                    const int64_t base = row + col0 * p.ldc;
+                    double xv[32];
+#pragma unroll
+                    for (int j = 0; j < 32; j++)
+                        xv[j] = (col0 + j < p.n) ? __ldcg(p.X + base + j * p.ldc) + __ldcg(p.Y + base + j * p.ldc) : 0.0;
+#pragma unroll
+                    for (int j = 0; j < 32; j++) {
+                        if (col0 + j < p.n) {
+                            int64_t v = reduce_signed(acc[j], p) - (int64_t)xv[j];   // X + Y < 2N, exact in double
+                            v += (v < 0) ? p.N : 0;
+                            v += (v < 0) ? p.N : 0;
+                            ((double *)p.C)[base + j * p.ldc] = (double)v;
                         }
                     }
                 } else {
@@ -315,9 +351,9 @@ struct ModN {
     uint64_t minv;
 };
 
-// residue of an integer-valued element, centred into (-N/2, N/2]
+// residue of an integer-valued element in [0, N)
 template <typename T>
-__device__ __forceinline__ int32_t centred(T v, const ModN &M) {
+__device__ __forceinline__ int32_t residue(T v, const ModN &M) {
     int64_t x = (int64_t)v;
     int64_t r;
     if (x >= 0 && x < M.n) {
@@ -328,8 +364,19 @@ __device__ __forceinline__ int32_t centred(T v, const ModN &M) {
         uint64_t q = gffm_dev::barrett64((uint64_t)(-x), (uint64_t)M.n, M.minv);
         r = q ? M.n - (int64_t)q : 0;
     }
-    if (2 * r > M.n) r -= M.n;
     return (int32_t)r;
+}
+
+// the value a split of mode MODE encodes for element v (and v2, SPLIT_SUM)
+template <int MODE, typename T>
+__device__ __forceinline__ int32_t split_value(T v, T v2, const ModN &M) {
+    int32_t r = residue(v, M);
+    if (MODE == SPLIT_RAW) return r;
+    if (MODE == SPLIT_SUM) {
+        r += residue(v2, M);
+        if (r >= M.n) r -= (int32_t)M.n;
+    }
+    return (2 * (int64_t)r > M.n) ? r - (int32_t)M.n : r;
 }
 
 template <int L>
@@ -343,16 +390,21 @@ __device__ __forceinline__ void digits(int32_t c, __half (&d)[L]) {
 }
 
 // A (m x k, column-major, lda) -> digit planes D[l][r][kk] (K-major, Mpad x Kpad per plane)
-template <typename T, int L>
-__global__ void __launch_bounds__(256) k_split_a(const T *__restrict__ A, int64_t lda, int m, int k, __half *__restrict__ D,
-                                                 int Mpad, int Kpad, ModN M) {
+template <typename T, int L, int MODE>
+__global__ void __launch_bounds__(256) k_split_a(const T *__restrict__ A, const T *__restrict__ A2, int64_t lda, int m,
+                                                 int k, __half *__restrict__ D, int Mpad, int Kpad, ModN M) {
     __shared__ int32_t tile[32][33];
     const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
     const int64_t r0 = (int64_t)blockIdx.y * 32, k0 = (int64_t)blockIdx.x * 32;
 #pragma unroll
     for (int i = 0; i < 4; i++) {
         int64_t kk = k0 + ty + 8 * i, r = r0 + tx;
-        tile[ty + 8 * i][tx] = (r < m && kk < k) ? centred(A[r + kk * lda], M) : 0;
+        int32_t v = 0;
+        if (r < m && kk < k) {
+            const int64_t off = r + kk * lda;
+            v = split_value<MODE>(A[off], MODE == SPLIT_SUM ? A2[off] : T(0), M);
+        }
+        tile[ty + 8 * i][tx] = v;
     }
     __syncthreads();
     const size_t plane = (size_t)Mpad * Kpad;
@@ -367,17 +419,18 @@ __global__ void __launch_bounds__(256) k_split_a(const T *__restrict__ A, int64_
 }
 
 // B (k x n, column-major, ldb) -> digit planes D[l][c][kk] (K-major, Npad x Kpad per plane)
-template <typename T, int L>
-__global__ void __launch_bounds__(256) k_split_b(const T *__restrict__ B, int64_t ldb, int k, int n, __half *__restrict__ D,
-                                                 int Npad, int Kpad, ModN M) {
+template <typename T, int L, int MODE>
+__global__ void __launch_bounds__(256) k_split_b(const T *__restrict__ B, const T *__restrict__ B2, int64_t ldb, int k,
+                                                 int n, __half *__restrict__ D, int Npad, int Kpad, ModN M) {
     const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;  // pair index
     const int64_t pairs_per_col = Kpad / 2;
     const int64_t total = pairs_per_col * Npad;
     if (idx >= total) return;
     const int64_t c = idx / pairs_per_col;
     const int64_t kk = (idx - c * pairs_per_col) * 2;
-    int32_t v0 = (c < n && kk < k) ? centred(B[kk + c * ldb], M) : 0;
-    int32_t v1 = (c < n && kk + 1 < k) ? centred(B[kk + 1 + c * ldb], M) : 0;
+    const int64_t off = kk + c * ldb;
+    int32_t v0 = (c < n && kk < k) ? split_value<MODE>(B[off], MODE == SPLIT_SUM ? B2[off] : T(0), M) : 0;
+    int32_t v1 = (c < n && kk + 1 < k) ? split_value<MODE>(B[off + 1], MODE == SPLIT_SUM ? B2[off + 1] : T(0), M) : 0;
     __half d0[L], d1[L];
     digits<L>(v0, d0);
     digits<L>(v1, d1);

@@ -46,9 +46,17 @@ int limbs_for(int64_t N) {
     return 4;
 }
 
-Layout layout(int64_t m, int64_t n, int64_t k, int64_t N) {
+int raw_limbs_for(int64_t N) {
+    // largest non-centred residue N - 1 must fit L balanced base-128 digits
+    if (N <= 64) return 1;
+    if (N <= 8128) return 2;
+    if (N <= 1040320) return 3;
+    return 4;
+}
+
+Layout layout_L(int64_t m, int64_t n, int64_t k, int L) {
     Layout g;
-    g.L = limbs_for(N);
+    g.L = L;
     g.Mpad = gffm::round_up(m > 0 ? m : 1, BM);
     g.Npad = gffm::round_up(n > 0 ? n : 1, BN);
     g.Kpad = gffm::round_up(k > 0 ? k : 1, BK);
@@ -56,6 +64,8 @@ Layout layout(int64_t m, int64_t n, int64_t k, int64_t N) {
     g.b_bytes = (size_t)g.L * g.Npad * g.Kpad * 2;
     return g;
 }
+
+Layout layout(int64_t m, int64_t n, int64_t k, int64_t N) { return layout_L(m, n, k, limbs_for(N)); }
 
 int check_args(int64_t m, int64_t n, int64_t k, int64_t lda, int64_t ldb, int64_t ldc, int64_t N) {
     using gffm::set_error;
@@ -69,30 +79,77 @@ int check_args(int64_t m, int64_t n, int64_t k, int64_t lda, int64_t ldb, int64_
     return GFFM_OK;
 }
 
-template <typename T>
-int split_a(const T *A, int64_t lda, int64_t m, int64_t k, __half *D, const Layout &g, int64_t N, cudaStream_t s) {
-    ModN M{N, ~uint64_t(0) / (uint64_t)N};
+template <typename T, int MODE>
+static void launch_split_a(const T *A, const T *A2, int64_t lda, int64_t m, int64_t k, __half *D, const Layout &g,
+                           ModN M, cudaStream_t s) {
     dim3 grid((unsigned)(g.Kpad / 32), (unsigned)(g.Mpad / 32));
+    const int mm = (int)m, kk = (int)k, Mp = (int)g.Mpad, Kp = (int)g.Kpad;
     switch (g.L) {
-        case 1: k_split_a<T, 1><<<grid, 256, 0, s>>>(A, lda, (int)m, (int)k, D, (int)g.Mpad, (int)g.Kpad, M); break;
-        case 2: k_split_a<T, 2><<<grid, 256, 0, s>>>(A, lda, (int)m, (int)k, D, (int)g.Mpad, (int)g.Kpad, M); break;
-        case 3: k_split_a<T, 3><<<grid, 256, 0, s>>>(A, lda, (int)m, (int)k, D, (int)g.Mpad, (int)g.Kpad, M); break;
-        default: k_split_a<T, 4><<<grid, 256, 0, s>>>(A, lda, (int)m, (int)k, D, (int)g.Mpad, (int)g.Kpad, M); break;
+        case 1: k_split_a<T, 1, MODE><<<grid, 256, 0, s>>>(A, A2, lda, mm, kk, D, Mp, Kp, M); break;
+        case 2: k_split_a<T, 2, MODE><<<grid, 256, 0, s>>>(A, A2, lda, mm, kk, D, Mp, Kp, M); break;
+        case 3: k_split_a<T, 3, MODE><<<grid, 256, 0, s>>>(A, A2, lda, mm, kk, D, Mp, Kp, M); break;
+        default: k_split_a<T, 4, MODE><<<grid, 256, 0, s>>>(A, A2, lda, mm, kk, D, Mp, Kp, M); break;
+    }
+}
+
+template <typename T, int MODE>
+static void launch_split_b(const T *B, const T *B2, int64_t ldb, int64_t k, int64_t n, __half *D, const Layout &g,
+                           ModN M, cudaStream_t s) {
+    int64_t total = (g.Kpad / 2) * g.Npad;
+    unsigned blocks = (unsigned)((total + 255) / 256);
+    const int kk = (int)k, nn = (int)n, Np = (int)g.Npad, Kp = (int)g.Kpad;
+    switch (g.L) {
+        case 1: k_split_b<T, 1, MODE><<<blocks, 256, 0, s>>>(B, B2, ldb, kk, nn, D, Np, Kp, M); break;
+        case 2: k_split_b<T, 2, MODE><<<blocks, 256, 0, s>>>(B, B2, ldb, kk, nn, D, Np, Kp, M); break;
+        case 3: k_split_b<T, 3, MODE><<<blocks, 256, 0, s>>>(B, B2, ldb, kk, nn, D, Np, Kp, M); break;
+        default: k_split_b<T, 4, MODE><<<blocks, 256, 0, s>>>(B, B2, ldb, kk, nn, D, Np, Kp, M); break;
+    }
+}
+
+// the raw and summed splits serve the Karatsuba products, which take Float64 digits only
+static int check_mode(int mode, bool is_double, const void *second) {
+    if (mode == SPLIT_CENTRED) return GFFM_OK;
+    if (!is_double || (mode != SPLIT_RAW && mode != SPLIT_SUM))
+        return gffm::set_error(GFFM_ERR_UNSUPPORTED, "digit split mode %d is not available for this element type", mode);
+    if (mode == SPLIT_SUM && !second) return gffm::set_error(GFFM_ERR_ARG, "summed digit split without a second operand");
+    return GFFM_OK;
+}
+
+template <typename T>
+int split_a(const T *A, int64_t lda, int64_t m, int64_t k, __half *D, const Layout &g, int64_t N, cudaStream_t s,
+            int mode, const T *A2) {
+    int st = check_mode(mode, sizeof(T) == 8, A2);
+    if (st) return st;
+    ModN M{N, ~uint64_t(0) / (uint64_t)N};
+    if constexpr (sizeof(T) == 8) {
+        if (mode == SPLIT_RAW)
+            launch_split_a<T, SPLIT_RAW>(A, A2, lda, m, k, D, g, M, s);
+        else if (mode == SPLIT_SUM)
+            launch_split_a<T, SPLIT_SUM>(A, A2, lda, m, k, D, g, M, s);
+        else
+            launch_split_a<T, SPLIT_CENTRED>(A, A2, lda, m, k, D, g, M, s);
+    } else {
+        launch_split_a<T, SPLIT_CENTRED>(A, A2, lda, m, k, D, g, M, s);
     }
     GFFM_LAUNCH_CHECK("k_split_a");
     return GFFM_OK;
 }
 
 template <typename T>
-int split_b(const T *B, int64_t ldb, int64_t k, int64_t n, __half *D, const Layout &g, int64_t N, cudaStream_t s) {
+int split_b(const T *B, int64_t ldb, int64_t k, int64_t n, __half *D, const Layout &g, int64_t N, cudaStream_t s,
+            int mode, const T *B2) {
+    int st = check_mode(mode, sizeof(T) == 8, B2);
+    if (st) return st;
     ModN M{N, ~uint64_t(0) / (uint64_t)N};
-    int64_t total = (g.Kpad / 2) * g.Npad;
-    unsigned blocks = (unsigned)((total + 255) / 256);
-    switch (g.L) {
-        case 1: k_split_b<T, 1><<<blocks, 256, 0, s>>>(B, ldb, (int)k, (int)n, D, (int)g.Npad, (int)g.Kpad, M); break;
-        case 2: k_split_b<T, 2><<<blocks, 256, 0, s>>>(B, ldb, (int)k, (int)n, D, (int)g.Npad, (int)g.Kpad, M); break;
-        case 3: k_split_b<T, 3><<<blocks, 256, 0, s>>>(B, ldb, (int)k, (int)n, D, (int)g.Npad, (int)g.Kpad, M); break;
-        default: k_split_b<T, 4><<<blocks, 256, 0, s>>>(B, ldb, (int)k, (int)n, D, (int)g.Npad, (int)g.Kpad, M); break;
+    if constexpr (sizeof(T) == 8) {
+        if (mode == SPLIT_RAW)
+            launch_split_b<T, SPLIT_RAW>(B, B2, ldb, k, n, D, g, M, s);
+        else if (mode == SPLIT_SUM)
+            launch_split_b<T, SPLIT_SUM>(B, B2, ldb, k, n, D, g, M, s);
+        else
+            launch_split_b<T, SPLIT_CENTRED>(B, B2, ldb, k, n, D, g, M, s);
+    } else {
+        launch_split_b<T, SPLIT_CENTRED>(B, B2, ldb, k, n, D, g, M, s);
     }
     GFFM_LAUNCH_CHECK("k_split_b");
     return GFFM_OK;
@@ -120,7 +177,10 @@ static int launch_gemm(int L, const CUtensorMap &ta, const CUtensorMap &tb, cons
 }
 
 int gemm_digits(const Layout &g, const __half *Ad, const __half *Bd, int64_t m, int64_t n, int64_t k, int64_t N,
-                void *C, int64_t ldc, int epi, int max_ctas, cudaStream_t s) {
+                void *C, int64_t ldc, int epi, int max_ctas, cudaStream_t s, const double *X, const double *Y) {
+    if (epi == EPI_KSUB_F64 && (!X || !Y)) return gffm::set_error(GFFM_ERR_ARG, "subtracting epilogue without X, Y");
+    if (N < 2 || N >= (epi == EPI_EXACT_I64 ? (int64_t(1) << 52) : (int64_t(1) << 26)))
+        return gffm::set_error(GFFM_ERR_MODULUS, "modulus %lld out of range for epilogue %d", (long long)N, epi);
     int st = get_encoder();
     if (st) return st;
     CUtensorMap ta, tb;
@@ -142,11 +202,13 @@ int gemm_digits(const Layout &g, const __half *Ad, const __half *Bd, int64_t m, 
     p.bias = N * (((int64_t(1) << 60) + N - 1) / N);
     int64_t w = 1 % N;
     for (int sft = 0; sft < MAX_SHIFTS; sft++) {
-        p.W[sft] = (int32_t)w;
-        w = (w * 128) % N;
+        p.W[sft] = (int32_t)w;      // unused by EPI_EXACT_I64, whose N may exceed 32 bits
+        w = (int64_t)(((__int128)w * 128) % N);
     }
     p.C = C;
     p.ldc = ldc;
+    p.X = X;
+    p.Y = Y;
     p.err = gffm::device_error_flag();
     if (!p.err) return gffm::check_device();
     int ntiles = p.mtiles * p.ntiles;
@@ -158,16 +220,24 @@ int gemm_digits(const Layout &g, const __half *Ad, const __half *Bd, int64_t m, 
         case EPI_STORE_F64: return launch_gemm<EPI_STORE_F64>(g.L, ta, tb, p, grid, s);
         case EPI_STORE_F32: return launch_gemm<EPI_STORE_F32>(g.L, ta, tb, p, grid, s);
         case EPI_STORE_I32: return launch_gemm<EPI_STORE_I32>(g.L, ta, tb, p, grid, s);
+        case EPI_EXACT_I64: return launch_gemm<EPI_EXACT_I64>(g.L, ta, tb, p, grid, s);
+        case EPI_KSUB_F64: return launch_gemm<EPI_KSUB_F64>(g.L, ta, tb, p, grid, s);
         default: return launch_gemm<EPI_SUB_I32>(g.L, ta, tb, p, grid, s);
     }
 }
 
-template int split_a<double>(const double *, int64_t, int64_t, int64_t, __half *, const Layout &, int64_t, cudaStream_t);
-template int split_a<float>(const float *, int64_t, int64_t, int64_t, __half *, const Layout &, int64_t, cudaStream_t);
-template int split_a<int32_t>(const int32_t *, int64_t, int64_t, int64_t, __half *, const Layout &, int64_t, cudaStream_t);
-template int split_b<double>(const double *, int64_t, int64_t, int64_t, __half *, const Layout &, int64_t, cudaStream_t);
-template int split_b<float>(const float *, int64_t, int64_t, int64_t, __half *, const Layout &, int64_t, cudaStream_t);
-template int split_b<int32_t>(const int32_t *, int64_t, int64_t, int64_t, __half *, const Layout &, int64_t, cudaStream_t);
+template int split_a<double>(const double *, int64_t, int64_t, int64_t, __half *, const Layout &, int64_t, cudaStream_t,
+                            int, const double *);
+template int split_a<float>(const float *, int64_t, int64_t, int64_t, __half *, const Layout &, int64_t, cudaStream_t,
+                            int, const float *);
+template int split_a<int32_t>(const int32_t *, int64_t, int64_t, int64_t, __half *, const Layout &, int64_t, cudaStream_t,
+                            int, const int32_t *);
+template int split_b<double>(const double *, int64_t, int64_t, int64_t, __half *, const Layout &, int64_t, cudaStream_t,
+                            int, const double *);
+template int split_b<float>(const float *, int64_t, int64_t, int64_t, __half *, const Layout &, int64_t, cudaStream_t,
+                            int, const float *);
+template int split_b<int32_t>(const int32_t *, int64_t, int64_t, int64_t, __half *, const Layout &, int64_t, cudaStream_t,
+                            int, const int32_t *);
 
 }  // namespace limb
 

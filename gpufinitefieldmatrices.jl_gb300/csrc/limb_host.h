@@ -9,8 +9,19 @@
 
 namespace limb {
 
-// epilogue of the GEMM: store Float64 / Float32 / int32 residues, or C = (C - AB) mod N on int32
-enum Epi { EPI_STORE_F64 = 0, EPI_STORE_F32 = 1, EPI_SUB_I32 = 2, EPI_STORE_I32 = 3 };
+// epilogue of the GEMM:
+//   EPI_STORE_F64 / F32 / I32  C = AB mod N stored as Float64 / Float32 / int32
+//   EPI_SUB_I32                C = (C - AB) mod N on int32
+//   EPI_EXACT_I64              C = AB mod N on int64 for 2 <= N < 2^52, from NON-centred digits
+//                              (SPLIT_RAW): every exact chunk value is folded in modulo N
+//   EPI_KSUB_F64               C = (AB - X - Y) mod N on Float64, X and Y Float64 residues with C's ldc
+enum Epi { EPI_STORE_F64 = 0, EPI_STORE_F32 = 1, EPI_SUB_I32 = 2, EPI_STORE_I32 = 3, EPI_EXACT_I64 = 4, EPI_KSUB_F64 = 5 };
+
+// digit split of an operand:
+//   SPLIT_CENTRED  x mod N centred into (-N/2, N/2]
+//   SPLIT_RAW      x mod N in [0, N)            (needs raw_limbs_for(N) digits)
+//   SPLIT_SUM      (x + y) mod N centred, y from a second array with the same leading dimension
+enum Split { SPLIT_CENTRED = 0, SPLIT_RAW = 1, SPLIT_SUM = 2 };
 
 struct Layout {
     int L;                 // digits per residue
@@ -19,17 +30,22 @@ struct Layout {
 };
 
 int limbs_for(int64_t N);
+int raw_limbs_for(int64_t N);
 Layout layout(int64_t m, int64_t n, int64_t k, int64_t N);
+Layout layout_L(int64_t m, int64_t n, int64_t k, int L);
 int check_args(int64_t m, int64_t n, int64_t k, int64_t lda, int64_t ldb, int64_t ldc, int64_t N);
 
-// digit planes of A (m x k) / B (k x n), column-major inputs of type T
+// digit planes of A (m x k) / B (k x n), column-major inputs of type T; A2 / B2 only for SPLIT_SUM
 template <typename T>
-int split_a(const T *A, int64_t lda, int64_t m, int64_t k, __half *D, const Layout &g, int64_t N, cudaStream_t s);
+int split_a(const T *A, int64_t lda, int64_t m, int64_t k, __half *D, const Layout &g, int64_t N, cudaStream_t s,
+            int mode = SPLIT_CENTRED, const T *A2 = nullptr);
 template <typename T>
-int split_b(const T *B, int64_t ldb, int64_t k, int64_t n, __half *D, const Layout &g, int64_t N, cudaStream_t s);
+int split_b(const T *B, int64_t ldb, int64_t k, int64_t n, __half *D, const Layout &g, int64_t N, cudaStream_t s,
+            int mode = SPLIT_CENTRED, const T *B2 = nullptr);
 
-// C (m x n, ldc) <- epilogue(A*B mod N) from digit planes; epi is a limb::Epi
+// C (m x n, ldc) <- epilogue(A*B mod N) from digit planes; epi is a limb::Epi.  X, Y: EPI_KSUB_F64 only.
 int gemm_digits(const Layout &g, const __half *Ad, const __half *Bd, int64_t m, int64_t n, int64_t k, int64_t N,
-                void *C, int64_t ldc, int epi, int max_ctas, cudaStream_t s);
+                void *C, int64_t ldc, int epi, int max_ctas, cudaStream_t s, const double *X = nullptr,
+                const double *Y = nullptr);
 
 }  // namespace limb

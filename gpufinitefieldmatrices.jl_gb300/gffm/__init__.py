@@ -18,3 +18,28 @@ from .elimination import (  # noqa: F401,E402
     pluq_gpu_kernel, lu_gpu_type, rref_gpu_type, apply_col_perm_, apply_col_inv_perm_, apply_col_perm,
     apply_row_perm_, apply_row_inv_perm_, apply_row_perm, perm_array_to_matrix,
 )
+from . import cumod as _cumod, karatsuba as _karatsuba  # noqa: E402
+from .karatsuba import (  # noqa: F401,E402
+    KaratsubaArray, KaratsubaMatrix, KaratsubaVector, KaratsubaZeros, KaratsubaMatrix_from, Karatsubacopy,
+    initialize_plan_, KMatMul_, KMatMul_gemv_, MatToKMat, KMatToMat, poly_karatsuba_matmul, scalar_multiply_,
+    find_max_ops, find_max_ops_karatsuba, nKMuls,
+)
+
+
+def _dispatch(name):
+    """Julia's multiple dispatch for the names both types define (add!, sub!, negate!, zero!, copy!)."""
+    on_mod, on_k = getattr(_cumod, name), getattr(_karatsuba, name)
+
+    def f(*args, **kw):
+        return (on_k if isinstance(args[0], KaratsubaArray) else on_mod)(*args, **kw)
+
+    f.__name__ = name
+    f.__doc__ = "%s for CuModArray (%s) or KaratsubaArray (%s)" % (name, on_mod.__doc__, on_k.__doc__)
+    return f
+
+
+add_ = _dispatch("add_")
+sub_ = _dispatch("sub_")
+negate_ = _dispatch("negate_")
+zero_ = _dispatch("zero_")
+copy_ = _dispatch("copy_")

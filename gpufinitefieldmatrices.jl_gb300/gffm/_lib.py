@@ -54,6 +54,20 @@ for _op in ("scalar_add", "scalar_sub", "rscalar_sub", "scalar_mul"):
     SIGNATURES["gffm_%s_f32" % _op] = (_INT, [_P, _P, _F, _I64, _I64, _P])
 SIGNATURES["gffm_mod_f64"] = (_INT, [_P, _P, _I64, _I64, _P])
 SIGNATURES["gffm_mod_f32"] = (_INT, [_P, _P, _I64, _I64, _P])
+SIGNATURES.update({
+    "gffm_karatsuba_workspace_size": (_INT, [_I64, _I64, _I64, _I64, _I64, _PSZ]),
+    "gffm_karatsuba_matmul_f64": (_INT, [_I64, _I64, _I64, _P, _P, _I64, _P, _P, _I64, _P, _P, _I64, _I64, _I64,
+                                         _P, _SZ, _P]),
+    "gffm_karatsuba_poly_workspace_size": (_INT, [_I64, _I64, _I64, _I64, _PSZ]),
+    "gffm_karatsuba_poly_matmul_f64": (_INT, [_I64, _I64, _I64, _P, _P, _I64, _P, _P, _I64, _P, _P, _P, _I64, _I64,
+                                              _P, _SZ, _P]),
+    "gffm_karatsuba_add_f64": (_INT, [_P, _P, _P, _P, _P, _P, _I64, _I64, _I64, _P]),
+    "gffm_karatsuba_sub_f64": (_INT, [_P, _P, _P, _P, _P, _P, _I64, _I64, _I64, _P]),
+    "gffm_karatsuba_negate_f64": (_INT, [_P, _P, _P, _P, _I64, _I64, _I64, _P]),
+    "gffm_karatsuba_scalar_mul_f64": (_INT, [_P, _P, _P, _P, _I64, _I64, _I64, _I64, _P]),
+    "gffm_karatsuba_from_values_f64": (_INT, [_P, _P, _P, _I64, _I64, _I64, _P]),
+    "gffm_karatsuba_to_values_f64": (_INT, [_P, _P, _P, _I64, _I64, _I64, _P]),
+})
 
 STATUS = {
     0: "GFFM_OK", 1: "GFFM_ERR_ARG", 2: "GFFM_ERR_SIZE", 3: "GFFM_ERR_MODULUS", 4: "GFFM_ERR_STRIPE",

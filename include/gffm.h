@@ -215,6 +215,56 @@ GFFM_API int gffm_apply_col_swaps_f64(double *A, int64_t lda, int64_t nrows, int
 GFFM_API int gffm_apply_col_swaps_f32(float *A, int64_t lda, int64_t nrows, int64_t ncols, const int64_t *swaps,
                                       int64_t nswaps, int inverse, gffm_stream_t stream);
 
+/* ---- KaratsubaArray (src/KaratsubaMatrix/) --------------------------------
+ * An element is two Float64 digits (d1, d2), d1 in [0, N1), d2 in [0, N2), of
+ * the value d1 + N1*d2 in Z/(N1*N2) (KaratsubaMatrix.jl:304,318-336).  Each
+ * digit matrix is column-major with its own padding, and both digit matrices of
+ * one operand share the leading dimension.  Results are the exact digits in
+ * Z/(N1*N2); they equal the reference's kernels whenever N2 divides N1 (all
+ * modulus pairs the reference constructs).
+ *
+ * KMatMul!(C, A, B) (KaratsubaMatrix.jl:133-204, kernels KaratsubaKernels.jl:129-158)
+ * and KMatMul_gemv! (:238-300, n = 1): three component products on the limb
+ * tensor-core GEMM plus a digit combine; 2 <= N1, N2 < 2^26.  C must not alias
+ * A or B.  Workspace: gffm_karatsuba_workspace_size bytes, or NULL. */
+GFFM_API int gffm_karatsuba_workspace_size(int64_t m, int64_t n, int64_t k, int64_t N1, int64_t N2, size_t *bytes);
+GFFM_API int gffm_karatsuba_matmul_f64(int64_t m, int64_t n, int64_t k, const double *A1, const double *A2,
+                                       int64_t lda, const double *B1, const double *B2, int64_t ldb, double *C1,
+                                       double *C2, int64_t ldc, int64_t N1, int64_t N2, void *workspace,
+                                       size_t workspace_bytes, gffm_stream_t stream);
+/* The polynomial reading of the same three products (no reference entry
+ * point; the two-component Karatsuba product of KaratsubaMatrix.jl:133-204
+ * without carries): (A0 + A1 x)(B0 + B1 x) mod p = C0 + C1 x + C2 x^2 with
+ * C0 = A0 B0, C2 = A1 B1, C1 = (A0 + A1)(B0 + B1) - C0 - C2; 2 <= p < 2^26.
+ * Outputs must not alias inputs.  Workspace: gffm_karatsuba_poly_workspace_size. */
+GFFM_API int gffm_karatsuba_poly_workspace_size(int64_t m, int64_t n, int64_t k, int64_t p, size_t *bytes);
+GFFM_API int gffm_karatsuba_poly_matmul_f64(int64_t m, int64_t n, int64_t k, const double *A0, const double *A1,
+                                            int64_t lda, const double *B0, const double *B1, int64_t ldb, double *C0,
+                                            double *C1, double *C2, int64_t ldc, int64_t p, void *workspace,
+                                            size_t workspace_bytes, gffm_stream_t stream);
+/* Elementwise digit ops over `len` elements of the (padded) digit arrays;
+ * N1*N2 <= 2^52.  add!(K, A, B) -> karatsuba_add_kernel! (KaratsubaMatrix.jl:505-536,
+ * KaratsubaKernels.jl:2-50) */
+GFFM_API int gffm_karatsuba_add_f64(double *C1, double *C2, const double *A1, const double *A2, const double *B1,
+                                    const double *B2, int64_t len, int64_t N1, int64_t N2, gffm_stream_t stream);
+/* sub!(K, A, B) -> karatsuba_sub_kernel! (KaratsubaMatrix.jl:583-629, KaratsubaKernels.jl:113-125) */
+GFFM_API int gffm_karatsuba_sub_f64(double *C1, double *C2, const double *A1, const double *A2, const double *B1,
+                                    const double *B2, int64_t len, int64_t N1, int64_t N2, gffm_stream_t stream);
+/* negate!(K, A) -> karatsuba_negate_kernel! (KaratsubaMatrix.jl:691-731, KaratsubaKernels.jl:79-111) */
+GFFM_API int gffm_karatsuba_negate_f64(double *C1, double *C2, const double *A1, const double *A2, int64_t len,
+                                       int64_t N1, int64_t N2, gffm_stream_t stream);
+/* scalar_multiply!(B, A, s) -> karatsuba_scalar_multiply_kernel! (KaratsubaMatrix.jl:631-666,
+ * KaratsubaKernels.jl:52-77); any integer s (reduced mod N1*N2) */
+GFFM_API int gffm_karatsuba_scalar_mul_f64(double *C1, double *C2, const double *A1, const double *A2, int64_t s,
+                                           int64_t len, int64_t N1, int64_t N2, gffm_stream_t stream);
+/* MatToKMat / KaratsubaMatrix(T, A, N1, N2, M) digit split (KaratsubaMatrix.jl:358-397):
+ * D1 = a mod N1, D2 = floor(a / N1) mod N2 for each (non-negative) value a */
+GFFM_API int gffm_karatsuba_from_values_f64(double *D1, double *D2, const double *A, int64_t len, int64_t N1,
+                                            int64_t N2, gffm_stream_t stream);
+/* Array(K) / getindex (KaratsubaMatrix.jl:304,318-336): A = D1 + N1*D2 */
+GFFM_API int gffm_karatsuba_to_values_f64(double *A, const double *D1, const double *D2, int64_t len, int64_t N1,
+                                          int64_t N2, gffm_stream_t stream);
+
 /* ---- limb GEMM without allocation -----------------------------------------
  * No counterpart in the reference.  For callers that cannot allocate device
  * memory when they multiply: a process whose HBM is already reserved by

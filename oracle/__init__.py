@@ -58,6 +58,8 @@ def lib():
                                           _i64, _i64, ctypes.c_int]
         L.or_karatsuba_addsub.restype = None
         L.or_karatsuba_addsub.argtypes = [_i64, _p, _p, _p, _p, _p, _p, _i64, _i64, ctypes.c_int]
+        L.or_karatsuba_scale.restype = None
+        L.or_karatsuba_scale.argtypes = [_i64, _p, _p, _i64, ctypes.c_int, _p, _p, _i64, _i64]
         _lib = L
     return _lib
 
@@ -158,6 +160,16 @@ def karatsuba_addsub(A1, A2, B1, B2, N1, N2, sub=False):
     C2 = np.zeros_like(A1)
     lib().or_karatsuba_addsub(A1.size, _ptr(A1), _ptr(A2), _ptr(B1), _ptr(B2), _ptr(C1), _ptr(C2),
                               int(N1), int(N2), 1 if sub else 0)
+    return C1, C2
+
+
+def karatsuba_scale(A1, A2, N1, N2, s=0, negate=False):
+    """Digit-form (s*A) or (-A) mod N1*N2 (karatsuba_scalar_multiply_kernel!, karatsuba_negate_kernel!)."""
+    A1, A2 = (np.ascontiguousarray(np.asarray(x, dtype=np.int64)) for x in (A1, A2))
+    C1 = np.zeros_like(A1)
+    C2 = np.zeros_like(A1)
+    lib().or_karatsuba_scale(A1.size, _ptr(A1), _ptr(A2), int(s), 1 if negate else 0, _ptr(C1), _ptr(C2),
+                             int(N1), int(N2))
     return C1, C2
 
 

@@ -431,3 +431,20 @@ void or_karatsuba_addsub(int64_t len, const int64_t *A1, const int64_t *A2,
         C2[i] = (int64_t)(c / N1);
     }
 }
+
+/* Karatsuba digit negation and scalar product (karatsuba_negate_kernel!,
+ * karatsuba_scalar_multiply_kernel!, KaratsubaKernels.jl:52-111): exact
+ * (-A) and (s*A) mod N1*N2 as digits, s any integer. */
+void or_karatsuba_scale(int64_t len, const int64_t *A1, const int64_t *A2, int64_t s, int negate,
+                        int64_t *C1, int64_t *C2, int64_t N1, int64_t N2) {
+    i128 M = (i128)N1 * (i128)N2;
+    i128 sm = (i128)s % M;
+    if (sm < 0) sm += M;
+    for (int64_t i = 0; i < len; i++) {
+        i128 a = ((i128)A1[i] + (i128)N1 * A2[i]) % M;
+        if (a < 0) a += M;
+        i128 c = negate ? (M - a) % M : (a * sm) % M;
+        C1[i] = (int64_t)(c % N1);
+        C2[i] = (int64_t)(c / N1);
+    }
+}

@@ -135,6 +135,9 @@ def main():
     add({"op": "karatsuba_sub", "src": "test/KaratsubaMatrix/basic_operations_test.jl:51-65 (A-B)",
          "A1": A, "A2": [[0, 0], [0, 0]], "B1": B, "B2": [[0, 0], [0, 0]], "N1": 100, "N2": 100,
          "expected_value": mod(elementwise(A, B, lambda a, b: a - b), 100 * 100)})
+    add({"op": "karatsuba_scalar", "src": "test/KaratsubaMatrix/basic_operations_test.jl:51-64 (a*A, a = 9)",
+         "A1": A, "A2": [[0, 0], [0, 0]], "s": 9, "N1": 100, "N2": 100,
+         "expected_value": mod([[9 * x for x in row] for row in A], 100 * 100)})
     C1 = [[1, 0, 3], [8, 11, 2], [2, 4, 6]]
     C2 = [[10, 3, 2], [7, 13, 7], [1, 0, 9]]
     D1 = [[9, 6, 5], [2, 17, 9], [4, 4, 23]]

@@ -79,3 +79,91 @@ def inverse_mod(A, N):
                 f = M[r][c]
                 M[r] = [(x - f * y) % N for x, y in zip(M[r], M[c])]
     return [r[n:] for r in M]
+
+
+# ---- Karatsuba kernels as the reference writes them (Julia rem / mod / div) ----
+def _rem(a, b):
+    """Julia rem / %: the sign of the dividend."""
+    r = abs(a) % abs(b)
+    return r if a >= 0 else -r
+
+
+def _div(a, b):
+    """Julia div: truncating division."""
+    q = abs(a) // abs(b)
+    return q if (a >= 0) == (b >= 0) else -q
+
+
+def kara_add(a1, a2, b1, b2, N1, N2):
+    # karatsuba_add_helper (src/KaratsubaMatrix/KaratsubaKernels.jl:2-17)
+    temp = _rem(a1 + b1, 2 * N1)
+    temp = _div(temp, N1)
+    res2 = _rem(temp + a2, 2 * N2)
+    res2 = _rem(res2 + b2, 2 * N2)
+    temp = _rem(temp * N1, N1 ** 2)
+    temp = _rem(b1 - temp, N1 ** 2)
+    res1 = _rem(a1 + temp, N1 ** 2)
+    return _rem(res1, N1), _rem(res2, N2)
+
+
+def kara_negate(a1, a2, N1, N2, M):
+    # karatsuba_negate_helper (KaratsubaKernels.jl:79-97)
+    res2 = _rem(0, N2)
+    res2 = _rem(res2 + N1, 2 * N1)
+    res2 = _rem(res2 - a1, 2 * N1)
+    res2 = _div(res2, N1)
+    res1 = _rem(res2 * N1, M ** 2)
+    res1 = _rem(res1 + a1, M ** 2)
+    res1 = _rem(-res1, N1)
+    res1 = res1 % N1
+    res2 = _rem(res2 + N2, M ** 2)
+    res2 = _rem(res2 - 1, M ** 2)
+    res2 = _rem(res2 - a2, M)
+    return res1, _rem(res2, N2)
+
+
+def kara_sub(a1, a2, b1, b2, N1, N2, M):
+    # karatsuba_sub_kernel! (KaratsubaKernels.jl:113-125): negate B, then add A
+    n1, n2 = kara_negate(b1, b2, N1, N2, M)
+    return kara_add(n1, n2, a1, a2, N1, N2)
+
+
+def kara_scalar(a1, a2, s, N1, N2):
+    # karatsuba_scalar_multiply_helper (KaratsubaKernels.jl:52-60)
+    res2 = _rem(a1 * s, N1 ** 2)
+    res2 = _div(res2, N1)
+    res1 = _rem(a2 * s, N2)
+    res2 = _rem(res2 + res1, N2)
+    res1 = _rem(a1 * s, N1)
+    return res1, res2
+
+
+def kara_matmul(A1, A2, B1, B2, N1, N2):
+    """KMatMul! (src/KaratsubaMatrix/KaratsubaMatrix.jl:133-204) with its kernels
+    karatsuba_matmul_kernel_1!/2! (KaratsubaKernels.jl:129-158), products exact
+    (the reference's striped Float64 mul! is exact for these bounds)."""
+    m, k, n = len(A1), len(A1[0]), len(B1[0])
+    Ap = [[_rem(A1[i][p] + A2[i][p], 2 * N1) for p in range(k)] for i in range(m)]
+    Bp = [[_rem(B1[p][j] + B2[p][j], 2 * N1) for j in range(n)] for p in range(k)]
+
+    def mm(X, Y, P):
+        return [[sum(X[i][p] * Y[p][j] for p in range(k)) % P for j in range(n)] for i in range(m)]
+
+    C1 = mm(A1, B1, N1 ** 2)                 # mul!(C.data1, A.data1, B.data1, R=N1, P=N1^2)
+    C2 = mm(Ap, Bp, (4 * N1) ** 2)           # mul!(C.data2, A.plan, B.plan, R=2N1, P=(4N1)^2)
+    T = mm(A2, B2, N1 ** 2)                  # mul!(B.plan, A.data2, B.data2, R=N1, P=N1^2)
+    R1 = [[0] * n for _ in range(m)]
+    R2 = [[0] * n for _ in range(m)]
+    Q = (4 * N1) ** 2
+    for i in range(m):
+        for j in range(n):
+            cc1 = C1[i][j] % (N1 ** 2)
+            cc2 = C2[i][j] % Q
+            bp = T[i][j] % N1
+            cp = _div(cc1, N1)
+            cc2 = _rem(cc2 - cc1, Q)
+            cc2 = _rem(cc2 - bp, Q)
+            cc2 = cc2 + cp
+            R1[i][j] = cc1 % N1
+            R2[i][j] = cc2 % N2
+    return R1, R2

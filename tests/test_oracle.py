@@ -86,6 +86,8 @@ def test_kat_karatsuba(case):
     N1, N2 = case["N1"], case["N2"]
     if case["op"] == "karatsuba_matmul":
         c1, c2 = oracle.karatsuba_matmul(case["A1"], case["A2"], case["B1"], case["B2"], N1, N2)
+    elif case["op"] == "karatsuba_scalar":
+        c1, c2 = oracle.karatsuba_scale(case["A1"], case["A2"], N1, N2, s=case["s"])
     else:
         c1, c2 = oracle.karatsuba_addsub(case["A1"], case["A2"], case["B1"], case["B2"], N1, N2,
                                          sub=case["op"] == "karatsuba_sub")
@@ -182,3 +184,55 @@ def test_lu_oracle_equals_pluq_on_full_column_rank():
         for (i, j) in rs:
             ident[i - 1], ident[j - 1] = ident[j - 1], ident[i - 1]
         assert perm == ident
+
+
+# ---- the oracle's exact Karatsuba digits against the reference's kernel formulas ----
+KARA_PAIRS = [(100, 100), (13 ** 4, 13 ** 3), (49, 7), (33554393, 33554393), (2 ** 20, 2 ** 10)]
+
+
+@pytest.mark.parametrize("N1,N2", KARA_PAIRS)
+def test_karatsuba_oracle_matches_reference_formulas(N1, N2):
+    """For N2 | N1 (every pair the reference constructs) the reference's
+    kernels compute the exact digits of the product / sum / difference /
+    scalar multiple in Z/(N1 N2): the oracle's definition."""
+    import pyref
+    rng = np.random.default_rng(N1 + N2)
+    m, k, n = 5, 7, 4
+    A1, B1 = rng.integers(0, N1, size=(m, k)), rng.integers(0, N1, size=(k, n))
+    A2, B2 = rng.integers(0, N2, size=(m, k)), rng.integers(0, N2, size=(k, n))
+    R1, R2 = pyref.kara_matmul(A1.tolist(), A2.tolist(), B1.tolist(), B2.tolist(), N1, N2)
+    c1, c2 = oracle.karatsuba_matmul(A1, A2, B1, B2, N1, N2)
+    assert c1.tolist() == R1 and c2.tolist() == R2
+    X1, X2 = rng.integers(0, N1, size=40), rng.integers(0, N2, size=40)
+    Y1, Y2 = rng.integers(0, N1, size=40), rng.integers(0, N2, size=40)
+    X1[:4] = 0
+    Y1[4:8] = 0
+    M = N1 * N2
+    xs = list(zip(X1.tolist(), X2.tolist()))
+    ys = list(zip(Y1.tolist(), Y2.tolist()))
+    add = [pyref.kara_add(a, b, c, d, N1, N2) for (a, b), (c, d) in zip(xs, ys)]
+    sub = [pyref.kara_sub(a, b, c, d, N1, N2, M) for (a, b), (c, d) in zip(xs, ys)]
+    neg = [pyref.kara_negate(a, b, N1, N2, M) for a, b in xs]
+    for s in (0, 1, 9, 100, 12345):
+        sc = [pyref.kara_scalar(a, b, s, N1, N2) for a, b in xs]
+        o1, o2 = oracle.karatsuba_scale(X1, X2, N1, N2, s=s)
+        assert list(zip(o1.tolist(), o2.tolist())) == sc
+    o1, o2 = oracle.karatsuba_addsub(X1, X2, Y1, Y2, N1, N2)
+    assert list(zip(o1.tolist(), o2.tolist())) == add
+    o1, o2 = oracle.karatsuba_addsub(X1, X2, Y1, Y2, N1, N2, sub=True)
+    assert list(zip(o1.tolist(), o2.tolist())) == sub
+    o1, o2 = oracle.karatsuba_scale(X1, X2, N1, N2, negate=True)
+    assert list(zip(o1.tolist(), o2.tolist())) == neg
+
+
+def test_karatsuba_reference_formula_is_not_the_product_when_n2_does_not_divide_n1():
+    """Documented deviation: for N2 not dividing N1 the reference drops the
+    N1^2 * A2 B2 term and reduces S1 mod N1^2; the library returns the product."""
+    import pyref
+    N1, N2 = 101, 103
+    A1, A2, B1, B2 = [[57]], [[88]], [[91]], [[77]]
+    R1, R2 = pyref.kara_matmul(A1, A2, B1, B2, N1, N2)
+    c1, c2 = oracle.karatsuba_matmul(A1, A2, B1, B2, N1, N2)
+    x, y = 57 + N1 * 88, 91 + N1 * 77
+    assert int(c1[0, 0]) + N1 * int(c2[0, 0]) == (x * y) % (N1 * N2)
+    assert (R1[0][0], R2[0][0]) != (int(c1[0, 0]), int(c2[0, 0]))
