@@ -180,8 +180,9 @@ __host__ __device__ constexpr uint32_t idesc_f16_f32(int M, int N) {
 }
 
 // --- modular helpers -------------------------------------------------------
-// r = x mod n for 0 <= x < 2^64 using a precomputed floor(2^64 / n) (Barrett,
-// one correction step).
+// r = x mod n for 0 <= x < 2^63 and n >= 2, using minv = floor((2^64 - 1) / n)
+// (Barrett).  The estimated quotient is at most one below the true one on
+// that range, so one correction step suffices.
 __device__ __forceinline__ uint64_t barrett64(uint64_t x, uint64_t n, uint64_t minv) {
     uint64_t q = __umul64hi(x, minv);
     uint64_t r = x - q * n;

@@ -1,0 +1,730 @@
+// k_batched.cu -- batched uneven instances: many independent products and
+// PLUQs, each with its own sizes and modulus, in three launches captured in
+// one CUDA graph:
+//   k_split_batched   digit planes of every product operand (one launch over all)
+//   k_gemm_grouped    persistent tcgen05 GEMM over the output tiles of every product;
+//                     the digit count L (1..4) of each instance is a runtime value
+//                     and each instance has its own TMA descriptors in global memory
+//   k_pluq_batched    persistent PLUQ, a CTA per instance (batched_pluq.cuh)
+// The product path is the limb GEMM of gemm_limb.cuh with per-tile instance
+// parameters; the PLUQ path follows pluq_gpu_kernel step for step.
+#include "batched_pluq.cuh"
+#include "gemm_limb.cuh"
+#include "limb_host.h"
+
+#include <algorithm>
+#include <numeric>
+#include <vector>
+
+namespace batched {
+
+using namespace limb;
+
+struct MMInst {
+    int m, n, L, kblocks, mtiles, ntiles, chunk_kb, Mpad, Npad, pad_;
+    int32_t W[MAX_SHIFTS];       // 2^(7s) mod N
+    int64_t N;
+    uint64_t minv;
+    int64_t bias;
+    double *C;
+    int64_t ldc;
+};
+
+struct WorkItem {
+    int inst, tm, tn, pad_;
+};
+
+struct SplitJob {
+    const double *src;
+    int64_t ld;
+    __half *dst;
+    int rows, cols;              // operand extent: A is m x k, B is k x n
+    int prow, kpad;              // digit rows per plane (Mpad or Npad) and padded K
+    int L, is_b;
+    int64_t N;
+    uint64_t minv;
+    int64_t blk0;                // first block of this job
+};
+
+constexpr int G_STAGES = 2;
+constexpr int G_STAGE_BYTES = 4 * (A_TILE + B_TILE);
+constexpr int G_SMEM_BYTES = G_STAGES * G_STAGE_BYTES + 1024;
+constexpr int G_TMEM_COLS = 512;
+
+// ---------------------------------------------------------------------------
+// digit split of every product operand
+// ---------------------------------------------------------------------------
+template <int L>
+__device__ __forceinline__ void split_a_tile(const SplitJob &J, int64_t local, int32_t (*tile)[33]) {
+    const int kt = J.kpad / 32;
+    const int64_t r0 = (local / kt) * 32, k0 = (local % kt) * 32;
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    const ModN M{J.N, J.minv};
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        const int64_t kk = k0 + ty + 8 * i, r = r0 + tx;
+        tile[ty + 8 * i][tx] = (r < J.rows && kk < J.cols) ? split_value<SPLIT_CENTRED>(J.src[r + kk * J.ld], 0.0, M) : 0;
+    }
+    __syncthreads();
+    const size_t plane = (size_t)J.prow * J.kpad;
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        const int64_t r = r0 + ty + 8 * i, kk = k0 + tx;
+        __half d[L];
+        digits<L>(tile[tx][ty + 8 * i], d);
+#pragma unroll
+        for (int l = 0; l < L; l++) J.dst[l * plane + (size_t)r * J.kpad + kk] = d[l];
+    }
+}
+
+template <int L>
+__device__ __forceinline__ void split_b_pairs(const SplitJob &J, int64_t local) {
+    const int64_t idx = local * 256 + threadIdx.x;
+    const int64_t ppc = J.kpad / 2;
+    if (idx >= ppc * J.prow) return;
+    const int64_t c = idx / ppc;
+    const int64_t kk = (idx - c * ppc) * 2;
+    const ModN M{J.N, J.minv};
+    const int k = J.rows, n = J.cols;
+    const int32_t v0 = (c < n && kk < k) ? split_value<SPLIT_CENTRED>(J.src[kk + c * J.ld], 0.0, M) : 0;
+    const int32_t v1 = (c < n && kk + 1 < k) ? split_value<SPLIT_CENTRED>(J.src[kk + 1 + c * J.ld], 0.0, M) : 0;
+    __half d0[L], d1[L];
+    digits<L>(v0, d0);
+    digits<L>(v1, d1);
+    const size_t plane = (size_t)J.prow * J.kpad;
+#pragma unroll
+    for (int l = 0; l < L; l++)
+        *reinterpret_cast<__half2 *>(J.dst + l * plane + (size_t)c * J.kpad + kk) = __halves2half2(d0[l], d1[l]);
+}
+
+__global__ void __launch_bounds__(256) k_split_batched(const SplitJob *__restrict__ jobs, int njobs) {
+    __shared__ int32_t tile[32][33];
+    const int64_t b = blockIdx.x;
+    int lo = 0, hi = njobs - 1;          // last job with blk0 <= b
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (jobs[mid].blk0 <= b) lo = mid; else hi = mid - 1;
+    }
+    const SplitJob J = jobs[lo];
+    const int64_t local = b - J.blk0;
+    if (J.is_b) {
+        switch (J.L) {
+            case 1: split_b_pairs<1>(J, local); break;
+            case 2: split_b_pairs<2>(J, local); break;
+            case 3: split_b_pairs<3>(J, local); break;
+            default: split_b_pairs<4>(J, local); break;
+        }
+    } else {
+        switch (J.L) {
+            case 1: split_a_tile<1>(J, local, tile); break;
+            case 2: split_a_tile<2>(J, local, tile); break;
+            case 3: split_a_tile<3>(J, local, tile); break;
+            default: split_a_tile<4>(J, local, tile); break;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// grouped limb GEMM over the output tiles of every product
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void tmap_acquire(const CUtensorMap *map) {
+    asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(map) : "memory");
+}
+
+__device__ __forceinline__ int64_t reduce_inst(int64_t acc, const MMInst &I) {
+    return (int64_t)gffm_dev::barrett64((uint64_t)(acc + I.bias), (uint64_t)I.N, I.minv);
+}
+
+__global__ void __launch_bounds__(NUM_THREADS, 1)
+    k_gemm_grouped(const MMInst *__restrict__ insts, const WorkItem *__restrict__ items, int nitems,
+                   const CUtensorMap *__restrict__ tmaps, int *err) {
+    extern __shared__ uint8_t dsmem_raw[];
+    __shared__ uint64_t full_bar[G_STAGES];
+    __shared__ uint64_t empty_bar[G_STAGES];
+    __shared__ uint64_t acc_full_bar, acc_empty_bar, drain_bar;
+    __shared__ uint32_t tmem_base_s;
+    __shared__ int abort_sh;
+    volatile int &abort_s = abort_sh;
+
+    uint8_t *smem = (uint8_t *)(((uintptr_t)dsmem_raw + 1023) & ~(uintptr_t)1023);
+    const int warp = threadIdx.x >> 5;
+    const int lane = threadIdx.x & 31;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < G_STAGES; s++) {
+            gffm_dev::mbar_init(&full_bar[s], 1);
+            gffm_dev::mbar_init(&empty_bar[s], 1);
+        }
+        gffm_dev::mbar_init(&acc_full_bar, 1);
+        gffm_dev::mbar_init(&acc_empty_bar, NUM_EPI_WARPS);
+        gffm_dev::mbar_init(&drain_bar, 1);
+        abort_s = 0;
+        gffm_dev::fence_mbar_init();
+    }
+    if (warp == 1) gffm_dev::tmem_alloc(&tmem_base_s, G_TMEM_COLS);
+    gffm_dev::tc_fence_before();
+    __syncthreads();
+    gffm_dev::tc_fence_after();
+    const uint32_t tmem = tmem_base_s;
+
+    if (warp == 0) {
+        // ---------------- TMA producer ----------------
+        if (lane == 0) {
+            int stage = 0;
+            uint32_t phase = 0;
+            uint32_t issued_parity_mask = 0, issued_mask = 0;
+            int last_inst = -1;
+            for (int t = blockIdx.x; t < nitems && !abort_s; t += gridDim.x) {
+                const WorkItem it = items[t];
+                const MMInst &I = insts[it.inst];
+                const int L = I.L;
+                const CUtensorMap *tmA = tmaps + 2 * it.inst;
+                const CUtensorMap *tmB = tmA + 1;
+                if (it.inst != last_inst) {
+                    tmap_acquire(tmA);
+                    tmap_acquire(tmB);
+                    last_inst = it.inst;
+                }
+                const uint32_t bytes = (uint32_t)L * (A_TILE + B_TILE);
+                for (int kb = 0; kb < I.kblocks; kb++) {
+                    if (!gffm_dev::mbar_wait(&empty_bar[stage], phase ^ 1)) {
+                        atomicOr(err, 1);
+                        abort_s = 1;
+                        break;
+                    }
+                    if (abort_s) break;
+                    uint8_t *sa = smem + stage * G_STAGE_BYTES;
+                    uint8_t *sb = sa + 4 * A_TILE;
+                    gffm_dev::mbar_arrive_expect_tx(&full_bar[stage], bytes);
+                    for (int l = 0; l < L; l++)
+                        gffm_dev::tma_load_2d(sa + l * A_TILE, tmA, &full_bar[stage], kb * BK, l * I.Mpad + it.tm * BM);
+                    for (int l = 0; l < L; l++)
+                        gffm_dev::tma_load_2d(sb + l * B_TILE, tmB, &full_bar[stage], kb * BK, l * I.Npad + it.tn * BN);
+                    issued_mask |= 1u << stage;
+                    issued_parity_mask = (issued_parity_mask & ~(1u << stage)) | (phase << stage);
+                    if (++stage == G_STAGES) {
+                        stage = 0;
+                        phase ^= 1;
+                    }
+                }
+            }
+            if (abort_s) {
+                for (int s = 0; s < G_STAGES; s++)
+                    if (issued_mask & (1u << s)) gffm_dev::mbar_wait(&full_bar[s], (issued_parity_mask >> s) & 1);
+            }
+        }
+    } else if (warp == 1) {
+        // ---------------- MMA issuer ----------------
+        if (lane == 0) {
+            int stage = 0;
+            uint32_t phase = 0, acc_phase = 0;
+            bool issued_any = false;
+            for (int t = blockIdx.x; t < nitems && !abort_s; t += gridDim.x) {
+                const WorkItem it = items[t];
+                const MMInst &I = insts[it.inst];
+                const int L = I.L;
+                const uint32_t idesc_full = gffm_dev::idesc_f16_f32(BM, BN * L);
+                const uint32_t idesc_lo = gffm_dev::idesc_f16_f32(BM, BN * (L > 1 ? L - 1 : 1));
+                const uint32_t idesc_one = gffm_dev::idesc_f16_f32(BM, BN);
+                for (int kb0 = 0; kb0 < I.kblocks && !abort_s; kb0 += I.chunk_kb) {
+                    const int kb1 = min(kb0 + I.chunk_kb, I.kblocks);
+                    if (!gffm_dev::mbar_wait(&acc_empty_bar, acc_phase ^ 1)) {
+                        atomicOr(err, 2);
+                        abort_s = 1;
+                        break;
+                    }
+                    gffm_dev::tc_fence_after();
+                    for (int kb = kb0; kb < kb1; kb++) {
+                        if (!gffm_dev::mbar_wait(&full_bar[stage], phase)) {
+                            atomicOr(err, 4);
+                            abort_s = 1;
+                            break;
+                        }
+                        gffm_dev::tc_fence_after();
+                        const uint32_t sa = gffm_dev::smem_u32(smem + stage * G_STAGE_BYTES);
+                        const uint32_t sb = sa + 4 * A_TILE;
+#pragma unroll
+                        for (int kk = 0; kk < BK / 16; kk++) {
+                            const uint64_t bdesc = gffm_dev::umma_desc_sw128(sb + kk * 32);
+                            if (kb == kb0 && kk == 0) {
+                                gffm_dev::mma_f16(tmem, gffm_dev::umma_desc_sw128(sa + kk * 32), bdesc, idesc_full, 0);
+                                for (int i = 1; i < L; i++) {
+                                    const uint64_t adesc = gffm_dev::umma_desc_sw128(sa + i * A_TILE + kk * 32);
+                                    gffm_dev::mma_f16(tmem + 64 * i, adesc, bdesc, idesc_lo, 1);
+                                    gffm_dev::mma_f16(tmem + 64 * (i + L - 1), adesc,
+                                                      gffm_dev::umma_desc_sw128(sb + (L - 1) * B_TILE + kk * 32),
+                                                      idesc_one, 0);
+                                }
+                            } else {
+                                for (int i = 0; i < L; i++)
+                                    gffm_dev::mma_f16(tmem + 64 * i, gffm_dev::umma_desc_sw128(sa + i * A_TILE + kk * 32),
+                                                      bdesc, idesc_full, 1);
+                            }
+                        }
+                        issued_any = true;
+                        gffm_dev::mma_commit(&empty_bar[stage]);
+                        if (++stage == G_STAGES) {
+                            stage = 0;
+                            phase ^= 1;
+                        }
+                    }
+                    if (abort_s) break;
+                    gffm_dev::mma_commit(&acc_full_bar);
+                    acc_phase ^= 1;
+                }
+            }
+            if (abort_s && issued_any) {
+                gffm_dev::mma_commit(&drain_bar);
+                gffm_dev::mbar_wait(&drain_bar, 0);
+            }
+        }
+    } else {
+        // ---------------- epilogue ----------------
+        const int quad = warp & 3;
+        const int half = (warp - 2) >> 2;
+        uint32_t acc_phase = 0;
+        for (int t = blockIdx.x; t < nitems; t += gridDim.x) {
+            const WorkItem it = items[t];
+            const MMInst I = insts[it.inst];
+            const int nshift = 2 * I.L - 1;
+            int64_t acc[32];
+#pragma unroll
+            for (int j = 0; j < 32; j++) acc[j] = 0;
+            bool ok = true;
+            int chunk = 0;
+            for (int kb0 = 0; kb0 < I.kblocks; kb0 += I.chunk_kb, chunk++) {
+                if (!gffm_dev::mbar_wait(&acc_full_bar, acc_phase)) {
+                    atomicOr(err, 8);
+                    abort_s = 1;
+                    ok = false;
+                    break;
+                }
+                gffm_dev::tc_fence_after();
+                for (int s = 0; s < nshift; s++) {
+                    uint32_t v[32];
+                    gffm_dev::tmem_ld_32x32b_x32(tmem + ((uint32_t)(quad * 32) << 16) + 64 * s + 32 * half, v);
+                    gffm_dev::tmem_ld_wait();
+                    const int w = I.W[s];
+#pragma unroll
+                    for (int j = 0; j < 32; j++) acc[j] += (int64_t)__float2int_rz(__uint_as_float(v[j])) * w;
+                }
+                gffm_dev::tc_fence_before();
+                __syncwarp();
+                if (lane == 0) gffm_dev::mbar_arrive(&acc_empty_bar);
+                acc_phase ^= 1;
+                if ((chunk & 63) == 63) {
+#pragma unroll
+                    for (int j = 0; j < 32; j++) acc[j] = reduce_inst(acc[j], I);
+                }
+            }
+            if (!ok || abort_s) break;
+            const int64_t row = (int64_t)it.tm * BM + quad * 32 + lane;
+            const int64_t col0 = (int64_t)it.tn * BN + half * 32;
+            if (row < I.m) {
+#pragma unroll
+                for (int j = 0; j < 32; j++)
+                    if (col0 + j < I.n) I.C[row + (col0 + j) * I.ldc] = (double)reduce_inst(acc[j], I);
+            }
+        }
+    }
+
+    gffm_dev::tc_fence_before();
+    __syncthreads();
+    gffm_dev::tc_fence_after();
+    if (warp == 1) gffm_dev::tmem_dealloc(tmem, G_TMEM_COLS);
+}
+
+}  // namespace batched
+
+// ---------------------------------------------------------------------------
+// host: plans
+// ---------------------------------------------------------------------------
+struct gffm_batch_plan_s {
+    int device = 0;
+    void *mem = nullptr;
+    size_t mem_bytes = 0;
+    int n_mm = 0, n_pq = 0, nitems = 0, njobs = 0;
+    int64_t split_blocks = 0;
+    int gemm_grid = 0, pq_grid = 0, pq_nb = 0, pq_rcap = 0;
+    size_t pq_smem = 0;
+    batched::MMInst *d_mm = nullptr;
+    batched::WorkItem *d_items = nullptr;
+    CUtensorMap *d_tmaps = nullptr;
+    batched::SplitJob *d_jobs = nullptr;
+    batched::PQInst *d_pq = nullptr;
+    int *d_order = nullptr, *d_next = nullptr;
+    int32_t *d_tmp = nullptr;
+    int tmp_ldw = 4, tmp_ldlw = 4;
+    cudaGraphExec_t exec = nullptr;
+    struct ZeroK {
+        double *C;
+        int64_t ldc, m, n;
+    };
+    std::vector<ZeroK> zero_k;   // products with an empty inner dimension: C = 0
+};
+
+namespace {
+
+using gffm::set_error;
+
+#define PLAN_CUDA(call)                                 \
+    do {                                                \
+        cudaError_t e__ = (call);                       \
+        if (e__ != cudaSuccess) {                       \
+            free_plan(p);                               \
+            return gffm::cuda_error(e__, #call);        \
+        }                                               \
+    } while (0)
+
+size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+int check_desc(const gffm_batch_desc &d, int64_t i) {
+    if (d.op != GFFM_BATCH_MATMUL && d.op != GFFM_BATCH_PLUQ)
+        return set_error(GFFM_ERR_ARG, "instance %lld: unknown op %lld", (long long)i, (long long)d.op);
+    if (d.N < 2 || d.N >= (int64_t(1) << 26))
+        return set_error(GFFM_ERR_MODULUS, "instance %lld: the batched path needs 2 <= N < 2^26 (got %lld)",
+                         (long long)i, (long long)d.N);
+    if (d.m < 0 || d.n < 0 || d.k < 0) return set_error(GFFM_ERR_ARG, "instance %lld: negative size", (long long)i);
+    if (d.op == GFFM_BATCH_MATMUL) {
+        int st = limb::check_args(d.m, d.n, d.k, d.lda, d.ldb, d.ldc, d.N);
+        if (st) return st;
+        if (d.m > 0 && d.n > 0 && (!d.C || (d.k > 0 && (!d.A || !d.B))))
+            return set_error(GFFM_ERR_ARG, "instance %lld: null data pointer", (long long)i);
+    } else {
+        if (d.m > 1024) return set_error(GFFM_ERR_UNSUPPORTED, "instance %lld: batched PLUQ needs m <= 1024", (long long)i);
+        if (d.n > (int64_t(1) << 20)) return set_error(GFFM_ERR_ARG, "instance %lld: n above 2^20", (long long)i);
+        if (d.lda < std::max<int64_t>(d.m, 1) || d.ldc < std::max<int64_t>(d.m, 1) || d.ldl < std::max<int64_t>(d.m, 1))
+            return set_error(GFFM_ERR_ARG, "instance %lld: leading dimension smaller than m", (long long)i);
+        if (d.l_cols < 1 || d.l_cols > (int64_t(1) << 20))
+            return set_error(GFFM_ERR_ARG, "instance %lld: l_cols out of range", (long long)i);
+        if (!d.info || (d.m > 0 && d.n > 0 && (!d.A || !d.C || !d.L || !d.row_swaps || !d.col_swaps)))
+            return set_error(GFFM_ERR_ARG, "instance %lld: null pointer", (long long)i);
+    }
+    return GFFM_OK;
+}
+
+struct Carve {
+    size_t off = 0;
+    size_t take(size_t bytes, size_t align = 256) {
+        off = align_up(off, align);
+        size_t o = off;
+        off += bytes;
+        return o;
+    }
+};
+
+int build_graph(gffm_batch_plan p, bool overlap) {
+    using namespace batched;
+    cudaStream_t s0, s1 = nullptr;
+    GFFM_CUDA(cudaStreamCreateWithFlags(&s0, cudaStreamNonBlocking));
+    cudaGraph_t graph = nullptr;
+    int st = GFFM_OK;
+    cudaEvent_t fork = nullptr, join = nullptr;
+    auto fail = [&](cudaError_t e, const char *what) {
+        if (st == GFFM_OK && e != cudaSuccess) st = gffm::cuda_error(e, what);
+    };
+    fail(cudaStreamBeginCapture(s0, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture");
+    if (!st) {
+        cudaStream_t pq_stream = s0;
+        if (overlap && p->n_mm > 0 && p->n_pq > 0) {
+            fail(cudaStreamCreateWithFlags(&s1, cudaStreamNonBlocking), "cudaStreamCreate");
+            fail(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming), "cudaEventCreate");
+            fail(cudaEventCreateWithFlags(&join, cudaEventDisableTiming), "cudaEventCreate");
+            fail(cudaEventRecord(fork, s0), "cudaEventRecord");
+            fail(cudaStreamWaitEvent(s1, fork, 0), "cudaStreamWaitEvent");
+            pq_stream = s1;
+        }
+        if (p->n_pq > 0) {
+            fail(cudaMemsetAsync(p->d_next, 0, sizeof(int), pq_stream), "cudaMemsetAsync");
+            PQArgs a;
+            a.inst = p->d_pq;
+            a.order = p->d_order;
+            a.count = p->n_pq;
+            a.nb = p->pq_nb;
+            a.rcap = p->pq_rcap;
+            a.next = p->d_next;
+            a.tmp = p->d_tmp;
+            a.tmp_ldw = p->tmp_ldw;
+            a.tmp_ldlw = p->tmp_ldlw;
+            k_pluq_batched<<<p->pq_grid, PQ_THREADS, p->pq_smem, pq_stream>>>(a);
+            fail(cudaGetLastError(), "k_pluq_batched");
+        }
+        for (const auto &z : p->zero_k)
+            fail(cudaMemset2DAsync(z.C, (size_t)z.ldc * 8, 0, (size_t)z.m * 8, (size_t)z.n, s0), "cudaMemset2DAsync");
+        if (p->n_mm > 0 && p->nitems > 0) {
+            k_split_batched<<<(unsigned)p->split_blocks, 256, 0, s0>>>(p->d_jobs, p->njobs);
+            fail(cudaGetLastError(), "k_split_batched");
+            k_gemm_grouped<<<p->gemm_grid, NUM_THREADS, G_SMEM_BYTES, s0>>>(p->d_mm, p->d_items, p->nitems, p->d_tmaps,
+                                                                          gffm::device_error_flag());
+            fail(cudaGetLastError(), "k_gemm_grouped");
+        }
+        if (s1) {
+            fail(cudaEventRecord(join, s1), "cudaEventRecord");
+            fail(cudaStreamWaitEvent(s0, join, 0), "cudaStreamWaitEvent");
+        }
+        cudaError_t e = cudaStreamEndCapture(s0, &graph);
+        fail(e, "cudaStreamEndCapture");
+    }
+    if (!st) fail(cudaGraphInstantiate(&p->exec, graph, 0), "cudaGraphInstantiate");
+    if (graph) cudaGraphDestroy(graph);
+    if (fork) cudaEventDestroy(fork);
+    if (join) cudaEventDestroy(join);
+    if (s1) cudaStreamDestroy(s1);
+    cudaStreamDestroy(s0);
+    return st;
+}
+
+void free_plan(gffm_batch_plan p) {
+    if (!p) return;
+    if (p->exec) cudaGraphExecDestroy(p->exec);
+    if (p->mem) cudaFree(p->mem);
+    delete p;
+}
+
+int create(const gffm_batch_desc *descs, int64_t count, const gffm_batch_tuning *tuning, gffm_batch_plan *out) {
+    using namespace batched;
+    if (!out) return set_error(GFFM_ERR_ARG, "plan is NULL");
+    *out = nullptr;
+    if (count < 0 || (count > 0 && !descs)) return set_error(GFFM_ERR_ARG, "bad descriptor array");
+    if (count > (int64_t(1) << 24)) return set_error(GFFM_ERR_ARG, "too many instances");
+    for (int64_t i = 0; i < count; i++) {
+        int st = check_desc(descs[i], i);
+        if (st) return st;
+    }
+    int st = gffm::check_device();
+    if (st) return st;
+    gffm_batch_tuning tu{};
+    if (tuning) tu = *tuning;
+    if (tu.pluq_panel != 0 && tu.pluq_panel != 8 && tu.pluq_panel != 16 && tu.pluq_panel != 32)
+        return set_error(GFFM_ERR_ARG, "pluq_panel must be 0, 8, 16 or 32");
+    if (tu.gemm_ctas < 0 || tu.pluq_ctas < 0) return set_error(GFFM_ERR_ARG, "negative grid size");
+
+    auto *p = new gffm_batch_plan_s();
+    PLAN_CUDA(cudaGetDevice(&p->device));
+    const int sms = gffm::sm_count();
+
+    std::vector<int64_t> mm_ids, pq_ids;
+    for (int64_t i = 0; i < count; i++) {
+        const gffm_batch_desc &d = descs[i];
+        if (d.m == 0 || d.n == 0) {
+            if (d.op == GFFM_BATCH_PLUQ) pq_ids.push_back(i);   // still reports its info
+            continue;
+        }
+        (d.op == GFFM_BATCH_MATMUL ? mm_ids : pq_ids).push_back(i);
+    }
+    p->n_mm = (int)mm_ids.size();
+    p->n_pq = (int)pq_ids.size();
+
+    // ---- layout of the one device allocation ----
+    Carve cv;
+    const size_t o_mm = cv.take(sizeof(MMInst) * std::max(1, p->n_mm));
+    const size_t o_tm = cv.take(sizeof(CUtensorMap) * 2 * std::max(1, p->n_mm), 128);
+    std::vector<MMInst> mm(p->n_mm);
+    std::vector<WorkItem> items;
+    std::vector<SplitJob> jobs;
+    std::vector<size_t> o_da(p->n_mm), o_db(p->n_mm);
+    std::vector<limb::Layout> lay(p->n_mm);
+    int64_t blk = 0;
+    for (int q = 0; q < p->n_mm; q++) {
+        const gffm_batch_desc &d = descs[mm_ids[q]];
+        MMInst &I = mm[q];
+        lay[q] = limb::layout(d.m, d.n, d.k, d.N);
+        const limb::Layout &g = lay[q];
+        I.m = (int)d.m;
+        I.n = (int)d.n;
+        I.L = g.L;
+        I.kblocks = (int)(d.k > 0 ? g.Kpad / BK : 0);
+        I.mtiles = (int)((d.m + BM - 1) / BM);
+        I.ntiles = (int)((d.n + BN - 1) / BN);
+        I.chunk_kb = 64 / g.L;
+        I.Mpad = (int)g.Mpad;
+        I.Npad = (int)g.Npad;
+        I.pad_ = 0;
+        I.N = d.N;
+        I.minv = ~uint64_t(0) / (uint64_t)d.N;
+        I.bias = d.N * (((int64_t(1) << 60) + d.N - 1) / d.N);
+        int64_t w = 1 % d.N;
+        for (int sft = 0; sft < MAX_SHIFTS; sft++) {
+            I.W[sft] = (int32_t)w;
+            w = (w * 128) % d.N;
+        }
+        I.C = d.C;
+        I.ldc = d.ldc;
+        if (d.k == 0) p->zero_k.push_back({d.C, d.ldc, d.m, d.n});
+        o_da[q] = cv.take(g.a_bytes, 1024);
+        o_db[q] = cv.take(g.b_bytes, 1024);
+    }
+    const size_t o_pq = cv.take(sizeof(PQInst) * std::max(1, p->n_pq));
+    const size_t o_order = cv.take(sizeof(int) * std::max(1, p->n_pq));
+    const size_t o_next = cv.take(sizeof(int));
+    std::vector<PQInst> pq(p->n_pq);
+    std::vector<size_t> o_w(p->n_pq), o_lw(p->n_pq);
+    int rcap = 4;
+    for (int q = 0; q < p->n_pq; q++) {
+        const gffm_batch_desc &d = descs[pq_ids[q]];
+        PQInst &I = pq[q];
+        I.m = (int)d.m;
+        I.n = (int)d.n;
+        I.l_cols = (int)d.l_cols;
+        I.lsw = (int)std::min<int64_t>((d.m + 31) / 32 * 32, d.l_cols);
+        I.M.n = (uint32_t)d.N;
+        I.M.minv = ~uint64_t(0) / (uint64_t)d.N;
+        I.mont = elim::make_mont((uint32_t)d.N);
+        I.A = d.A;
+        I.lda = d.lda;
+        I.U = d.C;
+        I.ldu = d.ldc;
+        I.L = d.L;
+        I.ldl = d.ldl;
+        I.ldw = (int)align_up((size_t)std::max<int64_t>(d.n, 1), 4);
+        I.lwc = (int)std::min<int64_t>(d.l_cols, d.n);
+        I.ldlw = (int)align_up((size_t)std::max(I.lwc, 1), 4);
+        I.pad_ = 0;
+        I.row_swaps = d.row_swaps;
+        I.col_swaps = d.col_swaps;
+        I.info = d.info;
+        o_w[q] = cv.take((size_t)std::max<int64_t>(d.m, 1) * I.ldw * 4);
+        o_lw[q] = cv.take((size_t)std::max<int64_t>(d.m, 1) * I.ldlw * 4);
+        rcap = std::max(rcap, (int)align_up((size_t)d.m, 4));
+        p->tmp_ldw = std::max(p->tmp_ldw, I.ldw);
+        p->tmp_ldlw = std::max(p->tmp_ldlw, I.ldlw);
+    }
+    // PLUQ grid (it sizes the per-CTA row-move buffers)
+    p->pq_nb = tu.pluq_panel ? tu.pluq_panel : 32;
+    p->pq_rcap = rcap;
+    p->pq_smem = pq_smem_words(rcap) * 4;
+    int per_sm = 1;
+    if (p->n_pq > 0) {
+        PLAN_CUDA(cudaFuncSetAttribute(k_pluq_batched, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->pq_smem));
+        PLAN_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pluq_batched, PQ_THREADS, p->pq_smem));
+        if (per_sm < 1) {
+            free_plan(p);
+            return set_error(GFFM_ERR_UNSUPPORTED, "batched PLUQ panel does not fit in shared memory");
+        }
+    }
+    p->pq_grid = std::max(1, std::min(p->n_pq, tu.pluq_ctas ? tu.pluq_ctas : per_sm * sms));
+    const size_t o_tmp = cv.take((size_t)p->pq_grid * PQ_MAX_MOVES * (p->tmp_ldw + p->tmp_ldlw) * 4);
+    // work items (output tiles), largest instances first
+    std::vector<int> mm_order(p->n_mm);
+    std::iota(mm_order.begin(), mm_order.end(), 0);
+    std::stable_sort(mm_order.begin(), mm_order.end(), [&](int a, int b) {
+        return (int64_t)mm[a].L * mm[a].L * mm[a].kblocks > (int64_t)mm[b].L * mm[b].L * mm[b].kblocks;
+    });
+    for (int q : mm_order)
+        for (int tm = 0; tm < mm[q].mtiles; tm++)
+            for (int tn = 0; tn < mm[q].ntiles; tn++)
+                if (mm[q].kblocks > 0) items.push_back(WorkItem{q, tm, tn, 0});
+    p->nitems = (int)items.size();
+    const size_t o_items = cv.take(sizeof(WorkItem) * std::max<size_t>(1, items.size()));
+    const size_t o_jobs = cv.take(sizeof(SplitJob) * std::max(1, 2 * p->n_mm));
+    p->mem_bytes = cv.off;
+    cudaError_t e = cudaMalloc(&p->mem, p->mem_bytes);
+    if (e != cudaSuccess) {
+        free_plan(p);
+        return gffm::cuda_error(e, "cudaMalloc (batched plan)");
+    }
+    uint8_t *base = static_cast<uint8_t *>(p->mem);
+    p->d_mm = reinterpret_cast<MMInst *>(base + o_mm);
+    p->d_tmaps = reinterpret_cast<CUtensorMap *>(base + o_tm);
+    p->d_pq = reinterpret_cast<PQInst *>(base + o_pq);
+    p->d_order = reinterpret_cast<int *>(base + o_order);
+    p->d_next = reinterpret_cast<int *>(base + o_next);
+    p->d_items = reinterpret_cast<WorkItem *>(base + o_items);
+    p->d_jobs = reinterpret_cast<SplitJob *>(base + o_jobs);
+    p->d_tmp = reinterpret_cast<int32_t *>(base + o_tmp);
+
+    // split jobs and TMA descriptors
+    std::vector<CUtensorMap> tmaps(2 * std::max(1, p->n_mm));
+    for (int q = 0; q < p->n_mm; q++) {
+        const gffm_batch_desc &d = descs[mm_ids[q]];
+        const limb::Layout &g = lay[q];
+        __half *da = reinterpret_cast<__half *>(base + o_da[q]);
+        __half *db = reinterpret_cast<__half *>(base + o_db[q]);
+        if (mm[q].kblocks > 0) {
+            SplitJob ja{d.A, d.lda, da, (int)d.m, (int)d.k, (int)g.Mpad, (int)g.Kpad, g.L, 0, d.N, mm[q].minv, blk};
+            blk += (g.Kpad / 32) * (g.Mpad / 32);
+            jobs.push_back(ja);
+            SplitJob jb{d.B, d.ldb, db, (int)d.k, (int)d.n, (int)g.Npad, (int)g.Kpad, g.L, 1, d.N, mm[q].minv, blk};
+            blk += ((g.Kpad / 2) * g.Npad + 255) / 256;
+            jobs.push_back(jb);
+        }
+        st = limb::encode_digit_map(&tmaps[2 * q], da, g.Kpad, (int64_t)g.L * g.Mpad, BM);
+        if (!st) st = limb::encode_digit_map(&tmaps[2 * q + 1], db, g.Kpad, (int64_t)g.L * g.Npad, BN);
+        if (st) {
+            free_plan(p);
+            return st;
+        }
+    }
+    p->njobs = (int)jobs.size();
+    p->split_blocks = blk;
+    // PLUQ workspace pointers and order (largest work first)
+    std::vector<int> order(p->n_pq);
+    for (int q = 0; q < p->n_pq; q++) {
+        pq[q].W = reinterpret_cast<int32_t *>(base + o_w[q]);
+        pq[q].LW = reinterpret_cast<int32_t *>(base + o_lw[q]);
+    }
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+        const int64_t wa = (int64_t)pq[a].m * pq[a].n * std::min(pq[a].m, pq[a].n);
+        const int64_t wb = (int64_t)pq[b].m * pq[b].n * std::min(pq[b].m, pq[b].n);
+        return wa > wb;
+    });
+
+    p->gemm_grid = std::max(1, std::min(p->nitems, tu.gemm_ctas ? tu.gemm_ctas : sms));
+    if (p->n_mm > 0) {
+        PLAN_CUDA(cudaFuncSetAttribute(k_gemm_grouped, cudaFuncAttributeMaxDynamicSharedMemorySize, G_SMEM_BYTES));
+    }
+
+    // upload the metadata
+    PLAN_CUDA(cudaMemcpy(p->d_mm, mm.data(), sizeof(MMInst) * mm.size(), cudaMemcpyHostToDevice));
+    PLAN_CUDA(cudaMemcpy(p->d_tmaps, tmaps.data(), sizeof(CUtensorMap) * 2 * p->n_mm, cudaMemcpyHostToDevice));
+    PLAN_CUDA(cudaMemcpy(p->d_items, items.data(), sizeof(WorkItem) * items.size(), cudaMemcpyHostToDevice));
+    PLAN_CUDA(cudaMemcpy(p->d_jobs, jobs.data(), sizeof(SplitJob) * jobs.size(), cudaMemcpyHostToDevice));
+    PLAN_CUDA(cudaMemcpy(p->d_pq, pq.data(), sizeof(PQInst) * pq.size(), cudaMemcpyHostToDevice));
+    PLAN_CUDA(cudaMemcpy(p->d_order, order.data(), sizeof(int) * order.size(), cudaMemcpyHostToDevice));
+
+    st = build_graph(p, tu.overlap != 0);
+    if (st) {
+        free_plan(p);
+        return st;
+    }
+    *out = p;
+    return GFFM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int gffm_batched_plan_create(const gffm_batch_desc *descs, int64_t count, const gffm_batch_tuning *tuning,
+                             gffm_batch_plan *plan) {
+    return create(descs, count, tuning, plan);
+}
+
+int gffm_batched_plan_info(gffm_batch_plan plan, int64_t *info) {
+    if (!plan || !info) return set_error(GFFM_ERR_ARG, "null argument");
+    info[0] = (int64_t)plan->mem_bytes;
+    info[1] = plan->n_mm;
+    info[2] = plan->n_pq;
+    info[3] = plan->nitems;
+    info[4] = plan->gemm_grid;
+    info[5] = plan->pq_grid;
+    return GFFM_OK;
+}
+
+int gffm_batched_run(gffm_batch_plan plan, gffm_stream_t stream) {
+    if (!plan) return set_error(GFFM_ERR_ARG, "plan is NULL");
+    if (!plan->exec) return GFFM_OK;
+    int dev = 0;
+    GFFM_CUDA(cudaGetDevice(&dev));
+    if (dev != plan->device) return set_error(GFFM_ERR_ARG, "the plan belongs to device %d", plan->device);
+    GFFM_CUDA(cudaGraphLaunch(plan->exec, gffm::as_stream(stream)));
+    return GFFM_OK;
+}
+
+int gffm_batched_plan_destroy(gffm_batch_plan plan) {
+    free_plan(plan);
+    return GFFM_OK;
+}
+
+}  // extern "C"

@@ -326,55 +326,6 @@ static int permute_rows(Work &w, const PermArgs &perm, int c_lo, int c_hi, cudaS
 }
 
 // deterministic Miller-Rabin for 32-bit n (bases 2, 7, 61)
-static bool is_prime_u32(uint32_t n) {
-    if (n < 2) return false;
-    for (uint32_t p : {2u, 3u, 5u, 7u, 11u, 13u, 61u})
-        if (n % p == 0) return n == p;
-    uint32_t d = n - 1;
-    int s = 0;
-    while ((d & 1) == 0) {
-        d >>= 1;
-        s++;
-    }
-    auto powm = [n](uint64_t b, uint32_t e) {
-        uint64_t r = 1;
-        b %= n;
-        while (e) {
-            if (e & 1) r = r * b % n;
-            b = b * b % n;
-            e >>= 1;
-        }
-        return r;
-    };
-    for (uint32_t a : {2u, 7u, 61u}) {
-        uint64_t x = powm(a, d);
-        if (x == 1 || x == n - 1) continue;
-        bool comp = true;
-        for (int i = 1; i < s; i++) {
-            x = x * x % n;
-            if (x == n - 1) {
-                comp = false;
-                break;
-            }
-        }
-        if (comp) return false;
-    }
-    return true;
-}
-
-static Mont make_mont(uint32_t n) {
-    Mont M{};
-    M.n = n;
-    M.prime = (n & 1u) && is_prime_u32(n);
-    if (n & 1u) {
-        uint32_t inv = n;  // Newton iteration for n^{-1} mod 2^32
-        for (int i = 0; i < 5; i++) inv *= 2u - n * inv;
-        M.nprime = 0u - inv;
-        M.r2 = (uint32_t)(((unsigned __int128)1 << 64) % n);
-    }
-    return M;
-}
-
 static int run_panel(Work &w, int m, int n, int R0, int C0, int nbw, const ModP &M, int lcols_check,
                      cudaStream_t s, int h_res[2], std::vector<int32_t> &h_prow, std::vector<int32_t> &h_pv) {
     using namespace gffm;

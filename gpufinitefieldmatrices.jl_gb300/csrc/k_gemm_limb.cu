@@ -37,6 +37,12 @@ static int make_map(CUtensorMap *map, const void *base, int64_t kpad, int64_t ro
     return GFFM_OK;
 }
 
+int encode_digit_map(void *map, const void *base, int64_t kpad, int64_t rows, int box_rows) {
+    int st = get_encoder();
+    if (st) return st;
+    return make_map(static_cast<CUtensorMap *>(map), base, kpad, rows, box_rows);
+}
+
 int limbs_for(int64_t N) {
     // largest centred residue floor(N/2) must fit L balanced base-128 digits:
     // max positive value 63 * (128^L - 1) / 127

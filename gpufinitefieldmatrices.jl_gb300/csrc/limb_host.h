@@ -43,6 +43,10 @@ template <typename T>
 int split_b(const T *B, int64_t ldb, int64_t k, int64_t n, __half *D, const Layout &g, int64_t N, cudaStream_t s,
             int mode = SPLIT_CENTRED, const T *B2 = nullptr);
 
+// Encode the TMA descriptor (a 128-byte CUtensorMap at `map`) of a digit array:
+// `rows` rows of `kpad` fp16, box 64 x box_rows, 128-byte swizzle.
+int encode_digit_map(void *map, const void *base, int64_t kpad, int64_t rows, int box_rows);
+
 // C (m x n, ldc) <- epilogue(A*B mod N) from digit planes; epi is a limb::Epi.  X, Y: EPI_KSUB_F64 only.
 int gemm_digits(const Layout &g, const __half *Ad, const __half *Bd, int64_t m, int64_t n, int64_t k, int64_t N,
                 void *C, int64_t ldc, int epi, int max_ctas, cudaStream_t s, const double *X = nullptr,

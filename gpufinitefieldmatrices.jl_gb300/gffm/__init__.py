@@ -43,3 +43,4 @@ sub_ = _dispatch("sub_")
 negate_ = _dispatch("negate_")
 zero_ = _dispatch("zero_")
 copy_ = _dispatch("copy_")
+from .batched import BatchPlan, Tuning as BatchTuning, batched_plan  # noqa: F401,E402

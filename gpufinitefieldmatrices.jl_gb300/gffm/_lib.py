@@ -67,6 +67,10 @@ SIGNATURES.update({
     "gffm_karatsuba_scalar_mul_f64": (_INT, [_P, _P, _P, _P, _I64, _I64, _I64, _I64, _P]),
     "gffm_karatsuba_from_values_f64": (_INT, [_P, _P, _P, _I64, _I64, _I64, _P]),
     "gffm_karatsuba_to_values_f64": (_INT, [_P, _P, _P, _I64, _I64, _I64, _P]),
+    "gffm_batched_plan_create": (_INT, [_P, _I64, _P, _P]),
+    "gffm_batched_plan_info": (_INT, [_P, _PI64]),
+    "gffm_batched_run": (_INT, [_P, _P]),
+    "gffm_batched_plan_destroy": (_INT, [_P]),
 })
 
 STATUS = {

@@ -265,6 +265,56 @@ GFFM_API int gffm_karatsuba_from_values_f64(double *D1, double *D2, const double
 GFFM_API int gffm_karatsuba_to_values_f64(double *A, const double *D1, const double *D2, int64_t len, int64_t N1,
                                           int64_t N2, gffm_stream_t stream);
 
+/* ---- batched uneven instances ---------------------------------------------
+ * No reference entry point: the reference runs one CuModMatrix product
+ * (mul!, CuModMatrix.jl:767-787) or one pluq_gpu_kernel (pluq_kernels.jl:46-157)
+ * per call.  A batch holds thousands of independent instances, each with its
+ * own sizes and modulus (2 <= N < 2^26), each a product or a PLUQ with the
+ * semantics of those calls.  Products run in one grouped tcgen05 kernel over
+ * all instances' output tiles, PLUQs in one persistent kernel (a CTA per
+ * instance); a plan validates the batch, lays out its workspace, encodes the
+ * per-instance TMA descriptors and captures the launches in a CUDA graph once.
+ * A plan is bound to the buffers its descriptors name. */
+enum gffm_batch_op { GFFM_BATCH_MATMUL = 0, GFFM_BATCH_PLUQ = 1 };
+
+typedef struct gffm_batch_desc {
+    int64_t op;            /* gffm_batch_op */
+    int64_t m, n, k;       /* MATMUL: C (m x n) = A (m x k) * B (k x n) mod N; PLUQ: A is m x n, m <= 1024 */
+    int64_t N;
+    const double *A;       /* column-major Float64 residues (device) */
+    int64_t lda;
+    const double *B;       /* MATMUL */
+    int64_t ldb;
+    double *C;             /* MATMUL: the product; PLUQ: U (may alias A) */
+    int64_t ldc;
+    double *L;             /* PLUQ: m x l_cols (the reference's L has l_cols = m + 32) */
+    int64_t ldl;
+    int64_t l_cols;
+    int64_t *row_swaps;    /* PLUQ, device, capacity 2*m: 1-based (i, j) pairs */
+    int64_t *col_swaps;    /* PLUQ, device, capacity 2*n */
+    int64_t *info;         /* PLUQ, device int64[4]: #row swaps, #col swaps, rank, status (0 or GFFM_ERR_BOUNDS) */
+} gffm_batch_desc;
+
+/* Tuning of a plan; 0 in a field picks the default.  pluq_panel: panel width
+ * (8, 16 or 32); gemm_ctas / pluq_ctas: persistent grid sizes; overlap: 1 runs
+ * the products and the PLUQs on two graph branches at once. */
+typedef struct gffm_batch_tuning {
+    int32_t pluq_panel;
+    int32_t gemm_ctas;
+    int32_t pluq_ctas;
+    int32_t overlap;
+} gffm_batch_tuning;
+
+typedef struct gffm_batch_plan_s *gffm_batch_plan;
+
+GFFM_API int gffm_batched_plan_create(const gffm_batch_desc *descs, int64_t count, const gffm_batch_tuning *tuning,
+                                      gffm_batch_plan *plan);
+/* info[0..5]: device bytes held, products, PLUQs, product output tiles, gemm CTAs, PLUQ CTAs */
+GFFM_API int gffm_batched_plan_info(gffm_batch_plan plan, int64_t *info);
+/* Launch the plan's graph on `stream` (asynchronous; the PLUQ results are in the descriptors' device arrays). */
+GFFM_API int gffm_batched_run(gffm_batch_plan plan, gffm_stream_t stream);
+GFFM_API int gffm_batched_plan_destroy(gffm_batch_plan plan);
+
 /* ---- limb GEMM without allocation -----------------------------------------
  * No counterpart in the reference.  For callers that cannot allocate device
  * memory when they multiply: a process whose HBM is already reserved by
