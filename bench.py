@@ -50,7 +50,11 @@ def parse_args():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain FP64 comparison")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--pluq", type=int, default=-1, help="PLUQ size to time (-1: default when available, 0: skip)")
+    ap.add_argument("--pluq", type=int, default=-1, help="PLUQ size to time (-1: 16384, 0: skip)")
+    ap.add_argument("--no-pluq-plain", action="store_true", help="skip the plain-Float64 PLUQ (about 10-30 s)")
+    ap.add_argument("--no-karatsuba", action="store_true")
+    ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--batch", type=int, default=4096, help="instances of the batched workload")
     ap.add_argument("--size", type=int, default=8192, help="m = n = k (8192 is the benchmark workload)")
     return ap.parse_args()
 
@@ -304,9 +308,11 @@ def run_ours(args):
         out["plain_fp64"] = plain_run(L, sp, dev)
         out["plain_fp64"]["limb_speedup"] = round(value / world / out["plain_fp64"]["value"], 1)
     if args.pluq != 0:
-        pl = pluq_run(args, L, sp, dev)
-        if pl is not None:
-            out["pluq"] = pl
+        out["pluq"] = pluq_run(args, L, sp, dev)
+    if not args.no_karatsuba:
+        out["karatsuba"] = karatsuba_run(L, sp, dev)
+    if not args.no_batched:
+        out["batched"] = batched_run(args, dev, value / world)
     if rank == 0 and not args.no_cpu:
         gops, threads, desc = cpu_sample()
         out["cpu_baseline"] = {"value": round(gops, 3), "unit": "Gop/s", "cores": threads, "kind": "port",
@@ -417,12 +423,146 @@ def plain_run(L, sp, dev):
 
 
 def pluq_run(args, L, sp, dev):
-    try:
-        import gffm
-        from gffm import elimination  # noqa: F401
-    except ImportError:
-        return None
-    return elimination.bench_pluq(args.pluq, sp, dev)
+    """Full-rank PLUQ mod p26 at 16384^2 on both forms (limb tensor-core trailing
+    products vs the plain Float64 ones), and the 1024^2 rank-900 PLUQ + RREF."""
+    import numpy as np
+    import torch
+    import gffm
+    import oracle
+    from gffm import elimination
+    out = {"limb": elimination.bench_pluq(args.pluq, sp, dev, reps=2)}
+    if not args.no_pluq_plain:
+        out["plain"] = elimination.bench_pluq(args.pluq, sp, dev, reps=1, method="plain", warmup=0)
+        out["limb_speedup"] = round(out["plain"]["seconds"] / out["limb"]["seconds"], 1)
+    # 1024 x 1024 of rank 900: (1024 x 900)(900 x 1024) mod p26, seeded
+    rng = np.random.default_rng(900)
+    X = rng.integers(0, P26, size=(1024, 900))
+    Y = rng.integers(0, P26, size=(900, 1024))
+    A = gffm.CuModMatrix(oracle.matmul(X, Y, P26), P26, elem_type=torch.float64)
+    t = {}
+    for name, fn in (("pluq", lambda: gffm.pluq_gpu_kernel(A)), ("rref", lambda: gffm.rref_gpu_type(A))):
+        fn()
+        torch.cuda.synchronize()
+        best = 1e9
+        for _ in range(5):
+            t0 = time.perf_counter()
+            fn()
+            torch.cuda.synchronize()
+            best = min(best, time.perf_counter() - t0)
+        t[name + "_ms"] = round(best * 1e3, 3)
+    t["rank"] = elimination.pluq_rank(A)
+    out["rank900_1024"] = t
+    return out
+
+
+def karatsuba_run(L, sp, dev):
+    """4096^2 two-component products mod p25 (3 component products, 4.12e11 counted
+    modular ops): the polynomial form, the reference's digit form (N1 = N2 = p25), and
+    the 4-product schoolbook on the same GEMM for comparison."""
+    import torch
+    import gffm
+    n, p = 4096, 33554393
+    g = torch.Generator(device=dev)
+    g.manual_seed(5)
+    Ms = [gffm.rand(torch.float64, n, n, p, generator=g) for _ in range(4)]
+    C = [gffm.zeros(torch.float64, n, n, p) for _ in range(3)]
+    ws = ctypes.c_size_t(0)
+    L.gffm_karatsuba_workspace_size(n, n, n, p, p, ctypes.byref(ws))
+    wbuf = torch.empty(ws.value, dtype=torch.uint8, device=dev)
+    d = [x.data.data_ptr() for x in Ms]
+    c = [x.data.data_ptr() for x in C]
+    ld = Ms[0].ld
+
+    def poly():
+        assert L.gffm_karatsuba_poly_matmul_f64(n, n, n, d[0], d[1], ld, d[2], d[3], ld, c[0], c[1], c[2], ld, p,
+                                                wbuf.data_ptr(), ws.value, sp) == 0
+
+    def digit():
+        assert L.gffm_karatsuba_matmul_f64(n, n, n, d[0], d[1], ld, d[2], d[3], ld, c[0], c[1], ld, p, p,
+                                           wbuf.data_ptr(), ws.value, sp) == 0
+
+    def timed(fn, reps=5):
+        fn()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    ops = 3 * 2.0 * n ** 3
+    tp, td = timed(poly), timed(digit)
+    # schoolbook: four products and one modular add (C1 = A0 B1 + A1 B0)
+    T = gffm.zeros(torch.float64, n, n, p)
+
+    def school4():
+        for (a, b, cc) in ((0, 2, c[0]), (1, 3, c[2]), (0, 3, c[1]), (1, 2, T.data.data_ptr())):
+            assert L.gffm_matmul_limb_f64(n, n, n, d[a], ld, d[b], ld, cc, ld, p, wbuf.data_ptr(), ws.value, sp) == 0
+        assert L.gffm_add_f64(c[1], c[1], T.data.data_ptr(), C[1].data.numel(), p, sp) == 0
+
+    ts = timed(school4)
+    return {"size": n, "modulus": p, "ops_counted": ops,
+            "poly_ms": round(tp, 3), "poly_gops": round(ops / tp / 1e6, 1),
+            "digit_form_ms": round(td, 3), "digit_form_gops": round(ops / td / 1e6, 1),
+            "schoolbook4_ms": round(ts, 3), "karatsuba_speedup_vs_schoolbook": round(ts / tp, 2)}
+
+
+def batched_run(args, dev, large_gemm_gops):
+    """The batched uneven-instance workload: 4096 instances, n uniform over the multiples
+    of 32 in [32, 512], p over the 32 fixed primes, half products half PLUQs, one graph."""
+    import torch
+    import gffm
+    from gffm import batched
+    specs = batched.config4_specs(args.batch, seed=1234)
+    g = torch.Generator(device=dev)
+    g.manual_seed(1234)
+    inst = batched.build_config4(specs, generator=g)
+    ops = batched.ops_of(specs)
+
+    def timed(plan, reps=5):
+        plan.run()
+        plan.run()
+        plan.run()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            plan.run()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    plan = gffm.BatchPlan(inst)
+    ms = timed(plan)
+    info = [x for x in plan.pluq_info() if x is not None]
+    full_rank = sum(1 for (op, n, _), x in zip([s for s in specs if s[0] == "pluq"], info) if x[2] == n)
+    out = {"instances": len(specs), "ops": ops, "ms": round(ms, 3), "gops": round(ops / ms / 1e6, 1),
+           "frac_of_large_gemm": round(ops / ms / 1e6 / large_gemm_gops, 3), "plan": plan.info(),
+           "pluq_full_rank": "%d/%d" % (full_rank, len(info))}
+    best = (ms, None)
+    for tu in ((0, 0, 0, 1), (16, 0, 0, 0), (16, 0, 0, 1)):
+        p2 = gffm.BatchPlan(inst, gffm.BatchTuning(*tu))
+        t2 = timed(p2)
+        out["tuning_%d_%d_%d_%d_ms" % tu] = round(t2, 3)
+        if t2 < best[0]:
+            best = (t2, tu)
+        del p2
+    mm = gffm.BatchPlan([x for x in inst if x[0] == "matmul"])
+    out["products_only_ms"] = round(timed(mm), 3)
+    del mm
+    pq = gffm.BatchPlan([x for x in inst if x[0] == "pluq"])
+    out["pluqs_only_ms"] = round(timed(pq), 3)
+    del pq
+    if best[1] is not None:
+        out["best_ms"] = round(best[0], 3)
+        out["best_tuning"] = list(best[1])
+        out["best_gops"] = round(ops / best[0] / 1e6, 1)
+        out["best_frac_of_large_gemm"] = round(ops / best[0] / 1e6 / large_gemm_gops, 3)
+    return out
 
 
 def main():

@@ -63,9 +63,12 @@ struct PQArgs {
     int tmp_ldw, tmp_ldlw;       // their row strides (>= every ldw / ldlw)
 };
 
-// shared-memory words a CTA needs for panel height rcap
+// shared-memory words a CTA needs for panel height rcap (panel + trailing pivot
+// rows; at least the 8 transpose tiles of 32 x 33 words the conversions use)
 __host__ __device__ constexpr size_t pq_smem_words(int rcap) {
-    return (size_t)PQ_MAX_NB * (rcap + 4) + (size_t)PQ_MAX_NB * PQ_CW;
+    return (size_t)PQ_MAX_NB * (rcap + 4) + (size_t)PQ_MAX_NB * PQ_CW > (size_t)8 * 32 * 33
+               ? (size_t)PQ_MAX_NB * (rcap + 4) + (size_t)PQ_MAX_NB * PQ_CW
+               : (size_t)8 * 32 * 33;
 }
 
 struct PQShared {
@@ -90,73 +93,150 @@ __device__ __forceinline__ uint32_t residue_of(double v, const elim::ModP &M) {
     return q ? M.n - q : 0;
 }
 
-// Column-major Float64 (m x n, ld) <-> row-major int32 (m x n, ldw) through 32 x 32
-// shared tiles (tile = 32 x 33 words of scratch).
+// Column-major Float64 (m x n, ld) <-> row-major int32 (m x n, ldw) through
+// 32 x 32 shared tiles, PQ_TPR tiles per round (scratch: PQ_TPR x 32 x 33 words):
+// every thread issues all 4 * PQ_TPR loads of a round before its first store.
+constexpr int PQ_TPR = 8;   // pq_smem_words reserves PQ_TPR * 32 * 33 words at least
+
 __device__ void to_rowmajor(const double *A, int64_t lda, int32_t *W, int ldw, int m, int n, const elim::ModP &M,
-                            int32_t *tile) {
+                            int32_t *scratch) {
     const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;   // 8 rows of 32 threads
-    for (int r0 = 0; r0 < m; r0 += 32)
-        for (int c0 = 0; c0 < n; c0 += 32) {
-            for (int cc = ty; cc < 32; cc += 8) {
-                const int r = r0 + tx, c = c0 + cc;
-                tile[cc * 33 + tx] = (r < m && c < n) ? (int32_t)residue_of(A[r + (int64_t)c * lda], M) : 0;
+    const int tc = (n + 31) >> 5, nt = ((m + 31) >> 5) * tc;
+    for (int t0 = 0; t0 < nt; t0 += PQ_TPR) {
+        double v[PQ_TPR][4];
+#pragma unroll
+        for (int q = 0; q < PQ_TPR; q++) {
+            const int r0 = ((t0 + q) / tc) * 32, c0 = ((t0 + q) % tc) * 32;
+#pragma unroll
+            for (int i = 0; i < 4; i++) {
+                const int r = r0 + tx, c = c0 + ty + 8 * i;
+                v[q][i] = (t0 + q < nt && r < m && c < n) ? A[r + (int64_t)c * lda] : 0.0;
             }
-            __syncthreads();
-            for (int rr = ty; rr < 32; rr += 8) {
-                const int r = r0 + rr, c = c0 + tx;
-                if (r < m && c < n) W[(int64_t)r * ldw + c] = tile[tx * 33 + rr];
-            }
-            __syncthreads();
         }
+#pragma unroll
+        for (int q = 0; q < PQ_TPR; q++)
+#pragma unroll
+            for (int i = 0; i < 4; i++) scratch[q * 1056 + (ty + 8 * i) * 33 + tx] = (int32_t)residue_of(v[q][i], M);
+        __syncthreads();
+#pragma unroll
+        for (int q = 0; q < PQ_TPR; q++) {
+            if (t0 + q >= nt) break;
+            const int r0 = ((t0 + q) / tc) * 32, c0 = ((t0 + q) % tc) * 32;
+#pragma unroll
+            for (int i = 0; i < 4; i++) {
+                const int r = r0 + ty + 8 * i, c = c0 + tx;
+                if (r < m && c < n) W[(int64_t)r * ldw + c] = scratch[q * 1056 + tx * 33 + ty + 8 * i];
+            }
+        }
+        __syncthreads();
+    }
 }
 
 __device__ void to_colmajor(const int32_t *W, int ldw, int wcols, double *A, int64_t lda, int m, int n,
-                            int32_t *tile) {
+                            int32_t *scratch) {
     const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
-    for (int r0 = 0; r0 < m; r0 += 32)
-        for (int c0 = 0; c0 < n; c0 += 32) {
-            for (int rr = ty; rr < 32; rr += 8) {
-                const int r = r0 + rr, c = c0 + tx;
-                tile[rr * 33 + tx] = (r < m && c < wcols) ? W[(int64_t)r * ldw + c] : 0;
+    const int tc = (n + 31) >> 5, nt = ((m + 31) >> 5) * tc;
+    for (int t0 = 0; t0 < nt; t0 += PQ_TPR) {
+        int32_t v[PQ_TPR][4];
+#pragma unroll
+        for (int q = 0; q < PQ_TPR; q++) {
+            const int r0 = ((t0 + q) / tc) * 32, c0 = ((t0 + q) % tc) * 32;
+#pragma unroll
+            for (int i = 0; i < 4; i++) {
+                const int r = r0 + ty + 8 * i, c = c0 + tx;
+                v[q][i] = (t0 + q < nt && r < m && c < wcols) ? W[(int64_t)r * ldw + c] : 0;
             }
-            __syncthreads();
-            for (int cc = ty; cc < 32; cc += 8) {
-                const int r = r0 + tx, c = c0 + cc;
-                if (r < m && c < n) A[r + (int64_t)c * lda] = (double)tile[tx * 33 + cc];
-            }
-            __syncthreads();
         }
+#pragma unroll
+        for (int q = 0; q < PQ_TPR; q++)
+#pragma unroll
+            for (int i = 0; i < 4; i++) scratch[q * 1056 + (ty + 8 * i) * 33 + tx] = v[q][i];
+        __syncthreads();
+#pragma unroll
+        for (int q = 0; q < PQ_TPR; q++) {
+            if (t0 + q >= nt) break;
+            const int r0 = ((t0 + q) / tc) * 32, c0 = ((t0 + q) % tc) * 32;
+#pragma unroll
+            for (int i = 0; i < 4; i++) {
+                const int r = r0 + tx, c = c0 + ty + 8 * i;
+                if (r < m && c < n) A[r + (int64_t)c * lda] = (double)scratch[q * 1056 + tx * 33 + ty + 8 * i];
+            }
+        }
+        __syncthreads();
+    }
 }
 
-// Gather the source rows of the composed row moves (columns [c_lo, c_hi) of a
-// row-major int32 matrix) into T (nmv rows of stride ldt) ...
+// Row moves of a panel on columns [c_lo, c_hi) of a row-major int32 matrix: gather
+// the sources into T (one row per move, stride ldt), then write the destinations
+// (times the pivot inverse for pivot rows when `scale`).  A warp per move row.
 __device__ __forceinline__ void gather_moves(const int32_t *X, int ldx, int c_lo, int c_hi, int32_t *T, int ldt,
                                              const PQShared &S) {
-    const int w = c_hi - c_lo;
-    if (w <= 0) return;
-    for (int idx = threadIdx.x; idx < S.nmv * w; idx += blockDim.x) {
-        const int k = idx / w, c = c_lo + (idx - k * w);
-        T[(int64_t)k * ldt + c] = X[(int64_t)S.mv_src[k] * ldx + c];
+    const int lane = threadIdx.x & 31;
+    for (int k = threadIdx.x >> 5; k < S.nmv; k += blockDim.x >> 5) {
+        const int32_t *src = X + (int64_t)S.mv_src[k] * ldx;
+        int32_t *dst = T + (int64_t)k * ldt;
+        for (int c = c_lo + lane; c < c_hi; c += 128) {
+            int32_t v[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++) v[u] = c + 32 * u < c_hi ? src[c + 32 * u] : 0;
+#pragma unroll
+            for (int u = 0; u < 4; u++)
+                if (c + 32 * u < c_hi) dst[c + 32 * u] = v[u];
+        }
     }
 }
-// ... and write them to their destinations (times the pivot inverse for pivot rows when `scale`).
 __device__ __forceinline__ void scatter_moves(int32_t *X, int ldx, int c_lo, int c_hi, const int32_t *T, int ldt,
                                               const PQShared &S, bool scale, const elim::ModP &M) {
-    const int w = c_hi - c_lo;
-    if (w <= 0) return;
-    for (int idx = threadIdx.x; idx < S.nmv * w; idx += blockDim.x) {
-        const int k = idx / w, c = c_lo + (idx - k * w);
-        const int32_t v = T[(int64_t)k * ldt + c];
-        const uint32_t sc = S.mv_scale[k];
-        X[(int64_t)S.mv_dst[k] * ldx + c] = (scale && sc) ? (int32_t)elim::mulmod((uint32_t)v, sc, M) : v;
+    const int lane = threadIdx.x & 31;
+    for (int k = threadIdx.x >> 5; k < S.nmv; k += blockDim.x >> 5) {
+        const int32_t *src = T + (int64_t)k * ldt;
+        int32_t *dst = X + (int64_t)S.mv_dst[k] * ldx;
+        const uint32_t sc = scale ? S.mv_scale[k] : 0u;
+        for (int c = c_lo + lane; c < c_hi; c += 128) {
+            int32_t v[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++) v[u] = c + 32 * u < c_hi ? src[c + 32 * u] : 0;
+#pragma unroll
+            for (int u = 0; u < 4; u++)
+                if (c + 32 * u < c_hi) dst[c + 32 * u] = sc ? (int32_t)elim::mulmod((uint32_t)v[u], sc, M) : v[u];
+        }
     }
 }
 
-__global__ void __launch_bounds__(PQ_THREADS) k_pluq_batched(PQArgs a) {
+__device__ __forceinline__ unsigned long long pkey32(uint32_t v, int lr) {
+    return ((unsigned long long)v << 32) | (0xFFFFFFFFu - (uint32_t)lr);
+}
+
+// Warp-wide: the pivot of panel column j from the lanes' best keys; lane 0 records
+// it (pivot row, value, inverse) as pivot number `t`, or flags a zero column, or the
+// reference's out-of-bounds L column.
+__device__ __forceinline__ void decide_pivot(unsigned long long best, int t, int r0, int j, int c0, int l_cols,
+                                             const elim::Mont &mont, PQShared &S) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long other = __shfl_xor_sync(0xffffffffu, best, o);
+        best = other > best ? other : best;
+    }
+    if ((threadIdx.x & 31) == 0) {
+        const uint32_t pv = (uint32_t)(best >> 32);
+        if (pv == 0) {
+            S.zero_hit = 1;
+        } else if (c0 + j >= l_cols) {
+            S.stop = 8;              // the reference indexes L out of bounds here
+        } else {
+            S.piv_prow[t] = r0 + (int)(0xFFFFFFFFu - (uint32_t)(best & 0xFFFFFFFFu));
+            S.piv_val[t] = pv;
+            S.piv_inv[t] = elim::mod_inverse(pv, mont);
+        }
+    }
+}
+
+__global__ void __launch_bounds__(PQ_THREADS, 2) k_pluq_batched(PQArgs a) {
     extern __shared__ __align__(16) int32_t pq_smem[];
     __shared__ PQShared S;
+    __shared__ uint32_t s_u[PQ_MAX_NB], s_us[PQ_MAX_NB];   // scaled pivot row of the panel and its Shoup factors
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int rs = a.rcap + 4;                        // panel column stride (words)
+    const int rs = a.rcap + 4;                        // panel column stride (words), a multiple of 4
     int32_t *P = pq_smem;                             // P[j * rs + lr]: panel column j, local row lr
     int32_t *Us = pq_smem + (size_t)PQ_MAX_NB * rs;   // Us[t * PQ_CW + c]: pivot rows of a trailing chunk
 
@@ -168,11 +248,18 @@ __global__ void __launch_bounds__(PQ_THREADS) k_pluq_batched(PQArgs a) {
         __syncthreads();
         const int ii = S.inst;
         if (ii < 0) break;
-        const PQInst I = a.inst[ii];
-        const int m = I.m, n = I.n;
-        const uint32_t N = I.M.n;
-        to_rowmajor(I.A, I.lda, I.W, I.ldw, m, n, I.M, Us);
-        for (int64_t idx = tid; idx < (int64_t)m * I.ldlw; idx += blockDim.x) I.LW[idx] = 0;
+        // the instance's fields, in registers
+        const PQInst *Ip = a.inst + ii;
+        const int m = Ip->m, n = Ip->n, l_cols = Ip->l_cols, lsw = Ip->lsw;
+        const elim::ModP M{Ip->M.n, Ip->M.minv};
+        const elim::Mont mont{Ip->mont.n, Ip->mont.nprime, Ip->mont.r2, Ip->mont.prime};
+        const uint32_t N = M.n;
+        int32_t *const W = Ip->W;
+        int32_t *const LW = Ip->LW;
+        const int ldw = Ip->ldw, ldlw = Ip->ldlw;
+        int64_t *const row_swaps = Ip->row_swaps;
+        to_rowmajor(Ip->A, Ip->lda, W, ldw, m, n, M, pq_smem);
+        for (int64_t idx = tid; idx < (int64_t)m * ldlw; idx += blockDim.x) LW[idx] = 0;
         __syncthreads();
 
         int row = 0, col = 0, nr = 0, nc = 0, status = 0;
@@ -183,7 +270,7 @@ __global__ void __launch_bounds__(PQ_THREADS) k_pluq_batched(PQArgs a) {
             // ---- panel load: W[r0 + lr][c0 + j] -> P[j][lr] ----
             for (int idx = tid; idx < R * nbc; idx += blockDim.x) {
                 const int lr = idx / nbc, j = idx - lr * nbc;
-                P[j * rs + lr] = I.W[(int64_t)(r0 + lr) * I.ldw + c0 + j];
+                P[j * rs + lr] = W[(int64_t)(r0 + lr) * ldw + c0 + j];
             }
             if (tid == 0) {
                 S.stop = 0;
@@ -191,36 +278,19 @@ __global__ void __launch_bounds__(PQ_THREADS) k_pluq_batched(PQArgs a) {
             }
             __syncthreads();
             int npiv = 0;
-            for (int j = 0; j < nbc && r0 + npiv < m; j++) {
-                // ---- pivot search: largest value, then lowest row ----
+            // Warp 0 decides the pivot of column j (search, inverse) while the other warps
+            // finish the previous step's update of columns j+1.. : the inverse is off the
+            // critical path except for the panel's first column.
+            if (warp == 0) {
                 unsigned long long best = 0;
-                for (int lr = npiv + tid; lr < R; lr += blockDim.x) {
-                    const uint32_t v = (uint32_t)P[j * rs + lr];
-                    const unsigned long long key = ((unsigned long long)v << 32) | (0xFFFFFFFFu - (uint32_t)lr);
+                for (int lr = lane; lr < R; lr += 32) {
+                    const unsigned long long key = pkey32((uint32_t)P[lr], lr);
                     best = key > best ? key : best;
                 }
-#pragma unroll
-                for (int o = 16; o > 0; o >>= 1) {
-                    const unsigned long long other = __shfl_xor_sync(0xffffffffu, best, o);
-                    best = other > best ? other : best;
-                }
-                if (lane == 0) S.red[warp] = best;
-                __syncthreads();
-                if (tid == 0) {
-                    unsigned long long b = 0;
-                    for (int w = 0; w < PQ_THREADS / 32; w++) b = S.red[w] > b ? S.red[w] : b;
-                    const uint32_t pv = (uint32_t)(b >> 32);
-                    if (pv == 0) {
-                        S.zero_hit = 1;
-                    } else if (c0 + j >= I.l_cols) {
-                        S.stop = 8;              // the reference indexes L out of bounds here
-                    } else {
-                        S.piv_prow[npiv] = r0 + (int)(0xFFFFFFFFu - (uint32_t)(b & 0xFFFFFFFFu));
-                        S.piv_val[npiv] = pv;
-                        S.piv_inv[npiv] = elim::mod_inverse(pv, I.mont);
-                    }
-                }
-                __syncthreads();
+                decide_pivot(best, 0, r0, 0, c0, l_cols, mont, S);
+            }
+            __syncthreads();
+            for (int j = 0; j < nbc; j++) {
                 if (S.zero_hit || S.stop) break;
                 const int plr = S.piv_prow[npiv] - r0;
                 const uint32_t inv = S.piv_inv[npiv];
@@ -230,95 +300,130 @@ __global__ void __launch_bounds__(PQ_THREADS) k_pluq_batched(PQArgs a) {
                     const int32_t x = P[jj * rs + plr];
                     const int32_t y = P[jj * rs + npiv];
                     P[jj * rs + plr] = y;
-                    P[jj * rs + npiv] = jj >= j ? (int32_t)elim::mulmod((uint32_t)x, inv, I.M) : x;
-                }
-                __syncthreads();
-                // ---- rank-1 update of the panel: rows below the pivot, columns right of j ----
-                for (int lr = npiv + 1 + tid; lr < R; lr += blockDim.x) {
-                    const uint32_t l = (uint32_t)P[j * rs + lr];
-                    if (!l) continue;
-                    const uint32_t nl = N - l;
-                    for (int jj = j + 1; jj < nbc; jj++) {
-                        const uint32_t u = (uint32_t)P[jj * rs + npiv];
-                        const uint32_t v = (uint32_t)P[jj * rs + lr] + elim::mulmod(nl, u, I.M);
-                        P[jj * rs + lr] = (int32_t)(v >= N ? v - N : v);
+                    if (jj >= j) {
+                        const uint32_t u = elim::mulmod((uint32_t)x, inv, M);
+                        P[jj * rs + npiv] = (int32_t)u;
+                        s_u[jj] = u;
+                        s_us[jj] = elim::shoup_pre(u, M);
+                    } else {
+                        P[jj * rs + npiv] = x;
                     }
                 }
-                npiv++;
                 __syncthreads();
+                npiv++;
+                const bool more = j + 1 < nbc && r0 + npiv < m;
+                if (warp == 0) {
+                    // column j+1 first, then its pivot
+                    unsigned long long best = 0;
+                    if (more) {
+                        for (int lr = npiv + lane; lr < R; lr += 32) {
+                            const uint32_t l = (uint32_t)P[j * rs + lr];
+                            uint32_t v = (uint32_t)P[(j + 1) * rs + lr];
+                            if (l) {
+                                v += elim::shoup_mul(N - l, s_u[j + 1], s_us[j + 1], N);
+                                v = v >= N ? v - N : v;
+                                P[(j + 1) * rs + lr] = (int32_t)v;
+                            }
+                            const unsigned long long key = pkey32(v, lr);
+                            best = key > best ? key : best;
+                        }
+                        decide_pivot(best, npiv, r0, j + 1, c0, l_cols, mont, S);
+                    }
+                } else {
+                    // columns j+2 .. of the panel, rows below the pivot
+                    const int nw = blockDim.x - 32;
+                    for (int lr = npiv + tid - 32; lr < R; lr += nw) {
+                        const uint32_t l = (uint32_t)P[j * rs + lr];
+                        if (!l) continue;
+                        const uint32_t nl = N - l;
+                        for (int jj = j + 2; jj < nbc; jj++) {
+                            const uint32_t v = (uint32_t)P[jj * rs + lr] + elim::shoup_mul(nl, s_u[jj], s_us[jj], N);
+                            P[jj * rs + lr] = (int32_t)(v >= N ? v - N : v);
+                        }
+                    }
+                }
+                __syncthreads();
+                if (!more) break;
             }
             const int zero_hit = S.zero_hit;
             const int stop = S.stop;
-            // ---- compose the panel's swaps into row moves; push the swap stack ----
+            // ---- compose the panel's swaps into row moves (local rows; `at` and the marks in Us) ----
             if (tid == 0) {
-                int rows_[PQ_MAX_MOVES], at[PQ_MAX_MOVES], nrows = 0;
-                auto slot = [&](int r) {
-                    for (int k = 0; k < nrows; k++)
-                        if (rows_[k] == r) return k;
-                    rows_[nrows] = r;
-                    at[nrows] = r;
-                    return nrows++;
-                };
+                int *at = Us;                       // at[lr]: local row whose content sits at lr
+                int *mk = Us + a.rcap;              // visited marks
                 for (int t = 0; t < npiv; t++) {
-                    const int r = r0 + t, pr = S.piv_prow[t];
-                    const int a1 = slot(r), a2 = slot(pr);
-                    const int x = at[a1];
-                    at[a1] = at[a2];
-                    at[a2] = x;
-                    if (pr != r) {
-                        I.row_swaps[2 * nr] = r + 1;
-                        I.row_swaps[2 * nr + 1] = pr + 1;
+                    const int pr = S.piv_prow[t] - r0;
+                    at[t] = t;
+                    at[pr] = pr;
+                    mk[t] = 0;
+                    mk[pr] = 0;
+                }
+                for (int t = 0; t < npiv; t++) {
+                    const int pr = S.piv_prow[t] - r0;
+                    const int x = at[t];
+                    at[t] = at[pr];
+                    at[pr] = x;
+                    if (pr != t) {
+                        row_swaps[2 * nr] = r0 + t + 1;
+                        row_swaps[2 * nr + 1] = r0 + pr + 1;
                         nr++;
                     }
                 }
                 int k = 0;
-                for (int q = 0; q < nrows; q++) {
-                    const int dst = rows_[q];
-                    const uint32_t sc = (dst >= r0 && dst < r0 + npiv) ? S.piv_inv[dst - r0] : 0u;
-                    if (at[q] == dst && sc == 0) continue;
-                    S.mv_dst[k] = dst;
-                    S.mv_src[k] = at[q];
-                    S.mv_scale[k] = sc;
-                    k++;
+                for (int q2 = 0; q2 < 2 * npiv; q2++) {
+                    {
+                        const int d = (q2 & 1) ? S.piv_prow[q2 >> 1] - r0 : (q2 >> 1);
+                        if (mk[d]) continue;
+                        mk[d] = 1;
+                        const uint32_t sc = d < npiv ? S.piv_inv[d] : 0u;
+                        if (at[d] == d && sc == 0) continue;
+                        S.mv_dst[k] = r0 + d;
+                        S.mv_src[k] = r0 + at[d];
+                        S.mv_scale[k] = sc;
+                        k++;
+                    }
                 }
                 S.nmv = k;
             }
             // ---- panel back to W: eliminated columns keep the pivot and above, zero below ----
             for (int idx = tid; idx < R * nbc; idx += blockDim.x) {
                 const int lr = idx / nbc, j = idx - lr * nbc;
-                I.W[(int64_t)(r0 + lr) * I.ldw + c0 + j] = (j < npiv && lr > j) ? 0 : P[j * rs + lr];
+                W[(int64_t)(r0 + lr) * ldw + c0 + j] = (j < npiv && lr > j) ? 0 : P[j * rs + lr];
             }
             // ---- L: this panel's columns (pivot, then the multipliers as swapped so far) ----
             for (int idx = tid; idx < R * npiv; idx += blockDim.x) {
-                const int t = idx / R, lr = idx - t * R;
-                if (lr >= t) I.LW[(int64_t)(r0 + lr) * I.ldlw + c0 + t] = lr == t ? (int32_t)S.piv_val[t] : P[t * rs + lr];
+                const int lr = idx / npiv, t = idx - lr * npiv;
+                if (lr >= t) LW[(int64_t)(r0 + lr) * ldlw + c0 + t] = lr == t ? (int32_t)S.piv_val[t] : P[t * rs + lr];
             }
             __syncthreads();
             if (npiv > 0) {
-                // the rows the panel's swaps moved, outside the panel: columns left of it (with the
-                // pivot-row scaling), trailing columns (moves only; their scaling comes with the
-                // substitution below), and L inside its swap width
+                // the rows the panel's swaps moved, outside the panel: trailing columns (moves
+                // only; their scaling comes with the substitution below), L inside its swap
+                // width, and -- only once a zero column has been skipped, the one way a column
+                // left of the panel holds non-zeros below its pivot row -- the left columns
+                // with the pivot-row scaling
                 int32_t *TW = a.tmp + (size_t)blockIdx.x * PQ_MAX_MOVES * (a.tmp_ldw + a.tmp_ldlw);
                 int32_t *TL = TW + (size_t)PQ_MAX_MOVES * a.tmp_ldw;
-                const int lsw_left = min(c0, I.lsw);
-                gather_moves(I.W, I.ldw, 0, c0, TW, a.tmp_ldw, S);
-                gather_moves(I.W, I.ldw, c0 + nbc, n, TW, a.tmp_ldw, S);
-                gather_moves(I.LW, I.ldlw, 0, lsw_left, TL, a.tmp_ldlw, S);
+                const int lsw_left = min(c0, lsw);
+                const int left = nc > 0 ? c0 : 0;
+                gather_moves(W, ldw, 0, left, TW, a.tmp_ldw, S);
+                gather_moves(W, ldw, c0 + nbc, n, TW, a.tmp_ldw, S);
+                gather_moves(LW, ldlw, 0, lsw_left, TL, a.tmp_ldlw, S);
                 __syncthreads();
-                scatter_moves(I.W, I.ldw, 0, c0, TW, a.tmp_ldw, S, true, I.M);
-                scatter_moves(I.W, I.ldw, c0 + nbc, n, TW, a.tmp_ldw, S, false, I.M);
-                scatter_moves(I.LW, I.ldlw, 0, lsw_left, TL, a.tmp_ldlw, S, false, I.M);
+                scatter_moves(W, ldw, 0, left, TW, a.tmp_ldw, S, true, M);
+                scatter_moves(W, ldw, c0 + nbc, n, TW, a.tmp_ldw, S, false, M);
+                scatter_moves(LW, ldlw, 0, lsw_left, TL, a.tmp_ldlw, S, false, M);
             }
             // L columns at or past the swap width must not see the swaps after their own step
             if (tid == 0) {
                 for (int t = 0; t < npiv; t++) {
                     const int c = c0 + t;
-                    if (c < I.lsw) continue;
-                    for (int s = npiv - 1; s > t; s--) {
-                        const int r = r0 + s, pr = S.piv_prow[s];
+                    if (c < lsw) continue;
+                    for (int s2 = npiv - 1; s2 > t; s2--) {
+                        const int r = r0 + s2, pr = S.piv_prow[s2];
                         if (pr == r) continue;
-                        int32_t *x = I.LW + (int64_t)r * I.ldlw + c;
-                        int32_t *y = I.LW + (int64_t)pr * I.ldlw + c;
+                        int32_t *x = LW + (int64_t)r * ldlw + c;
+                        int32_t *y = LW + (int64_t)pr * ldlw + c;
                         const int32_t tmp = *y;
                         *y = *x;
                         *x = tmp;
@@ -330,46 +435,60 @@ __global__ void __launch_bounds__(PQ_THREADS) k_pluq_batched(PQArgs a) {
             const int ct0 = c0 + nbc;
             for (int cb = ct0; npiv > 0 && cb < n; cb += PQ_CW) {
                 const int cw = min(PQ_CW, n - cb);
-                for (int idx = tid; idx < npiv * cw; idx += blockDim.x) {
-                    const int t = idx / cw, c = idx - t * cw;
-                    Us[t * PQ_CW + c] = I.W[(int64_t)(r0 + t) * I.ldw + cb + c];
+                for (int t = warp; t < npiv; t += PQ_THREADS / 32) {
+                    const int32_t *src = W + (int64_t)(r0 + t) * ldw + cb;
+                    for (int c = lane; c < cw; c += 32) Us[t * PQ_CW + c] = src[c];
                 }
                 __syncthreads();
                 if (tid < cw) {
                     for (int t = 0; t < npiv; t++) {
-                        uint64_t acc = (uint32_t)Us[t * PQ_CW + tid];
-                        for (int s = 0; s < t; s++) {
-                            const uint32_t l = (uint32_t)P[s * rs + t];
-                            acc += (uint64_t)(l ? N - l : 0u) * (uint32_t)Us[s * PQ_CW + tid];
+                        uint64_t acc0 = (uint32_t)Us[t * PQ_CW + tid], acc1 = 0, acc2 = 0, acc3 = 0;
+                        int s2 = 0;
+                        for (; s2 + 4 <= t; s2 += 4) {
+                            acc0 += (uint64_t)(N - (uint32_t)P[s2 * rs + t]) * (uint32_t)Us[s2 * PQ_CW + tid];
+                            acc1 += (uint64_t)(N - (uint32_t)P[(s2 + 1) * rs + t]) * (uint32_t)Us[(s2 + 1) * PQ_CW + tid];
+                            acc2 += (uint64_t)(N - (uint32_t)P[(s2 + 2) * rs + t]) * (uint32_t)Us[(s2 + 2) * PQ_CW + tid];
+                            acc3 += (uint64_t)(N - (uint32_t)P[(s2 + 3) * rs + t]) * (uint32_t)Us[(s2 + 3) * PQ_CW + tid];
                         }
-                        Us[t * PQ_CW + tid] = (int32_t)elim::mulmod(reduce_u64(acc, I.M), S.piv_inv[t], I.M);
+                        for (; s2 < t; s2++)
+                            acc0 += (uint64_t)(N - (uint32_t)P[s2 * rs + t]) * (uint32_t)Us[s2 * PQ_CW + tid];
+                        const uint64_t acc = acc0 + acc1 + acc2 + acc3;
+                        Us[t * PQ_CW + tid] = (int32_t)elim::mulmod(reduce_u64(acc, M), S.piv_inv[t], M);
                     }
                 }
                 __syncthreads();
-                for (int idx = tid; idx < npiv * cw; idx += blockDim.x) {
-                    const int t = idx / cw, c = idx - t * cw;
-                    I.W[(int64_t)(r0 + t) * I.ldw + cb + c] = Us[t * PQ_CW + c];
+                for (int t = warp; t < npiv; t += PQ_THREADS / 32) {
+                    int32_t *dst = W + (int64_t)(r0 + t) * ldw + cb;
+                    for (int c = lane; c < cw; c += 32) dst[c] = Us[t * PQ_CW + c];
                 }
-                // rows below the pivots: W += (N - l) u over 4 x 4 tiles per thread
-                const int rows = R - npiv;
-                const int trows = (rows + 3) >> 2, tcols = (cw + 3) >> 2;
+                // rows below the pivots: W += (N - l) u over 4 x 4 tiles per thread, the tile's
+                // W values fetched before the product loop; tiles start at a multiple of 4
+                // rows so the panel and pivot-row reads are 16-byte vectors
+                const int lr_base = npiv & ~3;
+                const int trows = (R - lr_base + 3) >> 2, tcols = (cw + 3) >> 2;
                 for (int tile = tid; tile < trows * tcols; tile += blockDim.x) {
                     const int tc = tile / trows, tr = tile - tc * trows;
-                    const int lr0 = npiv + 4 * tr, cc0 = 4 * tc;
+                    const int lr0 = lr_base + 4 * tr, cc0 = 4 * tc;
+                    uint32_t wv[4][4];
+#pragma unroll
+                    for (int x = 0; x < 4; x++) {
+                        const bool rok = lr0 + x >= npiv && lr0 + x < R;
+                        const int32_t *wrow = W + (int64_t)(r0 + lr0 + x) * ldw + cb + cc0;
+#pragma unroll
+                        for (int y = 0; y < 4; y++) wv[x][y] = (rok && cc0 + y < cw) ? (uint32_t)wrow[y] : 0u;
+                    }
                     uint64_t acc[4][4];
 #pragma unroll
                     for (int x = 0; x < 4; x++)
 #pragma unroll
-                        for (int y = 0; y < 4; y++) acc[x][y] = 0;
+                        for (int y = 0; y < 4; y++) acc[x][y] = wv[x][y];
+#pragma unroll 2
                     for (int t = 0; t < npiv; t++) {
-                        uint32_t lv[4], uv[4];
-#pragma unroll
-                        for (int x = 0; x < 4; x++) {
-                            const uint32_t l = (lr0 + x < R) ? (uint32_t)P[t * rs + lr0 + x] : 0u;
-                            lv[x] = l ? N - l : 0u;
-                        }
-#pragma unroll
-                        for (int y = 0; y < 4; y++) uv[y] = (cc0 + y < cw) ? (uint32_t)Us[t * PQ_CW + cc0 + y] : 0u;
+                        const int4 lq = *reinterpret_cast<const int4 *>(P + t * rs + lr0);
+                        const int4 uq = *reinterpret_cast<const int4 *>(Us + t * PQ_CW + cc0);
+                        const uint32_t lv[4] = {N - (uint32_t)lq.x, N - (uint32_t)lq.y, N - (uint32_t)lq.z,
+                                                N - (uint32_t)lq.w};
+                        const uint32_t uv[4] = {(uint32_t)uq.x, (uint32_t)uq.y, (uint32_t)uq.z, (uint32_t)uq.w};
 #pragma unroll
                         for (int x = 0; x < 4; x++)
 #pragma unroll
@@ -377,11 +496,11 @@ __global__ void __launch_bounds__(PQ_THREADS) k_pluq_batched(PQArgs a) {
                     }
 #pragma unroll
                     for (int x = 0; x < 4; x++) {
-                        if (lr0 + x < R) {
-                            int32_t *wrow = I.W + (int64_t)(r0 + lr0 + x) * I.ldw + cb + cc0;
+                        if (lr0 + x >= npiv && lr0 + x < R) {
+                            int32_t *wrow = W + (int64_t)(r0 + lr0 + x) * ldw + cb + cc0;
 #pragma unroll
                             for (int y = 0; y < 4; y++)
-                                if (cc0 + y < cw) wrow[y] = (int32_t)reduce_u64(acc[x][y] + (uint32_t)wrow[y], I.M);
+                                if (cc0 + y < cw) wrow[y] = (int32_t)reduce_u64(acc[x][y], M);
                         }
                     }
                 }
@@ -398,15 +517,15 @@ __global__ void __launch_bounds__(PQ_THREADS) k_pluq_batched(PQArgs a) {
                 const int last = n - 1;
                 if (col != last) {
                     for (int r = tid; r < m; r += blockDim.x) {
-                        int32_t *w = I.W + (int64_t)r * I.ldw;
+                        int32_t *w = W + (int64_t)r * ldw;
                         const int32_t x = w[col];
                         w[col] = w[last];
                         w[last] = x;
                     }
                 }
                 if (tid == 0) {
-                    I.col_swaps[2 * nc] = col + 1;
-                    I.col_swaps[2 * nc + 1] = last + 1;
+                    Ip->col_swaps[2 * nc] = col + 1;
+                    Ip->col_swaps[2 * nc + 1] = last + 1;
                 }
                 nc++;
                 col++;
@@ -414,13 +533,13 @@ __global__ void __launch_bounds__(PQ_THREADS) k_pluq_batched(PQArgs a) {
             __syncthreads();
         }
         __syncthreads();
-        to_colmajor(I.W, I.ldw, n, I.U, I.ldu, m, n, Us);
-        to_colmajor(I.LW, I.ldlw, I.lwc, I.L, I.ldl, m, I.l_cols, Us);
+        to_colmajor(W, ldw, n, Ip->U, Ip->ldu, m, n, pq_smem);
+        to_colmajor(LW, ldlw, Ip->lwc, Ip->L, Ip->ldl, m, l_cols, pq_smem);
         if (tid == 0) {
-            I.info[0] = nr;
-            I.info[1] = nc;
-            I.info[2] = row;
-            I.info[3] = status;
+            Ip->info[0] = nr;
+            Ip->info[1] = nc;
+            Ip->info[2] = row;
+            Ip->info[3] = status;
         }
         __syncthreads();
     }

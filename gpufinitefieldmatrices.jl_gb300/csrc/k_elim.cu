@@ -222,6 +222,8 @@ struct Work {
     int32_t *qlist;                              // [n] skipped columns
     __half *dA, *dB;                             // digit planes
     limb::Layout gl;
+    int plain = 0;                               // trailing products on the plain Float64 method
+    int64_t stripe = 1;                          // its stripe: find_max_stripe_ops(Float64, N)
 };
 
 static size_t al(size_t x) { return (x + 255) & ~size_t(255); }
@@ -295,6 +297,85 @@ struct Result {
     int rank = 0;
 };
 
+// The trailing products on the reference's plain Float64 arithmetic
+// (src/CuModMatrix/kernel_mul/stripe_mul.jl:175-244): exact FP64 products
+// summed in stripes of find_max_stripe_ops(Float64, N) and reduced mod N after
+// each stripe, 64 x 64 tiles of C per CTA, 4 x 4 per thread.  Operands as in
+// rowmajor_gemm; Y must not overlap C.  The comparison leg of the limb GEMM.
+__device__ __forceinline__ double plain_red(double x, double n, double inv) {
+    const double q = floor(x * inv);
+    double r = fma(-q, n, x);
+    if (r < 0.0) r += n;
+    if (r >= n) r -= n;
+    return r;
+}
+
+template <bool SUB>
+__global__ void __launch_bounds__(256) k_plain_rowmajor(int32_t *__restrict__ C, int64_t ldc,
+                                                        const int32_t *__restrict__ X, int64_t ldx,
+                                                        const int32_t *__restrict__ Y, int64_t ldy, int rows, int cols,
+                                                        int k, double Nd, double inv, int64_t stripe) {
+    __shared__ double Xs[16][65];
+    __shared__ double Ys[16][65];
+    const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+    const int r0 = blockIdx.y * 64, c0 = blockIdx.x * 64;
+    double acc[4][4];
+#pragma unroll
+    for (int i = 0; i < 4; i++)
+#pragma unroll
+        for (int j = 0; j < 4; j++) acc[i][j] = 0.0;
+    int64_t cnt = 0;
+    for (int k0 = 0; k0 < k; k0 += 16) {
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            const int e = tid + 256 * q;
+            const int r = e >> 4, kk = e & 15;
+            Xs[kk][r] = (r0 + r < rows && k0 + kk < k) ? (double)X[(int64_t)(r0 + r) * ldx + k0 + kk] : 0.0;
+            const int kk2 = e >> 6, c = e & 63;
+            Ys[kk2][c] = (k0 + kk2 < k && c0 + c < cols) ? (double)Y[(int64_t)(k0 + kk2) * ldy + c0 + c] : 0.0;
+        }
+        __syncthreads();
+        const int kmax = min(16, k - k0);
+        for (int kk = 0; kk < kmax; kk++) {
+            double xv[4], yv[4];
+#pragma unroll
+            for (int i = 0; i < 4; i++) xv[i] = Xs[kk][ty + 16 * i];
+#pragma unroll
+            for (int j = 0; j < 4; j++) yv[j] = Ys[kk][tx + 16 * j];
+#pragma unroll
+            for (int i = 0; i < 4; i++)
+#pragma unroll
+                for (int j = 0; j < 4; j++) acc[i][j] = fma(xv[i], yv[j], acc[i][j]);
+            if (++cnt == stripe) {
+#pragma unroll
+                for (int i = 0; i < 4; i++)
+#pragma unroll
+                    for (int j = 0; j < 4; j++) acc[i][j] = plain_red(acc[i][j], Nd, inv);
+                cnt = 0;
+            }
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        const int r = r0 + ty + 16 * i;
+        if (r >= rows) continue;
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            const int c = c0 + tx + 16 * j;
+            if (c >= cols) continue;
+            const double v = plain_red(acc[i][j], Nd, inv);
+            int32_t *cp = C + (int64_t)r * ldc + c;
+            if (SUB) {
+                double d = (double)*cp - v;
+                *cp = (int32_t)(d < 0.0 ? d + Nd : d);
+            } else {
+                *cp = (int32_t)v;
+            }
+        }
+    }
+}
+
 // Row-major products on the limb GEMM:
 // C (rows x cols, row-major, ldc) (-)= X (rows x k, row-major, ldx) * Y (k x cols, row-major, ldy),
 // epi = limb::EPI_SUB_I32 (C -= XY) or limb::EPI_STORE_I32 (C = XY; C may overlap Y, which is
@@ -303,6 +384,22 @@ static int rowmajor_gemm(Work &w, int64_t N, int32_t *C, int64_t ldc, const int3
                          const int32_t *Y, int64_t ldy, int64_t rows, int64_t cols, int64_t k, int epi,
                          cudaStream_t s) {
     if (rows <= 0 || cols <= 0 || k <= 0) return GFFM_OK;
+    if (w.plain) {
+        // Y may overlap C (U12 = L11^-1 P A12 in place): copy it out first
+        int32_t *Yc = reinterpret_cast<int32_t *>(w.dA);
+        GFFM_CUDA(cudaMemcpy2DAsync(Yc, (size_t)cols * 4, Y, (size_t)ldy * 4, (size_t)cols * 4, (size_t)k,
+                                    cudaMemcpyDeviceToDevice, s));
+        dim3 grid((unsigned)((cols + 63) / 64), (unsigned)((rows + 63) / 64));
+        const double Nd = (double)N;
+        if (epi == limb::EPI_SUB_I32)
+            k_plain_rowmajor<true><<<grid, 256, 0, s>>>(C, ldc, X, ldx, Yc, cols, (int)rows, (int)cols, (int)k, Nd,
+                                                         1.0 / Nd, w.stripe);
+        else
+            k_plain_rowmajor<false><<<grid, 256, 0, s>>>(C, ldc, X, ldx, Yc, cols, (int)rows, (int)cols, (int)k, Nd,
+                                                          1.0 / Nd, w.stripe);
+        GFFM_LAUNCH_CHECK("k_plain_rowmajor");
+        return GFFM_OK;
+    }
     // column-major view: C^T (cols x rows) -= Y^T (cols x k) * X^T (k x rows)
     limb::Layout g = limb::layout(cols, rows, k, N);
     int st = limb::split_a<int32_t>(Y, ldy, cols, k, w.dA, g, N, s);
@@ -325,7 +422,6 @@ static int permute_rows(Work &w, const PermArgs &perm, int c_lo, int c_hi, cudaS
     return GFFM_OK;
 }
 
-// deterministic Miller-Rabin for 32-bit n (bases 2, 7, 61)
 static int run_panel(Work &w, int m, int n, int R0, int C0, int nbw, const ModP &M, int lcols_check,
                      cudaStream_t s, int h_res[2], std::vector<int32_t> &h_prow, std::vector<int32_t> &h_pv) {
     using namespace gffm;
@@ -571,7 +667,8 @@ static int extract_l(Work &w, int64_t m, int64_t lcols, const Result &res, int m
 template <typename T>
 int pluq(int64_t m, int64_t n, const T *A, int64_t lda, T *U, int64_t ldu, T *L, int64_t ldl, int64_t lcols,
          int64_t N, int64_t *row_swaps, int64_t *n_row_swaps, int64_t *col_swaps, int64_t *n_col_swaps,
-         int64_t *rank, void *ws, size_t ws_bytes, gffm_stream_t stream, int mode, int64_t *perm) {
+         int64_t *rank, void *ws, size_t ws_bytes, gffm_stream_t stream, int mode, int64_t *perm,
+         bool plain = false) {
     using namespace gffm;
     int st = check_common(m, n, lda, N);
     if (st) return st;
@@ -602,6 +699,12 @@ int pluq(int64_t m, int64_t n, const T *A, int64_t lda, T *U, int64_t ldu, T *L,
     if (st) return st;
     Work w;
     bind_ws(scr.ptr, m, n, std::max<int64_t>(lcols, 1), &w);
+    w.plain = plain ? 1 : 0;
+    if (plain) {
+        // find_max_stripe_ops(Float64, N) = floor((2^53 - 1) / (N - 1)^2) - 1 (stripe_mul.jl:13-27)
+        const unsigned __int128 den = (unsigned __int128)(N - 1) * (unsigned __int128)(N - 1);
+        w.stripe = std::max<int64_t>(1, (int64_t)((((unsigned __int128)1 << 53) - 1) / den) - 1);
+    }
     st = load<T>(w, A, lda, m, n, N, s);
     if (st) return st;
     Result res;
@@ -680,6 +783,15 @@ int gffm_pluq_f64(int64_t m, int64_t n, const double *A, int64_t lda, double *U,
     if (!L) return gffm::set_error(GFFM_ERR_ARG, "L is NULL");
     return elim::pluq<double>(m, n, A, lda, U, ldu, L, ldl, l_cols, N, row_swaps, n_row_swaps, col_swaps, n_col_swaps,
                               rank, ws, ws_bytes, s, elim::MODE_PLUQ, nullptr);
+}
+
+int gffm_pluq_plain_f64(int64_t m, int64_t n, const double *A, int64_t lda, double *U, int64_t ldu, double *L,
+                        int64_t ldl, int64_t l_cols, int64_t N, int64_t *row_swaps, int64_t *n_row_swaps,
+                        int64_t *col_swaps, int64_t *n_col_swaps, int64_t *rank, void *ws, size_t ws_bytes,
+                        gffm_stream_t s) {
+    if (!L) return gffm::set_error(GFFM_ERR_ARG, "L is NULL");
+    return elim::pluq<double>(m, n, A, lda, U, ldu, L, ldl, l_cols, N, row_swaps, n_row_swaps, col_swaps, n_col_swaps,
+                              rank, ws, ws_bytes, s, elim::MODE_PLUQ, nullptr, true);
 }
 
 int gffm_pluq_f32(int64_t m, int64_t n, const float *A, int64_t lda, float *U, int64_t ldu, float *L, int64_t ldl,

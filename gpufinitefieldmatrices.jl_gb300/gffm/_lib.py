@@ -34,6 +34,8 @@ SIGNATURES = {
     "gffm_matmul_limb_f32": (_INT, [_I64, _I64, _I64, _P, _I64, _P, _I64, _P, _I64, _I64, _P, _SZ, _P]),
     "gffm_elim_workspace_size": (_INT, [_I64, _I64, _I64, _PSZ]),
     "gffm_pluq_f64": (_INT, [_I64, _I64, _P, _I64, _P, _I64, _P, _I64, _I64, _I64, _P, _P, _P, _P, _P, _P, _SZ, _P]),
+    "gffm_pluq_plain_f64": (_INT, [_I64, _I64, _P, _I64, _P, _I64, _P, _I64, _I64, _I64, _P, _P, _P, _P, _P, _P, _SZ,
+                                   _P]),
     "gffm_pluq_f32": (_INT, [_I64, _I64, _P, _I64, _P, _I64, _P, _I64, _I64, _I64, _P, _P, _P, _P, _P, _P, _SZ, _P]),
     "gffm_lu_f64": (_INT, [_I64, _I64, _P, _I64, _P, _I64, _P, _I64, _I64, _P, _P, _P, _SZ, _P]),
     "gffm_lu_f32": (_INT, [_I64, _I64, _P, _I64, _P, _I64, _P, _I64, _I64, _P, _P, _P, _SZ, _P]),

@@ -21,8 +21,18 @@ def _swaps_buf(P):
     return arr, arr.ctypes.data_as(ctypes.c_void_p), arr.shape[0]
 
 
-def pluq_gpu_kernel(A, debug=False):
-    """pluq_gpu_kernel(A) -> (U, L, Perm_rows, Perm_cols) (pluq_kernels.jl:46-157)."""
+def pluq_gpu_kernel(A, debug=False, method="limb"):
+    """pluq_gpu_kernel(A) -> (U, L, Perm_rows, Perm_cols) (pluq_kernels.jl:46-157).
+
+    method="plain" runs the trailing products on the reference's plain Float64
+    arithmetic instead of the limb tensor-core GEMM (Float64 storage only)."""
+    if method not in ("limb", "plain"):
+        raise ValueError("method must be 'limb' or 'plain'")
+    entry = "gffm_pluq_" + _sfx(A.dtype)
+    if method == "plain":
+        if A.dtype != torch.float64:
+            raise TypeError("the plain form takes Float64 storage")
+        entry = "gffm_pluq_plain_f64"
     rows, cols = A.data.shape[1] - TILE_WIDTH, A.data.shape[0] - TILE_WIDTH   # size(A.data) .- 32 (:82-84)
     U = CuModArray(torch.zeros_like(A.data), (rows, cols), A.N)
     L = CuModArray(torch.zeros((rows + TILE_WIDTH, rows + TILE_WIDTH), dtype=A.dtype, device=A.data.device),
@@ -30,7 +40,7 @@ def pluq_gpu_kernel(A, debug=False):
     rs = np.zeros((max(rows, 1), 2), dtype=np.int64)
     cs = np.zeros((max(cols, 1), 2), dtype=np.int64)
     nr, nc, rk = ctypes.c_int64(0), ctypes.c_int64(0), ctypes.c_int64(0)
-    call("gffm_pluq_" + _sfx(A.dtype), rows, cols, _ptr(A.data), A.ld, _ptr(U.data), U.ld, _ptr(L.data), L.ld,
+    call(entry, rows, cols, _ptr(A.data), A.ld, _ptr(U.data), U.ld, _ptr(L.data), L.ld,
          rows + TILE_WIDTH, A.N, rs.ctypes.data_as(ctypes.c_void_p), ctypes.byref(nr),
          cs.ctypes.data_as(ctypes.c_void_p), ctypes.byref(nc), ctypes.byref(rk), None, 0, _stream())
     Prows = [tuple(int(v) for v in rs[i]) for i in range(nr.value)]
@@ -140,9 +150,10 @@ def perm_array_to_matrix(perm, N, new_size, perm_stack=False, elem_type=torch.fl
 
 
 # -- benchmark helper used by bench.py -----------------------------------------
-def bench_pluq(size, stream_ptr, dev, reps=2):
+def bench_pluq(size, stream_ptr, dev, reps=2, method="limb", warmup=1):
     """Time pluq on a full-rank size x size matrix mod 67108859 (seeded uniform residues)
-    through the C ABI; returns a dict for the benchmark line."""
+    through the C ABI; returns a dict for the benchmark line.  method "plain" times the
+    plain Float64 trailing products."""
     import time
     p = 67108859
     if size is None or size < 0:
@@ -160,12 +171,15 @@ def bench_pluq(size, stream_ptr, dev, reps=2):
     cs = np.zeros((size, 2), dtype=np.int64)
     nr, nc, rk = ctypes.c_int64(0), ctypes.c_int64(0), ctypes.c_int64(0)
 
+    entry = "gffm_pluq_f64" if method == "limb" else "gffm_pluq_plain_f64"
+
     def run():
-        call("gffm_pluq_f64", size, size, _ptr(A.data), A.ld, _ptr(U.data), U.ld, _ptr(L.data), L.ld, size + 32, p,
+        call(entry, size, size, _ptr(A.data), A.ld, _ptr(U.data), U.ld, _ptr(L.data), L.ld, size + 32, p,
              rs.ctypes.data_as(ctypes.c_void_p), ctypes.byref(nr), cs.ctypes.data_as(ctypes.c_void_p),
              ctypes.byref(nc), ctypes.byref(rk), ctypes.c_void_p(buf.data_ptr()), ws.value, stream_ptr)
 
-    run()
+    for _ in range(warmup):
+        run()
     torch.cuda.synchronize()
     times = []
     for _ in range(reps):
@@ -175,5 +189,5 @@ def bench_pluq(size, stream_ptr, dev, reps=2):
         times.append(time.perf_counter() - t0)
     best = min(times)
     ops = 2.0 / 3.0 * size ** 3
-    return {"size": size, "modulus": p, "seconds": round(best, 4), "rank": rk.value,
+    return {"size": size, "modulus": p, "method": method, "seconds": round(best, 4), "rank": rk.value,
             "gops": round(ops / best / 1e9, 1), "ops": "2/3 n^3 modular multiply-adds"}

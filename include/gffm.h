@@ -177,6 +177,15 @@ GFFM_API int gffm_pluq_f32(int64_t m, int64_t n, const float *A, int64_t lda, fl
                            int64_t *col_swaps, int64_t *n_col_swaps, int64_t *rank, void *workspace,
                            size_t workspace_bytes, gffm_stream_t stream);
 
+/* The same factorization with the trailing products on the reference's plain
+ * Float64 arithmetic (stripe_mul.jl:175-244: exact FP64 products summed in
+ * stripes of find_max_stripe_ops(Float64, N), reduced after each stripe)
+ * instead of the limb tensor-core GEMM: the comparison leg of the two forms. */
+GFFM_API int gffm_pluq_plain_f64(int64_t m, int64_t n, const double *A, int64_t lda, double *U, int64_t ldu,
+                                 double *L, int64_t ldl, int64_t l_cols, int64_t N, int64_t *row_swaps,
+                                 int64_t *n_row_swaps, int64_t *col_swaps, int64_t *n_col_swaps, int64_t *rank,
+                                 void *workspace, size_t workspace_bytes, gffm_stream_t stream);
+
 /* lu_gpu_type(A) -> (U, L, Perm) (intended API, test/Experiments/rref_gpu_type.jl:60-103):
  * the same pivot rule without column swaps -- a zero column is skipped and
  * L's column index is the pivot count.  L is m x m; perm (host, m int64)
