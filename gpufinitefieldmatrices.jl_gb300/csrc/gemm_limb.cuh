@@ -5,6 +5,10 @@
 //     c = sum_{i<L} d_i 2^(7i),   d_i in [-64, 63],
 // each digit held exactly in fp16.  For A (m x k) and B (k x n):
 //     A*B = sum_s 2^(7s) C_s,   C_s = sum_{i+j=s} A_i B_j,   s = 0 .. 2L-2.
+// A product may instead use base-2^8 digits in [-128, 127] (fewer digits for
+// some moduli; |d_i d_j| <= 2^14, so chunks of 1024/L values of k, and the
+// weights below become 2^(8s) mod N): the kernels below do not depend on the
+// digit width, only the split and the host-side chunk and weights do.
 //
 // Tensor-core mapping.  The L digit tiles of B for one 64-column output tile
 // are stacked along N into one operand B' = [B_0; B_1; ...; B_{L-1}] (64L
@@ -63,7 +67,7 @@ struct Params {
     int64_t N;
     uint64_t minv;         // floor((2^64-1)/N)
     int64_t bias;          // multiple of N, >= 2^60
-    int32_t W[MAX_SHIFTS]; // 2^(7s) mod N
+    int32_t W[MAX_SHIFTS]; // 2^(bits*s) mod N
     void *C;
     int64_t ldc;
     const double *X, *Y;   // EPI_KSUB_F64 subtrahends
@@ -379,20 +383,22 @@ __device__ __forceinline__ int32_t split_value(T v, T v2, const ModN &M) {
     return (2 * (int64_t)r > M.n) ? r - (int32_t)M.n : r;
 }
 
+// L balanced base-2^bits digits of c (bits = 7: digits in [-64, 63]; bits = 8: [-128, 127])
 template <int L>
-__device__ __forceinline__ void digits(int32_t c, __half (&d)[L]) {
+__device__ __forceinline__ void digits(int32_t c, __half (&d)[L], int bits = 7) {
+    const int32_t half = 1 << (bits - 1), mask = (1 << bits) - 1;
 #pragma unroll
     for (int i = 0; i < L; i++) {
-        int32_t di = ((c + 64) & 127) - 64;
+        int32_t di = ((c + half) & mask) - half;
         d[i] = __int2half_rn(di);
-        c = (c - di) >> 7;
+        c = (c - di) >> bits;
     }
 }
 
 // A (m x k, column-major, lda) -> digit planes D[l][r][kk] (K-major, Mpad x Kpad per plane)
 template <typename T, int L, int MODE>
 __global__ void __launch_bounds__(256) k_split_a(const T *__restrict__ A, const T *__restrict__ A2, int64_t lda, int m,
-                                                 int k, __half *__restrict__ D, int Mpad, int Kpad, ModN M) {
+                                                 int k, __half *__restrict__ D, int Mpad, int Kpad, ModN M, int bits) {
     __shared__ int32_t tile[32][33];
     const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
     const int64_t r0 = (int64_t)blockIdx.y * 32, k0 = (int64_t)blockIdx.x * 32;
@@ -412,7 +418,7 @@ __global__ void __launch_bounds__(256) k_split_a(const T *__restrict__ A, const 
     for (int i = 0; i < 4; i++) {
         int64_t r = r0 + ty + 8 * i, kk = k0 + tx;
         __half d[L];
-        digits<L>(tile[tx][ty + 8 * i], d);
+        digits<L>(tile[tx][ty + 8 * i], d, bits);
 #pragma unroll
         for (int l = 0; l < L; l++) D[l * plane + (size_t)r * Kpad + kk] = d[l];
     }
@@ -421,7 +427,7 @@ __global__ void __launch_bounds__(256) k_split_a(const T *__restrict__ A, const 
 // B (k x n, column-major, ldb) -> digit planes D[l][c][kk] (K-major, Npad x Kpad per plane)
 template <typename T, int L, int MODE>
 __global__ void __launch_bounds__(256) k_split_b(const T *__restrict__ B, const T *__restrict__ B2, int64_t ldb, int k,
-                                                 int n, __half *__restrict__ D, int Npad, int Kpad, ModN M) {
+                                                 int n, __half *__restrict__ D, int Npad, int Kpad, ModN M, int bits) {
     const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;  // pair index
     const int64_t pairs_per_col = Kpad / 2;
     const int64_t total = pairs_per_col * Npad;
@@ -432,8 +438,8 @@ __global__ void __launch_bounds__(256) k_split_b(const T *__restrict__ B, const 
     int32_t v0 = (c < n && kk < k) ? split_value<MODE>(B[off], MODE == SPLIT_SUM ? B2[off] : T(0), M) : 0;
     int32_t v1 = (c < n && kk + 1 < k) ? split_value<MODE>(B[off + 1], MODE == SPLIT_SUM ? B2[off + 1] : T(0), M) : 0;
     __half d0[L], d1[L];
-    digits<L>(v0, d0);
-    digits<L>(v1, d1);
+    digits<L>(v0, d0, bits);
+    digits<L>(v1, d1, bits);
     const size_t plane = (size_t)Npad * Kpad;
 #pragma unroll
     for (int l = 0; l < L; l++)

@@ -44,6 +44,7 @@ struct SplitJob {
     int64_t N;
     uint64_t minv;
     int64_t blk0;                // first block of this job
+    int bits, pad_;              // digit width (7 or 8)
 };
 
 constexpr int G_STAGES = 2;
@@ -71,7 +72,7 @@ __device__ __forceinline__ void split_a_tile(const SplitJob &J, int64_t local, i
     for (int i = 0; i < 4; i++) {
         const int64_t r = r0 + ty + 8 * i, kk = k0 + tx;
         __half d[L];
-        digits<L>(tile[tx][ty + 8 * i], d);
+        digits<L>(tile[tx][ty + 8 * i], d, J.bits);
 #pragma unroll
         for (int l = 0; l < L; l++) J.dst[l * plane + (size_t)r * J.kpad + kk] = d[l];
     }
@@ -89,8 +90,8 @@ __device__ __forceinline__ void split_b_pairs(const SplitJob &J, int64_t local) 
     const int32_t v0 = (c < n && kk < k) ? split_value<SPLIT_CENTRED>(J.src[kk + c * J.ld], 0.0, M) : 0;
     const int32_t v1 = (c < n && kk + 1 < k) ? split_value<SPLIT_CENTRED>(J.src[kk + 1 + c * J.ld], 0.0, M) : 0;
     __half d0[L], d1[L];
-    digits<L>(v0, d0);
-    digits<L>(v1, d1);
+    digits<L>(v0, d0, J.bits);
+    digits<L>(v1, d1, J.bits);
     const size_t plane = (size_t)J.prow * J.kpad;
 #pragma unroll
     for (int l = 0; l < L; l++)
@@ -498,6 +499,8 @@ int create(const gffm_batch_desc *descs, int64_t count, const gffm_batch_tuning 
     if (tu.pluq_panel != 0 && tu.pluq_panel != 8 && tu.pluq_panel != 16 && tu.pluq_panel != 32)
         return set_error(GFFM_ERR_ARG, "pluq_panel must be 0, 8, 16 or 32");
     if (tu.gemm_ctas < 0 || tu.pluq_ctas < 0) return set_error(GFFM_ERR_ARG, "negative grid size");
+    if (tu.digit_bits != 0 && tu.digit_bits != 7 && tu.digit_bits != 8)
+        return set_error(GFFM_ERR_ARG, "digit_bits must be 0, 7 or 8");
 
     auto *p = new gffm_batch_plan_s();
     PLAN_CUDA(cudaGetDevice(&p->device));
@@ -528,7 +531,10 @@ int create(const gffm_batch_desc *descs, int64_t count, const gffm_batch_tuning 
     for (int q = 0; q < p->n_mm; q++) {
         const gffm_batch_desc &d = descs[mm_ids[q]];
         MMInst &I = mm[q];
-        lay[q] = limb::layout(d.m, d.n, d.k, d.N);
+        // digit width: the tuning's, else whichever needs fewer digits (7 on a tie)
+        const int bits = tu.digit_bits ? tu.digit_bits
+                                       : (limb::limbs_for_bits(d.N, 8) < limb::limbs_for(d.N) ? 8 : 7);
+        lay[q] = limb::layout_bits(d.m, d.n, d.k, d.N, bits);
         const limb::Layout &g = lay[q];
         I.m = (int)d.m;
         I.n = (int)d.n;
@@ -536,7 +542,7 @@ int create(const gffm_batch_desc *descs, int64_t count, const gffm_batch_tuning 
         I.kblocks = (int)(d.k > 0 ? g.Kpad / BK : 0);
         I.mtiles = (int)((d.m + BM - 1) / BM);
         I.ntiles = (int)((d.n + BN - 1) / BN);
-        I.chunk_kb = 64 / g.L;
+        I.chunk_kb = limb::chunk_kblocks(g);
         I.Mpad = (int)g.Mpad;
         I.Npad = (int)g.Npad;
         I.pad_ = 0;
@@ -546,7 +552,7 @@ int create(const gffm_batch_desc *descs, int64_t count, const gffm_batch_tuning 
         int64_t w = 1 % d.N;
         for (int sft = 0; sft < MAX_SHIFTS; sft++) {
             I.W[sft] = (int32_t)w;
-            w = (w * 128) % d.N;
+            w = (w * (g.bits == 8 ? 256 : 128)) % d.N;
         }
         I.C = d.C;
         I.ldc = d.ldc;
@@ -641,10 +647,12 @@ int create(const gffm_batch_desc *descs, int64_t count, const gffm_batch_tuning 
         __half *da = reinterpret_cast<__half *>(base + o_da[q]);
         __half *db = reinterpret_cast<__half *>(base + o_db[q]);
         if (mm[q].kblocks > 0) {
-            SplitJob ja{d.A, d.lda, da, (int)d.m, (int)d.k, (int)g.Mpad, (int)g.Kpad, g.L, 0, d.N, mm[q].minv, blk};
+            SplitJob ja{d.A, d.lda, da, (int)d.m, (int)d.k, (int)g.Mpad, (int)g.Kpad, g.L, 0, d.N, mm[q].minv, blk,
+                        g.bits, 0};
             blk += (g.Kpad / 32) * (g.Mpad / 32);
             jobs.push_back(ja);
-            SplitJob jb{d.B, d.ldb, db, (int)d.k, (int)d.n, (int)g.Npad, (int)g.Kpad, g.L, 1, d.N, mm[q].minv, blk};
+            SplitJob jb{d.B, d.ldb, db, (int)d.k, (int)d.n, (int)g.Npad, (int)g.Kpad, g.L, 1, d.N, mm[q].minv, blk,
+                        g.bits, 0};
             blk += ((g.Kpad / 2) * g.Npad + 255) / 256;
             jobs.push_back(jb);
         }

@@ -4,7 +4,9 @@
 #include "limb_host.h"
 
 #include <cudaTypedefs.h>
+#include <algorithm>
 #include <mutex>
+#include <vector>
 
 namespace limb {
 
@@ -52,6 +54,27 @@ int limbs_for(int64_t N) {
     return 4;
 }
 
+int limbs_for_bits(int64_t N, int bits) {
+    if (bits != 8) return limbs_for(N);
+    // largest centred residue floor(N/2) within 127 * (256^L - 1) / 255
+    if (N <= 255) return 1;
+    if (N <= 65279) return 2;
+    if (N <= 16711423) return 3;
+    return 4;
+}
+
+int chunk_kblocks(const Layout &g) {
+    // |d_i d_j| <= 2^(2 bits - 2) and at most L products per shift and k: the fp32 sums stay
+    // exact (<= 2^24) over 2^(26 - 2 bits) / L values of k
+    return g.bits == 8 ? std::max(1, 16 / g.L) : 64 / g.L;
+}
+
+Layout layout_bits(int64_t m, int64_t n, int64_t k, int64_t N, int bits) {
+    Layout g = layout_L(m, n, k, limbs_for_bits(N, bits));
+    g.bits = bits == 8 ? 8 : 7;
+    return g;
+}
+
 int raw_limbs_for(int64_t N) {
     // largest non-centred residue N - 1 must fit L balanced base-128 digits
     if (N <= 64) return 1;
@@ -91,10 +114,10 @@ static void launch_split_a(const T *A, const T *A2, int64_t lda, int64_t m, int6
     dim3 grid((unsigned)(g.Kpad / 32), (unsigned)(g.Mpad / 32));
     const int mm = (int)m, kk = (int)k, Mp = (int)g.Mpad, Kp = (int)g.Kpad;
     switch (g.L) {
-        case 1: k_split_a<T, 1, MODE><<<grid, 256, 0, s>>>(A, A2, lda, mm, kk, D, Mp, Kp, M); break;
-        case 2: k_split_a<T, 2, MODE><<<grid, 256, 0, s>>>(A, A2, lda, mm, kk, D, Mp, Kp, M); break;
-        case 3: k_split_a<T, 3, MODE><<<grid, 256, 0, s>>>(A, A2, lda, mm, kk, D, Mp, Kp, M); break;
-        default: k_split_a<T, 4, MODE><<<grid, 256, 0, s>>>(A, A2, lda, mm, kk, D, Mp, Kp, M); break;
+        case 1: k_split_a<T, 1, MODE><<<grid, 256, 0, s>>>(A, A2, lda, mm, kk, D, Mp, Kp, M, g.bits); break;
+        case 2: k_split_a<T, 2, MODE><<<grid, 256, 0, s>>>(A, A2, lda, mm, kk, D, Mp, Kp, M, g.bits); break;
+        case 3: k_split_a<T, 3, MODE><<<grid, 256, 0, s>>>(A, A2, lda, mm, kk, D, Mp, Kp, M, g.bits); break;
+        default: k_split_a<T, 4, MODE><<<grid, 256, 0, s>>>(A, A2, lda, mm, kk, D, Mp, Kp, M, g.bits); break;
     }
 }
 
@@ -105,16 +128,17 @@ static void launch_split_b(const T *B, const T *B2, int64_t ldb, int64_t k, int6
     unsigned blocks = (unsigned)((total + 255) / 256);
     const int kk = (int)k, nn = (int)n, Np = (int)g.Npad, Kp = (int)g.Kpad;
     switch (g.L) {
-        case 1: k_split_b<T, 1, MODE><<<blocks, 256, 0, s>>>(B, B2, ldb, kk, nn, D, Np, Kp, M); break;
-        case 2: k_split_b<T, 2, MODE><<<blocks, 256, 0, s>>>(B, B2, ldb, kk, nn, D, Np, Kp, M); break;
-        case 3: k_split_b<T, 3, MODE><<<blocks, 256, 0, s>>>(B, B2, ldb, kk, nn, D, Np, Kp, M); break;
-        default: k_split_b<T, 4, MODE><<<blocks, 256, 0, s>>>(B, B2, ldb, kk, nn, D, Np, Kp, M); break;
+        case 1: k_split_b<T, 1, MODE><<<blocks, 256, 0, s>>>(B, B2, ldb, kk, nn, D, Np, Kp, M, g.bits); break;
+        case 2: k_split_b<T, 2, MODE><<<blocks, 256, 0, s>>>(B, B2, ldb, kk, nn, D, Np, Kp, M, g.bits); break;
+        case 3: k_split_b<T, 3, MODE><<<blocks, 256, 0, s>>>(B, B2, ldb, kk, nn, D, Np, Kp, M, g.bits); break;
+        default: k_split_b<T, 4, MODE><<<blocks, 256, 0, s>>>(B, B2, ldb, kk, nn, D, Np, Kp, M, g.bits); break;
     }
 }
 
 // the raw and summed splits serve the Karatsuba products, which take Float64 digits only
-static int check_mode(int mode, bool is_double, const void *second) {
+static int check_mode(int mode, bool is_double, const void *second, int bits) {
     if (mode == SPLIT_CENTRED) return GFFM_OK;
+    if (bits != 7) return gffm::set_error(GFFM_ERR_UNSUPPORTED, "raw and summed digit splits use 7-bit digits");
     if (!is_double || (mode != SPLIT_RAW && mode != SPLIT_SUM))
         return gffm::set_error(GFFM_ERR_UNSUPPORTED, "digit split mode %d is not available for this element type", mode);
     if (mode == SPLIT_SUM && !second) return gffm::set_error(GFFM_ERR_ARG, "summed digit split without a second operand");
@@ -124,7 +148,7 @@ static int check_mode(int mode, bool is_double, const void *second) {
 template <typename T>
 int split_a(const T *A, int64_t lda, int64_t m, int64_t k, __half *D, const Layout &g, int64_t N, cudaStream_t s,
             int mode, const T *A2) {
-    int st = check_mode(mode, sizeof(T) == 8, A2);
+    int st = check_mode(mode, sizeof(T) == 8, A2, g.bits);
     if (st) return st;
     ModN M{N, ~uint64_t(0) / (uint64_t)N};
     if constexpr (sizeof(T) == 8) {
@@ -144,7 +168,7 @@ int split_a(const T *A, int64_t lda, int64_t m, int64_t k, __half *D, const Layo
 template <typename T>
 int split_b(const T *B, int64_t ldb, int64_t k, int64_t n, __half *D, const Layout &g, int64_t N, cudaStream_t s,
             int mode, const T *B2) {
-    int st = check_mode(mode, sizeof(T) == 8, B2);
+    int st = check_mode(mode, sizeof(T) == 8, B2, g.bits);
     if (st) return st;
     ModN M{N, ~uint64_t(0) / (uint64_t)N};
     if constexpr (sizeof(T) == 8) {
@@ -187,6 +211,8 @@ int gemm_digits(const Layout &g, const __half *Ad, const __half *Bd, int64_t m, 
     if (epi == EPI_KSUB_F64 && (!X || !Y)) return gffm::set_error(GFFM_ERR_ARG, "subtracting epilogue without X, Y");
     if (N < 2 || N >= (epi == EPI_EXACT_I64 ? (int64_t(1) << 52) : (int64_t(1) << 26)))
         return gffm::set_error(GFFM_ERR_MODULUS, "modulus %lld out of range for epilogue %d", (long long)N, epi);
+    if (epi == EPI_EXACT_I64 && g.bits != 7)
+        return gffm::set_error(GFFM_ERR_UNSUPPORTED, "the exact epilogue takes 7-bit digits");
     int st = get_encoder();
     if (st) return st;
     CUtensorMap ta, tb;
@@ -202,14 +228,14 @@ int gemm_digits(const Layout &g, const __half *Ad, const __half *Bd, int64_t m, 
     p.Npad = (int)g.Npad;
     p.mtiles = (int)((m + BM - 1) / BM);
     p.ntiles = (int)((n + BN - 1) / BN);
-    p.chunk_kb = 64 / g.L;
+    p.chunk_kb = chunk_kblocks(g);
     p.N = N;
     p.minv = ~uint64_t(0) / (uint64_t)N;
     p.bias = N * (((int64_t(1) << 60) + N - 1) / N);
     int64_t w = 1 % N;
     for (int sft = 0; sft < MAX_SHIFTS; sft++) {
         p.W[sft] = (int32_t)w;      // unused by EPI_EXACT_I64, whose N may exceed 32 bits
-        w = (int64_t)(((__int128)w * 128) % N);
+        w = (int64_t)(((__int128)w * (g.bits == 8 ? 256 : 128)) % N);
     }
     p.C = C;
     p.ldc = ldc;
@@ -247,13 +273,54 @@ template int split_b<int32_t>(const int32_t *, int64_t, int64_t, int64_t, __half
 
 }  // namespace limb
 
+namespace limb {
+
+// The process-wide tune table (the one piece of global mutable state: written by
+// gffm_tune_table_set, read by every limb product).
+static std::vector<gffm_tune_entry> g_tune;
+static std::mutex g_tune_mu;
+
+void tuned_for(int64_t m, int64_t n, int64_t k, int64_t N, int *bits, int *max_ctas) {
+    *bits = 7;
+    *max_ctas = 0;
+    const double work = (double)m * (double)n * (double)k;
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    for (const gffm_tune_entry &e : g_tune) {
+        if (N < e.N_lo || N > e.N_hi || work < e.work_lo || work > e.work_hi) continue;
+        *bits = e.tuning.digit_bits == 8 ? 8 : 7;
+        *max_ctas = e.tuning.max_ctas > 0 ? e.tuning.max_ctas : 0;
+        return;
+    }
+}
+
+}  // namespace limb
+
 namespace {
+
+int check_tuning(const gffm_limb_tuning *t) {
+    if (!t) return GFFM_OK;
+    if (t->digit_bits != 0 && t->digit_bits != 7 && t->digit_bits != 8)
+        return gffm::set_error(GFFM_ERR_ARG, "digit_bits must be 0, 7 or 8");
+    if (t->max_ctas < 0) return gffm::set_error(GFFM_ERR_ARG, "max_ctas must be >= 0");
+    return GFFM_OK;
+}
+
+// the digit width and grid of a product: an explicit tuning, else the tune table
+void pick(const gffm_limb_tuning *t, int64_t m, int64_t n, int64_t k, int64_t N, int *bits, int *ctas) {
+    limb::tuned_for(m, n, k, N, bits, ctas);
+    if (t) {
+        if (t->digit_bits) *bits = t->digit_bits;
+        *ctas = t->max_ctas;
+    }
+}
 
 template <typename T>
 int matmul_limb(int64_t m, int64_t n, int64_t k, const T *A, int64_t lda, const T *B, int64_t ldb, T *C, int64_t ldc,
-                int64_t N, void *ws, size_t ws_bytes, gffm_stream_t stream) {
+                int64_t N, void *ws, size_t ws_bytes, gffm_stream_t stream, const gffm_limb_tuning *tune = nullptr) {
     using namespace gffm;
-    int st = limb::check_args(m, n, k, lda, ldb, ldc, N);
+    int st = check_tuning(tune);
+    if (st) return st;
+    st = limb::check_args(m, n, k, lda, ldb, ldc, N);
     if (st) return st;
     if (m == 0 || n == 0) return GFFM_OK;
     if (!C || (k > 0 && (!A || !B))) return set_error(GFFM_ERR_ARG, "null data pointer");
@@ -265,7 +332,9 @@ int matmul_limb(int64_t m, int64_t n, int64_t k, const T *A, int64_t lda, const 
         GFFM_CUDA(cudaMemset2DAsync(C, (size_t)ldc * sizeof(T), 0, (size_t)m * sizeof(T), (size_t)n, s));
         return GFFM_OK;
     }
-    limb::Layout g = limb::layout(m, n, k, N);
+    int bits, ctas;
+    pick(tune, m, n, k, N, &bits, &ctas);
+    limb::Layout g = limb::layout_bits(m, n, k, N, bits);
     Scratch scr;
     st = scr.acquire(ws, ws_bytes, g.a_bytes + g.b_bytes, s);
     if (st) return st;
@@ -276,19 +345,53 @@ int matmul_limb(int64_t m, int64_t n, int64_t k, const T *A, int64_t lda, const 
     st = limb::split_b<T>(B, ldb, k, n, Bd, g, N, s);
     if (st) return st;
     return limb::gemm_digits(g, Ad, Bd, m, n, k, N, C, ldc,
-                             sizeof(T) == 8 ? limb::EPI_STORE_F64 : limb::EPI_STORE_F32, 0, s);
+                             sizeof(T) == 8 ? limb::EPI_STORE_F64 : limb::EPI_STORE_F32, ctas, s);
 }
 
 }  // namespace
 
 extern "C" {
 
-int gffm_matmul_limb_workspace_size(int64_t m, int64_t n, int64_t k, int64_t N, size_t *bytes) {
+int gffm_matmul_limb_tuned_workspace_size(int64_t m, int64_t n, int64_t k, int64_t N, const gffm_limb_tuning *tuning,
+                                          size_t *bytes) {
     if (!bytes) return gffm::set_error(GFFM_ERR_ARG, "bytes is NULL");
-    int st = limb::check_args(m, n, k, m > 1 ? m : 1, k > 1 ? k : 1, m > 1 ? m : 1, N);
+    int st = check_tuning(tuning);
     if (st) return st;
-    limb::Layout g = limb::layout(m, n, k, N);
+    st = limb::check_args(m, n, k, m > 1 ? m : 1, k > 1 ? k : 1, m > 1 ? m : 1, N);
+    if (st) return st;
+    int bits, ctas;
+    pick(tuning, m, n, k, N, &bits, &ctas);
+    limb::Layout g = limb::layout_bits(m, n, k, N, bits);
     *bytes = (m == 0 || n == 0 || k == 0) ? 0 : g.a_bytes + g.b_bytes;
+    return GFFM_OK;
+}
+
+int gffm_matmul_limb_workspace_size(int64_t m, int64_t n, int64_t k, int64_t N, size_t *bytes) {
+    return gffm_matmul_limb_tuned_workspace_size(m, n, k, N, nullptr, bytes);
+}
+
+int gffm_matmul_limb_tuned_f64(int64_t m, int64_t n, int64_t k, const double *A, int64_t lda, const double *B,
+                               int64_t ldb, double *C, int64_t ldc, int64_t N, const gffm_limb_tuning *tuning, void *ws,
+                               size_t ws_bytes, gffm_stream_t s) {
+    if (!tuning) return gffm::set_error(GFFM_ERR_ARG, "tuning is NULL");
+    return matmul_limb<double>(m, n, k, A, lda, B, ldb, C, ldc, N, ws, ws_bytes, s, tuning);
+}
+
+int gffm_tune_table_set(const gffm_tune_entry *entries, int64_t count) {
+    if (count < 0 || (count > 0 && !entries)) return gffm::set_error(GFFM_ERR_ARG, "bad tune table");
+    for (int64_t i = 0; i < count; i++) {
+        int st = check_tuning(&entries[i].tuning);
+        if (st) return st;
+    }
+    std::lock_guard<std::mutex> lk(limb::g_tune_mu);
+    limb::g_tune.assign(entries, entries + count);
+    return GFFM_OK;
+}
+
+int gffm_tune_table_size(int64_t *count) {
+    if (!count) return gffm::set_error(GFFM_ERR_ARG, "count is NULL");
+    std::lock_guard<std::mutex> lk(limb::g_tune_mu);
+    *count = (int64_t)limb::g_tune.size();
     return GFFM_OK;
 }
 

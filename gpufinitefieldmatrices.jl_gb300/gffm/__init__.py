@@ -10,7 +10,7 @@ from .cumod import (  # noqa: F401
     TILE_WIDTH, DEFAULT_TYPE, CuModArray, CuModMatrix, CuModVector, wrap, zeros, eye, rand, similar, copy,
     add_, sub_, elementwise_multiply_, scalar_add_, scalar_sub_, rscalar_sub_, scalar_mul_, negate_,
     mod_, mod_elements_, fill_, zero_, copy_, change_modulus, change_modulus_no_alloc_,
-    mul_, stripe_mul_, mat_mul_gpu_type, mat_mul_type_inplace_, find_max_stripe_ops,
+    mul_, stripe_mul_, mat_mul_gpu_type, mat_mul_type_inplace_, find_max_stripe_ops, limbs_for, LimbTuning,
     CuModArraySizeMismatchException, CuModArrayModulusMismatchException, CuModMatrixNotSquareException,
     CuModMatrixModulusNotPrimeException,
 )
@@ -44,3 +44,4 @@ negate_ = _dispatch("negate_")
 zero_ = _dispatch("zero_")
 copy_ = _dispatch("copy_")
 from .batched import BatchPlan, Tuning as BatchTuning, batched_plan  # noqa: F401,E402
+from . import autotune  # noqa: F401,E402

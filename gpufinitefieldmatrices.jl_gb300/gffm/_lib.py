@@ -69,6 +69,10 @@ SIGNATURES.update({
     "gffm_karatsuba_scalar_mul_f64": (_INT, [_P, _P, _P, _P, _I64, _I64, _I64, _I64, _P]),
     "gffm_karatsuba_from_values_f64": (_INT, [_P, _P, _P, _I64, _I64, _I64, _P]),
     "gffm_karatsuba_to_values_f64": (_INT, [_P, _P, _P, _I64, _I64, _I64, _P]),
+    "gffm_tune_table_set": (_INT, [_P, _I64]),
+    "gffm_tune_table_size": (_INT, [_PI64]),
+    "gffm_matmul_limb_tuned_workspace_size": (_INT, [_I64, _I64, _I64, _I64, _P, _PSZ]),
+    "gffm_matmul_limb_tuned_f64": (_INT, [_I64, _I64, _I64, _P, _I64, _P, _I64, _P, _I64, _I64, _P, _P, _SZ, _P]),
     "gffm_batched_plan_create": (_INT, [_P, _I64, _P, _P]),
     "gffm_batched_plan_info": (_INT, [_P, _PI64]),
     "gffm_batched_run": (_INT, [_P, _P]),
@@ -108,6 +112,9 @@ def load(path=None):
         fn.restype = res
         fn.argtypes = args
     _lib = L
+    # install the shipped autotune table (gffm/tuning.json) as the library's tune table
+    from . import autotune
+    autotune.apply()
     return L
 
 

@@ -30,7 +30,7 @@ class _Desc(ctypes.Structure):
 class Tuning(ctypes.Structure):
     """gffm_batch_tuning: 0 in a field picks the library default."""
     _fields_ = [("pluq_panel", ctypes.c_int32), ("gemm_ctas", ctypes.c_int32), ("pluq_ctas", ctypes.c_int32),
-                ("overlap", ctypes.c_int32)]
+                ("overlap", ctypes.c_int32), ("digit_bits", ctypes.c_int32)]
 
 
 class BatchPlan:
@@ -79,6 +79,13 @@ class BatchPlan:
             else:
                 raise ValueError("instance kind must be 'matmul' or 'pluq'")
         self._plan = ctypes.c_void_p()
+        if isinstance(tuning, str):
+            if tuning != "auto":
+                raise ValueError("tuning must be a Tuning, None or 'auto'")
+            from . import autotune
+            best = autotune.lookup_batched(instances)
+            tuning = None if best is None else Tuning(best["pluq_panel"], best["gemm_ctas"], best["pluq_ctas"],
+                                                       best["overlap"], best.get("digit_bits", 0))
         tu = tuning if tuning is not None else Tuning()
         call("gffm_batched_plan_create", ctypes.cast(descs, ctypes.c_void_p), len(instances), ctypes.byref(tu),
              ctypes.byref(self._plan))

@@ -366,7 +366,22 @@ def change_modulus_no_alloc_(A, new_N):
 LIMB_MAX_N = 2 ** 26
 
 
-def _gemm(C, A, B, N, method, stripe=0):
+def limbs_for(N, bits=7):
+    """Digits per residue of the limb GEMM with balanced base-2^bits digits
+    (csrc/k_gemm_limb.cu: limbs_for, limbs_for_bits)."""
+    thresholds = (255, 65279, 16711423) if bits == 8 else (127, 16255, 2080639)
+    for L, t in enumerate(thresholds, 1):
+        if N <= t:
+            return L
+    return 4
+
+
+class LimbTuning(ctypes.Structure):
+    """gffm_limb_tuning: digit width (0 = the tune table's choice, 7 or 8) and grid (0 = one CTA per SM)."""
+    _fields_ = [("digit_bits", ctypes.c_int32), ("max_ctas", ctypes.c_int32)]
+
+
+def _gemm(C, A, B, N, method, stripe=0, tuning=None):
     if A.dtype != B.dtype or A.dtype != C.dtype:
         raise TypeError("Mismatched element types in matmul")
     m, k = A.rows(), A.cols()
@@ -374,7 +389,12 @@ def _gemm(C, A, B, N, method, stripe=0):
     sfx = _sfx(C.dtype)
     if method == "auto":
         method = "limb" if 2 <= N < LIMB_MAX_N else "plain"
-    if method == "limb":
+    if method == "limb" and tuning is not None:
+        if C.dtype != torch.float64:
+            raise TypeError("an explicit limb tuning takes Float64 storage")
+        call("gffm_matmul_limb_tuned_f64", m, n, k, _ptr(A.data), A.ld, _ptr(B.data), B.ld, _ptr(C.data), C.ld, N,
+             ctypes.byref(tuning), None, 0, _stream())
+    elif method == "limb":
         call("gffm_matmul_limb_" + sfx, m, n, k, _ptr(A.data), A.ld, _ptr(B.data), B.ld, _ptr(C.data), C.ld, N,
              None, 0, _stream())
     elif method == "plain":
@@ -417,15 +437,16 @@ def stripe_mul_(C, A, B, M=None):
     return _gemm(C, A, B, A.N, "plain", stripe=M or 0)
 
 
-def mat_mul_gpu_type(A, B, mod_N=-1, method="auto"):
-    """mat_mul_gpu_type(A, B, mod_N) (mat_mul_gpu_direct.jl:8-42), exact for every size."""
+def mat_mul_gpu_type(A, B, mod_N=-1, method="auto", tuning=None):
+    """mat_mul_gpu_type(A, B, mod_N) (mat_mul_gpu_direct.jl:8-42), exact for every size.
+    ``tuning``: an optional LimbTuning for the limb path."""
     N = mod_N if mod_N > 0 else A.N
     if A.cols() != B.rows():
         raise CuModArraySizeMismatchException(
             "Matrix dimensions do not match. A has %d rows and %d cols, B has %d rows and %d cols."
             % (A.rows(), A.cols(), B.rows(), B.cols()))
     C = zeros(A.dtype, A.rows(), B.cols(), N)
-    return _gemm(C, A, B, N, method)
+    return _gemm(C, A, B, N, method, tuning=tuning)
 
 
 def mat_mul_type_inplace_(C, A, B, mod_N=-1, method="auto"):

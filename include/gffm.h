@@ -149,6 +149,33 @@ GFFM_API int gffm_matmul_limb_f32(int64_t m, int64_t n, int64_t k, const float *
                          int64_t ldb, float *C, int64_t ldc, int64_t N, void *workspace, size_t workspace_bytes,
                          gffm_stream_t stream);
 
+/* ---- tuning of the limb GEMM (no reference counterpart) -----------------------
+ * digit_bits: 7 (balanced base-2^7 digits, the default) or 8 (base-2^8: one
+ * digit fewer for 16255 < N <= 65279 and 2080639 < N <= 16711423, with 4x more
+ * frequent exact-accumulation drains); 0 keeps the table's / default choice.
+ * max_ctas: persistent grid size (0 = one CTA per SM).  The process-wide tune
+ * table (written by the autotuner, gffm/autotune.py) maps a modulus range and a
+ * work range (m*n*k) to a tuning; gffm_matmul_limb_* and its workspace size
+ * consult it, first matching entry wins.  It is the library's only global
+ * mutable state. */
+typedef struct gffm_limb_tuning {
+    int32_t digit_bits;
+    int32_t max_ctas;
+} gffm_limb_tuning;
+typedef struct gffm_tune_entry {
+    int64_t N_lo, N_hi;       /* inclusive modulus range */
+    double work_lo, work_hi;  /* inclusive m*n*k range */
+    gffm_limb_tuning tuning;
+} gffm_tune_entry;
+GFFM_API int gffm_tune_table_set(const gffm_tune_entry *entries, int64_t count);
+GFFM_API int gffm_tune_table_size(int64_t *count);
+GFFM_API int gffm_matmul_limb_tuned_workspace_size(int64_t m, int64_t n, int64_t k, int64_t N,
+                                                   const gffm_limb_tuning *tuning, size_t *bytes);
+GFFM_API int gffm_matmul_limb_tuned_f64(int64_t m, int64_t n, int64_t k, const double *A, int64_t lda,
+                                        const double *B, int64_t ldb, double *C, int64_t ldc, int64_t N,
+                                        const gffm_limb_tuning *tuning, void *workspace, size_t workspace_bytes,
+                                        gffm_stream_t stream);
+
 /* ---- elimination over Z/N, 2 <= N < 2^26 -----------------------------------
  * Blocked right-looking elimination with the reference's exact step
  * semantics; the trailing updates run on the limb tensor-core GEMM.  These
@@ -306,12 +333,14 @@ typedef struct gffm_batch_desc {
 
 /* Tuning of a plan; 0 in a field picks the default.  pluq_panel: panel width
  * (8, 16 or 32); gemm_ctas / pluq_ctas: persistent grid sizes; overlap: 1 runs
- * the products and the PLUQs on two graph branches at once. */
+ * the products and the PLUQs on two graph branches at once; digit_bits: 7 or 8
+ * for every product (0: per instance, whichever needs fewer digits). */
 typedef struct gffm_batch_tuning {
     int32_t pluq_panel;
     int32_t gemm_ctas;
     int32_t pluq_ctas;
     int32_t overlap;
+    int32_t digit_bits;
 } gffm_batch_tuning;
 
 typedef struct gffm_batch_plan_s *gffm_batch_plan;

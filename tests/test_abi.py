@@ -61,3 +61,29 @@ def test_host_side_argument_errors(lib):
     ws = ctypes.c_size_t(0)
     assert lib.gffm_matmul_limb_workspace_size(8192, 8192, 8192, 67108859, ctypes.byref(ws)) == 0
     assert ws.value == 4 * (8192 + 8192) * 8192 * 2
+
+
+def test_tuning_structs_match_header():
+    """ctypes layouts of gffm_limb_tuning, gffm_tune_entry, gffm_batch_tuning and gffm_batch_desc."""
+    import ctypes
+    from gffm import autotune, batched, cumod
+    assert ctypes.sizeof(cumod.LimbTuning) == 8
+    assert ctypes.sizeof(autotune._Entry) == 40
+    assert ctypes.sizeof(batched.Tuning) == 20
+    assert ctypes.sizeof(batched._Desc) == 17 * 8
+
+
+def test_limbs_for_thresholds():
+    from gffm import cumod
+    assert [cumod.limbs_for(N) for N in (2, 127, 128, 16255, 16256, 2080639, 2080640, 2 ** 26 - 1)] == \
+        [1, 1, 2, 2, 3, 3, 4, 4]
+    assert [cumod.limbs_for(N, 8) for N in (2, 255, 256, 65279, 65280, 16711423, 16711424, 2 ** 26 - 1)] == \
+        [1, 1, 2, 2, 3, 3, 4, 4]
+
+
+def test_fixed_primes_of_the_batched_workload():
+    from gffm import batched
+    assert batched.fixed_primes() == [
+        1021, 1447, 2039, 2887, 4093, 5791, 8191, 11579, 16381, 23167, 32749, 46337, 65521, 92681, 131071, 185363,
+        262139, 370723, 524287, 741431, 1048573, 1482907, 2097143, 2965819, 4194301, 5931641, 8388593, 11863279,
+        16777213, 23726561, 33554393, 47453111]

@@ -14,7 +14,8 @@ P26 = 67108859
 P25 = 33554393
 
 MM = [(1, 1, 1, 2), (5, 7, 3, 7), (130, 200, 70, 65521), (64, 64, 64, P26), (300, 17, 129, 2 ** 20),
-      (128, 512, 64, 1021), (33, 0, 20, 11), (257, 300, 190, 2080639), (96, 96, 96, 127), (40, 5000, 40, P25)]
+      (128, 512, 64, 1021), (33, 0, 20, 11), (257, 300, 190, 2080639), (96, 96, 96, 127), (40, 5000, 40, P25),
+      (200, 700, 100, 8388593), (64, 2000, 64, 16711423), (70, 300, 50, 65279)]
 PQ = [("uniform", 1, 1, 7), ("uniform", 5, 5, 7), ("uniform", 33, 20, 3), ("uniform", 20, 33, 65521),
       ("uniform", 64, 64, P26), ("uniform", 100, 130, 11579), ("uniform", 200, 200, P25), ("uniform", 300, 300, 1021),
       ("zero_cols", 40, 40, 13), ("zero_cols", 100, 130, 65521), ("lead_zero", 70, 80, 7), ("rank30", 96, 96, P26),
@@ -63,8 +64,8 @@ def check(gffm, inst, want, results):
         assert np.array_equal(Ld[:m, :m + 32], L0)
 
 
-@pytest.mark.parametrize("tuning", [None, (8, 0, 0, 0), (16, 3, 5, 1), (32, 1, 1, 0), (32, 0, 0, 1)],
-                         ids=["default", "nb8", "nb16-small-grids-overlap", "one-cta-each", "overlap"])
+@pytest.mark.parametrize("tuning", [None, (8, 0, 0, 0, 7), (16, 3, 5, 1, 8), (32, 1, 1, 0, 0), (32, 0, 0, 1, 0)],
+                         ids=["default", "nb8-7bit", "nb16-small-grids-overlap-8bit", "one-cta-each", "overlap"])
 def test_mixed_batch_matches_oracle(gffm, tuning):
     inst, want = build(gffm, 77)
     tu = gffm.BatchTuning(*tuning) if tuning else None
@@ -137,7 +138,7 @@ def test_batched_errors(gffm):
         gffm.BatchPlan([("pluq", big)])
     assert ei.value.status == 10
     with pytest.raises(gffm.GFFMError) as ei:
-        gffm.BatchPlan([("pluq", gffm.zeros(torch.float64, 4, 4, 7))], gffm.BatchTuning(12, 0, 0, 0))
+        gffm.BatchPlan([("pluq", gffm.zeros(torch.float64, 4, 4, 7))], gffm.BatchTuning(12, 0, 0, 0, 0))
     assert ei.value.status == 1
     empty = gffm.BatchPlan([])
     empty.run()

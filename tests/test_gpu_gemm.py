@@ -255,3 +255,62 @@ def test_empty_and_degenerate(gffm):
     Z = gffm.zeros(torch.float64, 0, 4, N)
     gffm.mul_(gffm.zeros(torch.float64, 0, 3, N), Z, gffm.zeros(torch.float64, 4, 3, N), method="limb")
     status_ok(gffm)
+
+
+# ---- digit width (the autotuner's choice): 8-bit digits at every boundary ----
+BITS8_MODULI = [2, 7, 255, 256, 65279, 65280, 65521, 2080640, 8388593, 16711423, 16711424, P26]
+
+
+@pytest.mark.parametrize("N", BITS8_MODULI)
+@pytest.mark.parametrize("shape", [(5, 7, 3), (129, 65, 100), (130, 200, 1025), (64, 64, 4160)],
+                         ids=lambda s: "x".join(map(str, s)))
+def test_limb_gemm_8bit_digits(gffm, N, shape):
+    rng = np.random.default_rng(N * 3 + shape[2])
+    m, n, k = shape
+    tu = gffm.LimbTuning(8, 0)
+    for name, A, B in patterns(rng, N, m, n, k):
+        Ag = gffm.CuModMatrix(A, N, elem_type=torch.float64)
+        Bg = gffm.CuModMatrix(B, N, elem_type=torch.float64)
+        got = as_int(gffm.mat_mul_gpu_type(Ag, Bg, method="limb", tuning=tu))
+        want = oracle.matmul(A, B, N)
+        assert np.array_equal(got, want), "%s: %d mismatches" % (name, int((got != want).sum()))
+    status_ok(gffm)
+
+
+def test_tune_table_routes_products(gffm):
+    """A tune table entry switches the digit width (visible in the workspace size) and the
+    grid; the products stay exact; clearing restores the defaults."""
+    import ctypes
+    from gffm import autotune
+    N, m, n, k = 8388593, 300, 200, 1000
+    L = gffm.load_library()
+    ws7 = ctypes.c_size_t(0)
+    assert L.gffm_matmul_limb_workspace_size(m, n, k, N, ctypes.byref(ws7)) == 0
+    table = {"gemm": [{"N_lo": 2080640, "N_hi": 16711423, "work_lo": 0, "work_hi": 1e30, "digit_bits": 8,
+                       "max_ctas": 7}], "batched": {}}
+    try:
+        assert autotune.apply(table) == 1
+        ws8 = ctypes.c_size_t(0)
+        assert L.gffm_matmul_limb_workspace_size(m, n, k, N, ctypes.byref(ws8)) == 0
+        assert ws8.value * 4 == ws7.value * 3          # 3 digits instead of 4
+        rng = np.random.default_rng(5)
+        A, B = rng.integers(0, N, size=(m, k)), rng.integers(0, N, size=(k, n))
+        C = gffm.mat_mul_gpu_type(gffm.CuModMatrix(A, N, elem_type=torch.float64),
+                                  gffm.CuModMatrix(B, N, elem_type=torch.float64))
+        assert np.array_equal(as_int(C), oracle.matmul(A, B, N))
+    finally:
+        autotune.apply()
+    ws = ctypes.c_size_t(0)
+    assert L.gffm_matmul_limb_workspace_size(m, n, k, N, ctypes.byref(ws)) == 0
+    assert ws.value == ws7.value or autotune.load_table().get("gemm")
+    status_ok(gffm)
+
+
+def test_limb_tuning_errors(gffm):
+    A = gffm.CuModMatrix([[1, 2], [3, 4]], 7, elem_type=torch.float64)
+    with pytest.raises(gffm.GFFMError) as ei:
+        gffm.mat_mul_gpu_type(A, A, method="limb", tuning=gffm.LimbTuning(9, 0))
+    assert ei.value.status == 1
+    with pytest.raises(gffm.GFFMError) as ei:
+        gffm.mat_mul_gpu_type(A, A, method="limb", tuning=gffm.LimbTuning(7, -1))
+    assert ei.value.status == 1
