@@ -55,6 +55,8 @@ def parse_args():
     ap.add_argument("--no-karatsuba", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--batch", type=int, default=4096, help="instances of the batched workload")
+    ap.add_argument("--only", default=None, choices=["gemm", "pluq", "karatsuba", "batched"],
+                    help="run one leg alone and print its fields (for profiling; not the benchmark line)")
     ap.add_argument("--size", type=int, default=8192, help="m = n = k (8192 is the benchmark workload)")
     return ap.parse_args()
 
@@ -223,6 +225,12 @@ def run_ours(args):
     stream = torch.cuda.current_stream()
     sp = ctypes.c_void_p(stream.cuda_stream)
 
+    if args.only in ("pluq", "karatsuba", "batched"):
+        leg = {"pluq": lambda: pluq_run(args, L, sp, dev), "karatsuba": lambda: karatsuba_run(L, sp, dev),
+               "batched": lambda: batched_run(args, dev, 112000.0)}[args.only]()
+        print(json.dumps({"only": args.only, args.only: leg}), flush=True)
+        return
+
     g = torch.Generator(device=dev)
     g.manual_seed(1234 + rank)
     A = gffm.rand(torch.float64, M, K, P26, generator=g)
@@ -302,6 +310,9 @@ def run_ours(args):
         "clocks": clk, "gpu_launches": 3 * args.steps, "roofline": roofline, "spot_check_ok": spot_ok,
     }
 
+    if args.only == "gemm":
+        print(json.dumps(out), flush=True)
+        return
     if not args.no_e2e:
         out["e2e"] = e2e_run(args, L, sp, dev, world, dist)
     if not args.no_plain:
@@ -431,6 +442,8 @@ def pluq_run(args, L, sp, dev):
     import oracle
     from gffm import elimination
     out = {"limb": elimination.bench_pluq(args.pluq, sp, dev, reps=2)}
+    if args.only == "pluq":
+        return out
     if not args.no_pluq_plain:
         out["plain"] = elimination.bench_pluq(args.pluq, sp, dev, reps=1, method="plain", warmup=0)
         out["limb_speedup"] = round(out["plain"]["seconds"] / out["limb"]["seconds"], 1)
@@ -536,18 +549,20 @@ def batched_run(args, dev, large_gemm_gops):
         torch.cuda.synchronize()
         return e0.elapsed_time(e1) / reps
 
-    plan = gffm.BatchPlan(inst)
+    plan = gffm.BatchPlan(inst, "auto")
     ms = timed(plan)
     info = [x for x in plan.pluq_info() if x is not None]
     full_rank = sum(1 for (op, n, _), x in zip([s for s in specs if s[0] == "pluq"], info) if x[2] == n)
     out = {"instances": len(specs), "ops": ops, "ms": round(ms, 3), "gops": round(ops / ms / 1e6, 1),
            "frac_of_large_gemm": round(ops / ms / 1e6 / large_gemm_gops, 3), "plan": plan.info(),
            "pluq_full_rank": "%d/%d" % (full_rank, len(info))}
+    if args.only == "batched":
+        return out
     best = (ms, None)
-    for tu in ((0, 0, 0, 1), (16, 0, 0, 0), (16, 0, 0, 1)):
+    for tu in ((0, 0, 0, 1, 0), (16, 0, 0, 0, 0), (32, 0, 0, 0, 7)):
         p2 = gffm.BatchPlan(inst, gffm.BatchTuning(*tu))
         t2 = timed(p2)
-        out["tuning_%d_%d_%d_%d_ms" % tu] = round(t2, 3)
+        out["tuning_%d_%d_%d_%d_%d_ms" % tu] = round(t2, 3)
         if t2 < best[0]:
             best = (t2, tu)
         del p2

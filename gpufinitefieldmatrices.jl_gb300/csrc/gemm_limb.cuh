@@ -48,14 +48,24 @@ constexpr int NUM_THREADS = 64 + 32 * NUM_EPI_WARPS;
 constexpr int MAX_SHIFTS = 7;
 constexpr int TILE_GROUP = 16;     // output-tile rows per raster group (L2 reuse)
 
-template <int L>
+// Tile width BNV: 64 (one accumulator set, 8 epilogue warps on 2 x 32 columns) or 32
+// (two accumulator sets in TMEM, 4 epilogue warps per set: the drain of one tile
+// overlaps the mma's of the next -- for short K, where a tile is one or two
+// exact chunks and the drain is as long as the products).
+template <int L, int BNV = 64>
 struct Cfg {
-    static constexpr int STAGE_BYTES = L * (A_TILE + B_TILE);
-    static constexpr int STAGES = (L == 4) ? 2 : (L == 3 ? 3 : (L == 2 ? 4 : 8));
+    static constexpr int B_T = BNV * BK * 2;
+    static constexpr int STAGE_BYTES = L * (A_TILE + B_T);
+    static constexpr int STAGES = BNV == 64 ? ((L == 4) ? 2 : (L == 3 ? 3 : (L == 2 ? 4 : 8)))
+                                            : ((L == 4) ? 2 : (L == 3 ? 3 : (L == 2 ? 5 : 8)));
     static constexpr int NSHIFT = 2 * L - 1;
-    static constexpr int TMEM_COLS = (64 * NSHIFT <= 64) ? 64 : (64 * NSHIFT <= 128 ? 128 : (64 * NSHIFT <= 256 ? 256 : 512));
-    static constexpr int CHUNK_KB = 64 / L;  // Kc = 4096 / L
+    static constexpr int ACC_BUFS = BNV == 32 ? 2 : 1;
+    static constexpr int BUF_COLS = BNV == 32 ? 256 : 0;   // column offset of the second accumulator set
+    static constexpr int EPI_PER_BUF = NUM_EPI_WARPS / ACC_BUFS;
+    static constexpr int TMEM_COLS = BNV == 32 ? 512
+                                               : ((64 * NSHIFT <= 64) ? 64 : (64 * NSHIFT <= 128 ? 128 : (64 * NSHIFT <= 256 ? 256 : 512)));
     static constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024;
+    static_assert(STAGES * STAGE_BYTES + 1024 <= 227 * 1024, "stages exceed shared memory");
 };
 
 struct Params {
@@ -88,14 +98,16 @@ __device__ __forceinline__ int64_t reduce_signed(int64_t acc, const Params &p) {
     return (int64_t)gffm_dev::barrett64((uint64_t)(acc + p.bias), (uint64_t)p.N, p.minv);
 }
 
-template <int L, int EPI>
+template <int L, int EPI, int BNV = 64>
 __global__ void __launch_bounds__(NUM_THREADS, 1)
     k_gemm_limb(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, Params p) {
-    using C_ = Cfg<L>;
+    using C_ = Cfg<L, BNV>;
+    constexpr int AB = C_::ACC_BUFS;
     extern __shared__ uint8_t dsmem_raw[];
     __shared__ uint64_t full_bar[C_::STAGES];
     __shared__ uint64_t empty_bar[C_::STAGES];
-    __shared__ uint64_t acc_full_bar, acc_empty_bar, drain_bar;
+    __shared__ uint64_t acc_full_bar[AB], acc_empty_bar[AB];
+    __shared__ uint64_t drain_bar;
     __shared__ uint32_t tmem_base_s;
     __shared__ int abort_sh;
     volatile int &abort_s = abort_sh;
@@ -110,8 +122,10 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
             gffm_dev::mbar_init(&full_bar[s], 1);
             gffm_dev::mbar_init(&empty_bar[s], 1);
         }
-        gffm_dev::mbar_init(&acc_full_bar, 1);
-        gffm_dev::mbar_init(&acc_empty_bar, NUM_EPI_WARPS);
+        for (int b = 0; b < AB; b++) {
+            gffm_dev::mbar_init(&acc_full_bar[b], 1);
+            gffm_dev::mbar_init(&acc_empty_bar[b], C_::EPI_PER_BUF);
+        }
         gffm_dev::mbar_init(&drain_bar, 1);
         abort_s = 0;
         gffm_dev::fence_mbar_init();
@@ -148,7 +162,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
                         gffm_dev::tma_load_2d(sa + l * A_TILE, &tmA, &full_bar[stage], kb * BK, l * p.Mpad + tm * BM);
 #pragma unroll
                     for (int l = 0; l < L; l++)
-                        gffm_dev::tma_load_2d(sb + l * B_TILE, &tmB, &full_bar[stage], kb * BK, l * p.Npad + tn * BN);
+                        gffm_dev::tma_load_2d(sb + l * C_::B_T, &tmB, &full_bar[stage], kb * BK, l * p.Npad + tn * BNV);
                     issued_mask |= 1u << stage;
                     issued_parity_mask = (issued_parity_mask & ~(1u << stage)) | (phase << stage);
                     if (++stage == C_::STAGES) {
@@ -167,15 +181,21 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
         // ---------------- MMA issuer ----------------
         if (lane == 0) {
             int stage = 0;
-            uint32_t phase = 0, acc_phase = 0;
+            uint32_t phase = 0;
+            uint32_t acc_phase[AB];
+#pragma unroll
+            for (int b = 0; b < AB; b++) acc_phase[b] = 0;
             bool issued_any = false;
-            const uint32_t idesc_full = gffm_dev::idesc_f16_f32(BM, BN * L);
-            const uint32_t idesc_lo = gffm_dev::idesc_f16_f32(BM, BN * (L > 1 ? L - 1 : 1));
-            const uint32_t idesc_one = gffm_dev::idesc_f16_f32(BM, BN);
-            for (int t = blockIdx.x; t < ntiles_total && !abort_s; t += gridDim.x) {
+            const uint32_t idesc_full = gffm_dev::idesc_f16_f32(BM, BNV * L);
+            const uint32_t idesc_lo = gffm_dev::idesc_f16_f32(BM, BNV * (L > 1 ? L - 1 : 1));
+            const uint32_t idesc_one = gffm_dev::idesc_f16_f32(BM, BNV);
+            int local = 0;
+            for (int t = blockIdx.x; t < ntiles_total && !abort_s; t += gridDim.x, local++) {
+                const int buf = AB == 2 ? (local & 1) : 0;
+                const uint32_t acc = tmem + (uint32_t)(buf * C_::BUF_COLS);
                 for (int kb0 = 0; kb0 < p.kblocks && !abort_s; kb0 += p.chunk_kb) {
                     int kb1 = kb0 + p.chunk_kb < p.kblocks ? kb0 + p.chunk_kb : p.kblocks;
-                    if (!gffm_dev::mbar_wait(&acc_empty_bar, acc_phase ^ 1)) {
+                    if (!gffm_dev::mbar_wait(&acc_empty_bar[buf], acc_phase[buf] ^ 1)) {
                         atomicOr(p.err, 2);
                         abort_s = 1;
                         break;
@@ -195,19 +215,19 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
                             const uint64_t bdesc = gffm_dev::umma_desc_sw128(sb + kk * 32);
                             if (kb == kb0 && kk == 0) {
                                 // first k-step of a chunk: initialise every shift accumulator once
-                                gffm_dev::mma_f16(tmem, gffm_dev::umma_desc_sw128(sa + kk * 32), bdesc, idesc_full, 0);
+                                gffm_dev::mma_f16(acc, gffm_dev::umma_desc_sw128(sa + kk * 32), bdesc, idesc_full, 0);
 #pragma unroll
                                 for (int i = 1; i < L; i++) {
                                     const uint64_t adesc = gffm_dev::umma_desc_sw128(sa + i * A_TILE + kk * 32);
-                                    gffm_dev::mma_f16(tmem + 64 * i, adesc, bdesc, idesc_lo, 1);
-                                    gffm_dev::mma_f16(tmem + 64 * (i + L - 1), adesc,
-                                                      gffm_dev::umma_desc_sw128(sb + (L - 1) * B_TILE + kk * 32),
+                                    gffm_dev::mma_f16(acc + BNV * i, adesc, bdesc, idesc_lo, 1);
+                                    gffm_dev::mma_f16(acc + BNV * (i + L - 1), adesc,
+                                                      gffm_dev::umma_desc_sw128(sb + (L - 1) * C_::B_T + kk * 32),
                                                       idesc_one, 0);
                                 }
                             } else {
 #pragma unroll
                                 for (int i = 0; i < L; i++)
-                                    gffm_dev::mma_f16(tmem + 64 * i, gffm_dev::umma_desc_sw128(sa + i * A_TILE + kk * 32),
+                                    gffm_dev::mma_f16(acc + BNV * i, gffm_dev::umma_desc_sw128(sa + i * A_TILE + kk * 32),
                                                       bdesc, idesc_full, 1);
                             }
                         }
@@ -219,8 +239,8 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
                         }
                     }
                     if (abort_s) break;
-                    gffm_dev::mma_commit(&acc_full_bar);
-                    acc_phase ^= 1;
+                    gffm_dev::mma_commit(&acc_full_bar[buf]);
+                    acc_phase[buf] ^= 1;
                 }
             }
             if (abort_s && issued_any) {
@@ -233,9 +253,14 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
         // ---------------- epilogue ----------------
         const int ew = warp - 2;
         const int quad = warp & 3;       // TMEM lane quadrant this warp may access
-        const int half = ew >> 2;        // which 32 of the 64 tile columns
+        // BNV = 64: `half` picks which 32 of the 64 tile columns; BNV = 32: which accumulator set
+        const int half = ew >> 2;
         uint32_t acc_phase = 0;
-        for (int t = blockIdx.x; t < ntiles_total; t += gridDim.x) {
+        int local = 0;
+        for (int t = blockIdx.x; t < ntiles_total; t += gridDim.x, local++) {
+            if (AB == 2 && (local & 1) != half) continue;      // the other warp group's tile
+            const int buf = AB == 2 ? half : 0;
+            const uint32_t accb = tmem + (uint32_t)(buf * C_::BUF_COLS) + (AB == 2 ? 0u : (uint32_t)(32 * half));
             int tm, tn;
             tile_coords(t, p.mtiles, p.ntiles, tm, tn);
             int64_t acc[32];
@@ -244,7 +269,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
             bool ok = true;
             int chunk = 0;
             for (int kb0 = 0; kb0 < p.kblocks; kb0 += p.chunk_kb, chunk++) {
-                if (!gffm_dev::mbar_wait(&acc_full_bar, acc_phase)) {
+                if (!gffm_dev::mbar_wait(&acc_full_bar[buf], acc_phase)) {
                     atomicOr(p.err, 8);
                     abort_s = 1;
                     ok = false;
@@ -254,7 +279,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
 #pragma unroll
                 for (int s = 0; s < C_::NSHIFT; s++) {
                     uint32_t v[32];
-                    gffm_dev::tmem_ld_32x32b_x32(tmem + ((uint32_t)(quad * 32) << 16) + 64 * s + 32 * half, v);
+                    gffm_dev::tmem_ld_32x32b_x32(accb + ((uint32_t)(quad * 32) << 16) + BNV * s, v);
                     gffm_dev::tmem_ld_wait();
                     if (EPI == EPI_EXACT_I64) {
                         // exact chunk value sum_s C_s 2^(7s), in [0, 2^62) for raw digits: wrapping
@@ -271,7 +296,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
                 }
                 gffm_dev::tc_fence_before();
                 __syncwarp();
-                if (lane == 0) gffm_dev::mbar_arrive(&acc_empty_bar);
+                if (lane == 0) gffm_dev::mbar_arrive(&acc_empty_bar[buf]);
                 acc_phase ^= 1;
                 if (EPI == EPI_EXACT_I64) {
                     // acc < N < 2^52 before the chunk, so acc + chunk < 2^63: one Barrett step
@@ -285,7 +310,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
             }
             if (!ok || abort_s) break;
             const int64_t row = (int64_t)tm * BM + quad * 32 + lane;
-            const int64_t col0 = (int64_t)tn * BN + half * 32;
+            const int64_t col0 = (int64_t)tn * BNV + (AB == 2 ? 0 : half * 32);
             if (row < p.m) {
                 if (EPI == EPI_SUB_I32) {
                     // read-modify-write: issue all 32 loads before any store

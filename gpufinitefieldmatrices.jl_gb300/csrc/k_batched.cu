@@ -98,29 +98,36 @@ __device__ __forceinline__ void split_b_pairs(const SplitJob &J, int64_t local) 
         *reinterpret_cast<__half2 *>(J.dst + l * plane + (size_t)c * J.kpad + kk) = __halves2half2(d0[l], d1[l]);
 }
 
-__global__ void __launch_bounds__(256) k_split_batched(const SplitJob *__restrict__ jobs, int njobs) {
+// A block takes one chunk: up to SPLIT_CHUNK consecutive work units (32 x 32 tiles
+// of A, or 256 digit pairs of B) of one operand, found with a single table load.
+constexpr int SPLIT_CHUNK = 8;
+
+struct SplitChunk {
+    int job, local0, count, pad_;
+};
+
+__global__ void __launch_bounds__(256) k_split_batched(const SplitJob *__restrict__ jobs,
+                                                       const SplitChunk *__restrict__ chunks) {
     __shared__ int32_t tile[32][33];
-    const int64_t b = blockIdx.x;
-    int lo = 0, hi = njobs - 1;          // last job with blk0 <= b
-    while (lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        if (jobs[mid].blk0 <= b) lo = mid; else hi = mid - 1;
-    }
-    const SplitJob J = jobs[lo];
-    const int64_t local = b - J.blk0;
-    if (J.is_b) {
-        switch (J.L) {
-            case 1: split_b_pairs<1>(J, local); break;
-            case 2: split_b_pairs<2>(J, local); break;
-            case 3: split_b_pairs<3>(J, local); break;
-            default: split_b_pairs<4>(J, local); break;
-        }
-    } else {
-        switch (J.L) {
-            case 1: split_a_tile<1>(J, local, tile); break;
-            case 2: split_a_tile<2>(J, local, tile); break;
-            case 3: split_a_tile<3>(J, local, tile); break;
-            default: split_a_tile<4>(J, local, tile); break;
+    const SplitChunk ch = chunks[blockIdx.x];
+    const SplitJob J = jobs[ch.job];
+    for (int u = 0; u < ch.count; u++) {
+        const int64_t local = (int64_t)ch.local0 + u;
+        if (J.is_b) {
+            switch (J.L) {
+                case 1: split_b_pairs<1>(J, local); break;
+                case 2: split_b_pairs<2>(J, local); break;
+                case 3: split_b_pairs<3>(J, local); break;
+                default: split_b_pairs<4>(J, local); break;
+            }
+        } else {
+            switch (J.L) {
+                case 1: split_a_tile<1>(J, local, tile); break;
+                case 2: split_a_tile<2>(J, local, tile); break;
+                case 3: split_a_tile<3>(J, local, tile); break;
+                default: split_a_tile<4>(J, local, tile); break;
+            }
+            __syncthreads();   // the tile is reused by the next unit
         }
     }
 }
@@ -352,6 +359,8 @@ struct gffm_batch_plan_s {
     batched::WorkItem *d_items = nullptr;
     CUtensorMap *d_tmaps = nullptr;
     batched::SplitJob *d_jobs = nullptr;
+    batched::SplitChunk *d_chunks = nullptr;
+    int64_t nchunks = 0;
     batched::PQInst *d_pq = nullptr;
     int *d_order = nullptr, *d_next = nullptr;
     int32_t *d_tmp = nullptr;
@@ -453,7 +462,7 @@ int build_graph(gffm_batch_plan p, bool overlap) {
         for (const auto &z : p->zero_k)
             fail(cudaMemset2DAsync(z.C, (size_t)z.ldc * 8, 0, (size_t)z.m * 8, (size_t)z.n, s0), "cudaMemset2DAsync");
         if (p->n_mm > 0 && p->nitems > 0) {
-            k_split_batched<<<(unsigned)p->split_blocks, 256, 0, s0>>>(p->d_jobs, p->njobs);
+            k_split_batched<<<(unsigned)p->nchunks, 256, 0, s0>>>(p->d_jobs, p->d_chunks);
             fail(cudaGetLastError(), "k_split_batched");
             k_gemm_grouped<<<p->gemm_grid, NUM_THREADS, G_SMEM_BYTES, s0>>>(p->d_mm, p->d_items, p->nitems, p->d_tmaps,
                                                                           gffm::device_error_flag());
@@ -623,6 +632,15 @@ int create(const gffm_batch_desc *descs, int64_t count, const gffm_batch_tuning 
     p->nitems = (int)items.size();
     const size_t o_items = cv.take(sizeof(WorkItem) * std::max<size_t>(1, items.size()));
     const size_t o_jobs = cv.take(sizeof(SplitJob) * std::max(1, 2 * p->n_mm));
+    // split work units per job: 32 x 32 tiles of A, 256 digit pairs of B
+    int64_t nchunks = 0;
+    for (int q = 0; q < p->n_mm; q++) {
+        if (mm[q].kblocks == 0) continue;
+        const limb::Layout &g = lay[q];
+        const int64_t ua = (g.Kpad / 32) * (g.Mpad / 32), ub = ((g.Kpad / 2) * g.Npad + 255) / 256;
+        nchunks += (ua + SPLIT_CHUNK - 1) / SPLIT_CHUNK + (ub + SPLIT_CHUNK - 1) / SPLIT_CHUNK;
+    }
+    const size_t o_chunks = cv.take(sizeof(SplitChunk) * std::max<int64_t>(1, nchunks));
     p->mem_bytes = cv.off;
     cudaError_t e = cudaMalloc(&p->mem, p->mem_bytes);
     if (e != cudaSuccess) {
@@ -637,6 +655,7 @@ int create(const gffm_batch_desc *descs, int64_t count, const gffm_batch_tuning 
     p->d_next = reinterpret_cast<int *>(base + o_next);
     p->d_items = reinterpret_cast<WorkItem *>(base + o_items);
     p->d_jobs = reinterpret_cast<SplitJob *>(base + o_jobs);
+    p->d_chunks = reinterpret_cast<SplitChunk *>(base + o_chunks);
     p->d_tmp = reinterpret_cast<int32_t *>(base + o_tmp);
 
     // split jobs and TMA descriptors
@@ -665,6 +684,14 @@ int create(const gffm_batch_desc *descs, int64_t count, const gffm_batch_tuning 
     }
     p->njobs = (int)jobs.size();
     p->split_blocks = blk;
+    std::vector<SplitChunk> chunks;
+    chunks.reserve((size_t)nchunks);
+    for (size_t j = 0; j < jobs.size(); j++) {
+        const int64_t units = (j + 1 < jobs.size() ? jobs[j + 1].blk0 : blk) - jobs[j].blk0;
+        for (int64_t u = 0; u < units; u += SPLIT_CHUNK)
+            chunks.push_back(SplitChunk{(int)j, (int)u, (int)std::min<int64_t>(SPLIT_CHUNK, units - u), 0});
+    }
+    p->nchunks = (int64_t)chunks.size();
     // PLUQ workspace pointers and order (largest work first)
     std::vector<int> order(p->n_pq);
     for (int q = 0; q < p->n_pq; q++) {
@@ -688,6 +715,7 @@ int create(const gffm_batch_desc *descs, int64_t count, const gffm_batch_tuning 
     PLAN_CUDA(cudaMemcpy(p->d_tmaps, tmaps.data(), sizeof(CUtensorMap) * 2 * p->n_mm, cudaMemcpyHostToDevice));
     PLAN_CUDA(cudaMemcpy(p->d_items, items.data(), sizeof(WorkItem) * items.size(), cudaMemcpyHostToDevice));
     PLAN_CUDA(cudaMemcpy(p->d_jobs, jobs.data(), sizeof(SplitJob) * jobs.size(), cudaMemcpyHostToDevice));
+    PLAN_CUDA(cudaMemcpy(p->d_chunks, chunks.data(), sizeof(SplitChunk) * chunks.size(), cudaMemcpyHostToDevice));
     PLAN_CUDA(cudaMemcpy(p->d_pq, pq.data(), sizeof(PQInst) * pq.size(), cudaMemcpyHostToDevice));
     PLAN_CUDA(cudaMemcpy(p->d_order, order.data(), sizeof(int) * order.size(), cudaMemcpyHostToDevice));
 

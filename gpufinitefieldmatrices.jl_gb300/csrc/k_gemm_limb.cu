@@ -2,6 +2,7 @@
 // argument checks, workspace layout, TMA descriptors and launches.
 #include "gemm_limb.cuh"
 #include "limb_host.h"
+#include "limb_launch.cuh"
 
 #include <cudaTypedefs.h>
 #include <algorithm>
@@ -185,26 +186,16 @@ int split_b(const T *B, int64_t ldb, int64_t k, int64_t n, __half *D, const Layo
     return GFFM_OK;
 }
 
-template <int L, int EPI>
-static int launch_gemm_L(const CUtensorMap &ta, const CUtensorMap &tb, const Params &p, int grid, cudaStream_t s) {
-    auto kern = k_gemm_limb<L, EPI>;
-    GFFM_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, Cfg<L>::SMEM_BYTES));
-    gffm::profile_hook().before(s);
-    kern<<<grid, NUM_THREADS, Cfg<L>::SMEM_BYTES, s>>>(ta, tb, p);
-    gffm::profile_hook().after(s);
-    GFFM_LAUNCH_CHECK("k_gemm_limb");
-    return GFFM_OK;
-}
-
 template <int EPI>
 static int launch_gemm(int L, const CUtensorMap &ta, const CUtensorMap &tb, const Params &p, int grid, cudaStream_t s) {
     switch (L) {
-        case 1: return launch_gemm_L<1, EPI>(ta, tb, p, grid, s);
-        case 2: return launch_gemm_L<2, EPI>(ta, tb, p, grid, s);
-        case 3: return launch_gemm_L<3, EPI>(ta, tb, p, grid, s);
-        default: return launch_gemm_L<4, EPI>(ta, tb, p, grid, s);
+        case 1: return launch_gemm_L<1, EPI, 64>(ta, tb, p, grid, s);
+        case 2: return launch_gemm_L<2, EPI, 64>(ta, tb, p, grid, s);
+        case 3: return launch_gemm_L<3, EPI, 64>(ta, tb, p, grid, s);
+        default: return launch_gemm_L<4, EPI, 64>(ta, tb, p, grid, s);
     }
 }
+
 
 int gemm_digits(const Layout &g, const __half *Ad, const __half *Bd, int64_t m, int64_t n, int64_t k, int64_t N,
                 void *C, int64_t ldc, int epi, int max_ctas, cudaStream_t s, const double *X, const double *Y) {
@@ -218,7 +209,11 @@ int gemm_digits(const Layout &g, const __half *Ad, const __half *Bd, int64_t m, 
     CUtensorMap ta, tb;
     st = make_map(&ta, Ad, g.Kpad, (int64_t)g.L * g.Mpad, BM);
     if (st) return st;
-    st = make_map(&tb, Bd, g.Kpad, (int64_t)g.L * g.Npad, BN);
+    // 64-column tiles (one accumulator set) unless the tuning asks for 32-column tiles with
+    // two accumulator sets; measured on GB300 the 64-column tile wins at every K tried (the
+    // narrower tile doubles the A-operand traffic per output), so 32 is a tuner candidate only
+    const int bnv = g.bn == 32 ? 32 : 64;
+    st = make_map(&tb, Bd, g.Kpad, (int64_t)g.L * g.Npad, bnv);
     if (st) return st;
     Params p;
     p.m = (int)m;
@@ -227,7 +222,7 @@ int gemm_digits(const Layout &g, const __half *Ad, const __half *Bd, int64_t m, 
     p.Mpad = (int)g.Mpad;
     p.Npad = (int)g.Npad;
     p.mtiles = (int)((m + BM - 1) / BM);
-    p.ntiles = (int)((n + BN - 1) / BN);
+    p.ntiles = (int)((n + bnv - 1) / bnv);
     p.chunk_kb = chunk_kblocks(g);
     p.N = N;
     p.minv = ~uint64_t(0) / (uint64_t)N;
@@ -248,6 +243,7 @@ int gemm_digits(const Layout &g, const __half *Ad, const __half *Bd, int64_t m, 
     int grid = gffm::sm_count();
     if (max_ctas > 0 && grid > max_ctas) grid = max_ctas;
     if (grid > ntiles) grid = ntiles;
+    if (bnv == 32) return launch_gemm_short(epi, g.L, ta, tb, p, grid, s);
     switch (epi) {
         case EPI_STORE_F64: return launch_gemm<EPI_STORE_F64>(g.L, ta, tb, p, grid, s);
         case EPI_STORE_F32: return launch_gemm<EPI_STORE_F32>(g.L, ta, tb, p, grid, s);
@@ -280,15 +276,17 @@ namespace limb {
 static std::vector<gffm_tune_entry> g_tune;
 static std::mutex g_tune_mu;
 
-void tuned_for(int64_t m, int64_t n, int64_t k, int64_t N, int *bits, int *max_ctas) {
+void tuned_for(int64_t m, int64_t n, int64_t k, int64_t N, int *bits, int *max_ctas, int *tile_n) {
     *bits = 7;
     *max_ctas = 0;
+    *tile_n = 64;
     const double work = (double)m * (double)n * (double)k;
     std::lock_guard<std::mutex> lk(g_tune_mu);
     for (const gffm_tune_entry &e : g_tune) {
         if (N < e.N_lo || N > e.N_hi || work < e.work_lo || work > e.work_hi) continue;
         *bits = e.tuning.digit_bits == 8 ? 8 : 7;
         *max_ctas = e.tuning.max_ctas > 0 ? e.tuning.max_ctas : 0;
+        *tile_n = e.tuning.tile_n == 32 ? 32 : 64;
         return;
     }
 }
@@ -302,15 +300,18 @@ int check_tuning(const gffm_limb_tuning *t) {
     if (t->digit_bits != 0 && t->digit_bits != 7 && t->digit_bits != 8)
         return gffm::set_error(GFFM_ERR_ARG, "digit_bits must be 0, 7 or 8");
     if (t->max_ctas < 0) return gffm::set_error(GFFM_ERR_ARG, "max_ctas must be >= 0");
+    if (t->tile_n != 0 && t->tile_n != 32 && t->tile_n != 64)
+        return gffm::set_error(GFFM_ERR_ARG, "tile_n must be 0, 32 or 64");
     return GFFM_OK;
 }
 
-// the digit width and grid of a product: an explicit tuning, else the tune table
-void pick(const gffm_limb_tuning *t, int64_t m, int64_t n, int64_t k, int64_t N, int *bits, int *ctas) {
-    limb::tuned_for(m, n, k, N, bits, ctas);
+// the digit width, grid and tile width of a product: an explicit tuning, else the tune table
+void pick(const gffm_limb_tuning *t, int64_t m, int64_t n, int64_t k, int64_t N, int *bits, int *ctas, int *tile_n) {
+    limb::tuned_for(m, n, k, N, bits, ctas, tile_n);
     if (t) {
         if (t->digit_bits) *bits = t->digit_bits;
         *ctas = t->max_ctas;
+        if (t->tile_n) *tile_n = t->tile_n;
     }
 }
 
@@ -332,9 +333,10 @@ int matmul_limb(int64_t m, int64_t n, int64_t k, const T *A, int64_t lda, const 
         GFFM_CUDA(cudaMemset2DAsync(C, (size_t)ldc * sizeof(T), 0, (size_t)m * sizeof(T), (size_t)n, s));
         return GFFM_OK;
     }
-    int bits, ctas;
-    pick(tune, m, n, k, N, &bits, &ctas);
+    int bits, ctas, tile_n;
+    pick(tune, m, n, k, N, &bits, &ctas, &tile_n);
     limb::Layout g = limb::layout_bits(m, n, k, N, bits);
+    g.bn = tile_n;
     Scratch scr;
     st = scr.acquire(ws, ws_bytes, g.a_bytes + g.b_bytes, s);
     if (st) return st;
@@ -359,8 +361,8 @@ int gffm_matmul_limb_tuned_workspace_size(int64_t m, int64_t n, int64_t k, int64
     if (st) return st;
     st = limb::check_args(m, n, k, m > 1 ? m : 1, k > 1 ? k : 1, m > 1 ? m : 1, N);
     if (st) return st;
-    int bits, ctas;
-    pick(tuning, m, n, k, N, &bits, &ctas);
+    int bits, ctas, tile_n;
+    pick(tuning, m, n, k, N, &bits, &ctas, &tile_n);
     limb::Layout g = limb::layout_bits(m, n, k, N, bits);
     *bytes = (m == 0 || n == 0 || k == 0) ? 0 : g.a_bytes + g.b_bytes;
     return GFFM_OK;

@@ -26,6 +26,7 @@ enum Split { SPLIT_CENTRED = 0, SPLIT_RAW = 1, SPLIT_SUM = 2 };
 struct Layout {
     int L;                 // digits per residue
     int bits = 7;          // digit width: balanced base-2^bits digits (7 or 8)
+    int bn = 64;           // output tile width: 64, or 32 with two accumulator sets
     int64_t Mpad, Npad, Kpad;
     size_t a_bytes, b_bytes;
 };
@@ -36,8 +37,8 @@ int raw_limbs_for(int64_t N);
 Layout layout(int64_t m, int64_t n, int64_t k, int64_t N);
 Layout layout_bits(int64_t m, int64_t n, int64_t k, int64_t N, int bits);
 int chunk_kblocks(const Layout &g);        // k-blocks of 64 per exact accumulation chunk
-// the process-wide tune table's choice for a product (digit width, grid); defaults 7 / 0
-void tuned_for(int64_t m, int64_t n, int64_t k, int64_t N, int *bits, int *max_ctas);
+// the process-wide tune table's choice for a product (digit width, grid, tile width); defaults 7 / 0 / 64
+void tuned_for(int64_t m, int64_t n, int64_t k, int64_t N, int *bits, int *max_ctas, int *tile_n);
 Layout layout_L(int64_t m, int64_t n, int64_t k, int L);
 int check_args(int64_t m, int64_t n, int64_t k, int64_t lda, int64_t ldb, int64_t ldc, int64_t N);
 

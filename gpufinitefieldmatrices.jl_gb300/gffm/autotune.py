@@ -8,7 +8,8 @@ and keeps the winners in a small JSON table, ``gffm/tuning.json``:
   table (``gffm_tune_table_set``); every ``gffm_matmul_limb_*`` call and its
   workspace-size query consult it (first matching modulus and m*n*k range).
   Candidates are the digit width (7-bit digits, or 8-bit digits where they
-  need one digit fewer) and the persistent grid size.
+  need one digit fewer), the persistent grid size and the output tile width
+  (64 columns, or 32 with two accumulator sets).
 * ``"batched"``: per batch signature (the multiset of instance shapes, ops and
   digit counts), the best ``gffm_batch_tuning`` -- panel width of the PLUQ
   kernel, grid split, overlap of the two graph branches, digit width.
@@ -32,7 +33,8 @@ BITS8_RANGES = [(16256, 65279), (2080640, 16711423)]
 
 
 class _LimbTuning(ctypes.Structure):
-    _fields_ = [("digit_bits", ctypes.c_int32), ("max_ctas", ctypes.c_int32)]
+    _fields_ = [("digit_bits", ctypes.c_int32), ("max_ctas", ctypes.c_int32), ("tile_n", ctypes.c_int32),
+                ("reserved", ctypes.c_int32)]
 
 
 class _Entry(ctypes.Structure):
@@ -60,7 +62,7 @@ def apply(table=None):
     arr = (_Entry * max(1, len(ents)))()
     for i, e in enumerate(ents):
         arr[i] = _Entry(int(e["N_lo"]), int(e["N_hi"]), float(e["work_lo"]), float(e["work_hi"]),
-                        _LimbTuning(int(e["digit_bits"]), int(e.get("max_ctas", 0))))
+                        _LimbTuning(int(e["digit_bits"]), int(e.get("max_ctas", 0)), int(e.get("tile_n", 0)), 0))
     call("gffm_tune_table_set", ctypes.cast(arr, ctypes.c_void_p), len(ents))
     return len(ents)
 
@@ -78,13 +80,13 @@ def _time(fn, reps):
     return e0.elapsed_time(e1) / reps
 
 
-def time_gemm(m, n, k, N, digit_bits, max_ctas=0, reps=5, generator=None):
+def time_gemm(m, n, k, N, digit_bits, max_ctas=0, reps=5, generator=None, tile_n=0):
     """Milliseconds of one C = A*B mod N (resident Float64 operands) with a given tuning."""
     from .cumod import rand, zeros
     A = rand(torch.float64, m, k, N, generator=generator)
     B = rand(torch.float64, k, n, N, generator=generator)
     C = zeros(torch.float64, m, n, N)
-    tu = _LimbTuning(digit_bits, max_ctas)
+    tu = _LimbTuning(digit_bits, max_ctas, tile_n, 0)
     ws = ctypes.c_size_t(0)
     call("gffm_matmul_limb_tuned_workspace_size", m, n, k, N, ctypes.byref(tu), ctypes.byref(ws))
     buf = torch.empty(max(1, ws.value), dtype=torch.uint8, device="cuda")
@@ -113,16 +115,18 @@ def tune_gemm(shapes=((512, 512, 512), (2048, 2048, 2048), (8192, 8192, 8192)),
             best = None
             for bits in (7, 8):
                 for ctas in (0, sms // 2):
-                    t = time_gemm(m, n, k, N, bits, ctas, reps, g)
-                    log.append({"N": N, "m": m, "n": n, "k": k, "digit_bits": bits, "max_ctas": ctas, "ms": round(t, 4)})
-                    if best is None or t < best[0]:
-                        best = (t, bits, ctas)
+                    for tile_n in (64, 32):
+                        t = time_gemm(m, n, k, N, bits, ctas, reps, g, tile_n)
+                        log.append({"N": N, "m": m, "n": n, "k": k, "digit_bits": bits, "max_ctas": ctas,
+                                    "tile_n": tile_n, "ms": round(t, 4)})
+                        if best is None or t < best[0]:
+                            best = (t, bits, ctas, tile_n)
             w = m * n * k
             i = works.index(w)
             lo = 0.0 if i == 0 else (works[i - 1] * w) ** 0.5
             hi = 1e30 if i == len(works) - 1 else (works[i + 1] * w) ** 0.5
             entries.append({"N_lo": rng[0], "N_hi": rng[1], "work_lo": lo, "work_hi": hi,
-                            "digit_bits": best[1], "max_ctas": best[2], "tuned_on": [m, n, k, N],
+                            "digit_bits": best[1], "max_ctas": best[2], "tile_n": best[3], "tuned_on": [m, n, k, N],
                             "ms": round(best[0], 4)})
     return entries, log
 

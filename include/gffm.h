@@ -153,7 +153,7 @@ GFFM_API int gffm_matmul_limb_f32(int64_t m, int64_t n, int64_t k, const float *
  * digit_bits: 7 (balanced base-2^7 digits, the default) or 8 (base-2^8: one
  * digit fewer for 16255 < N <= 65279 and 2080639 < N <= 16711423, with 4x more
  * frequent exact-accumulation drains); 0 keeps the table's / default choice.
- * max_ctas: persistent grid size (0 = one CTA per SM).  The process-wide tune
+ * max_ctas: persistent grid size (0 = one CTA per SM); tile_n: 0/64 or 32.  The process-wide tune
  * table (written by the autotuner, gffm/autotune.py) maps a modulus range and a
  * work range (m*n*k) to a tuning; gffm_matmul_limb_* and its workspace size
  * consult it, first matching entry wins.  It is the library's only global
@@ -161,6 +161,8 @@ GFFM_API int gffm_matmul_limb_f32(int64_t m, int64_t n, int64_t k, const float *
 typedef struct gffm_limb_tuning {
     int32_t digit_bits;
     int32_t max_ctas;
+    int32_t tile_n;           /* output tile width: 64 (default) or 32 with two TMEM accumulator sets */
+    int32_t reserved;         /* 0 */
 } gffm_limb_tuning;
 typedef struct gffm_tune_entry {
     int64_t N_lo, N_hi;       /* inclusive modulus range */

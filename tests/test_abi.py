@@ -67,8 +67,8 @@ def test_tuning_structs_match_header():
     """ctypes layouts of gffm_limb_tuning, gffm_tune_entry, gffm_batch_tuning and gffm_batch_desc."""
     import ctypes
     from gffm import autotune, batched, cumod
-    assert ctypes.sizeof(cumod.LimbTuning) == 8
-    assert ctypes.sizeof(autotune._Entry) == 40
+    assert ctypes.sizeof(cumod.LimbTuning) == 16
+    assert ctypes.sizeof(autotune._Entry) == 48
     assert ctypes.sizeof(batched.Tuning) == 20
     assert ctypes.sizeof(batched._Desc) == 17 * 8
 

@@ -267,7 +267,7 @@ BITS8_MODULI = [2, 7, 255, 256, 65279, 65280, 65521, 2080640, 8388593, 16711423,
 def test_limb_gemm_8bit_digits(gffm, N, shape):
     rng = np.random.default_rng(N * 3 + shape[2])
     m, n, k = shape
-    tu = gffm.LimbTuning(8, 0)
+    tu = gffm.LimbTuning(8, 0, 0, 0)
     for name, A, B in patterns(rng, N, m, n, k):
         Ag = gffm.CuModMatrix(A, N, elem_type=torch.float64)
         Bg = gffm.CuModMatrix(B, N, elem_type=torch.float64)
@@ -284,11 +284,12 @@ def test_tune_table_routes_products(gffm):
     from gffm import autotune
     N, m, n, k = 8388593, 300, 200, 1000
     L = gffm.load_library()
-    ws7 = ctypes.c_size_t(0)
-    assert L.gffm_matmul_limb_workspace_size(m, n, k, N, ctypes.byref(ws7)) == 0
     table = {"gemm": [{"N_lo": 2080640, "N_hi": 16711423, "work_lo": 0, "work_hi": 1e30, "digit_bits": 8,
                        "max_ctas": 7}], "batched": {}}
     try:
+        assert autotune.apply({"gemm": []}) == 0          # no table: 7-bit digits
+        ws7 = ctypes.c_size_t(0)
+        assert L.gffm_matmul_limb_workspace_size(m, n, k, N, ctypes.byref(ws7)) == 0
         assert autotune.apply(table) == 1
         ws8 = ctypes.c_size_t(0)
         assert L.gffm_matmul_limb_workspace_size(m, n, k, N, ctypes.byref(ws8)) == 0
@@ -299,18 +300,31 @@ def test_tune_table_routes_products(gffm):
                                   gffm.CuModMatrix(B, N, elem_type=torch.float64))
         assert np.array_equal(as_int(C), oracle.matmul(A, B, N))
     finally:
-        autotune.apply()
-    ws = ctypes.c_size_t(0)
-    assert L.gffm_matmul_limb_workspace_size(m, n, k, N, ctypes.byref(ws)) == 0
-    assert ws.value == ws7.value or autotune.load_table().get("gemm")
+        autotune.apply()                                  # back to the shipped table
     status_ok(gffm)
 
 
 def test_limb_tuning_errors(gffm):
     A = gffm.CuModMatrix([[1, 2], [3, 4]], 7, elem_type=torch.float64)
     with pytest.raises(gffm.GFFMError) as ei:
-        gffm.mat_mul_gpu_type(A, A, method="limb", tuning=gffm.LimbTuning(9, 0))
+        gffm.mat_mul_gpu_type(A, A, method="limb", tuning=gffm.LimbTuning(9, 0, 0, 0))
     assert ei.value.status == 1
     with pytest.raises(gffm.GFFMError) as ei:
-        gffm.mat_mul_gpu_type(A, A, method="limb", tuning=gffm.LimbTuning(7, -1))
+        gffm.mat_mul_gpu_type(A, A, method="limb", tuning=gffm.LimbTuning(7, -1, 0, 0))
     assert ei.value.status == 1
+
+
+@pytest.mark.parametrize("N", [7, 16255, 65521, 8388593, P26])
+@pytest.mark.parametrize("bits", [7, 8])
+@pytest.mark.parametrize("shape", [(130, 200, 128), (129, 65, 1025), (300, 70, 5000)], ids=lambda s: "x".join(map(str, s)))
+def test_limb_gemm_32_column_tiles(gffm, N, bits, shape):
+    """The 32-column tile with two accumulator sets (a tuner candidate) is exact too."""
+    rng = np.random.default_rng(N + bits + shape[2])
+    m, n, k = shape
+    tu = gffm.LimbTuning(bits, 0, 32, 0)
+    for name, A, B in patterns(rng, N, m, n, k):
+        got = as_int(gffm.mat_mul_gpu_type(gffm.CuModMatrix(A, N, elem_type=torch.float64),
+                                           gffm.CuModMatrix(B, N, elem_type=torch.float64), method="limb", tuning=tu))
+        want = oracle.matmul(A, B, N)
+        assert np.array_equal(got, want), "%s: %d mismatches" % (name, int((got != want).sum()))
+    status_ok(gffm)
