@@ -442,9 +442,7 @@ def pluq_run(args, L, sp, dev):
     import oracle
     from gffm import elimination
     out = {"limb": elimination.bench_pluq(args.pluq, sp, dev, reps=2)}
-    if args.only == "pluq":
-        return out
-    if not args.no_pluq_plain:
+    if not args.no_pluq_plain and args.only != "pluq":
         out["plain"] = elimination.bench_pluq(args.pluq, sp, dev, reps=1, method="plain", warmup=0)
         out["limb_speedup"] = round(out["plain"]["seconds"] / out["limb"]["seconds"], 1)
     # 1024 x 1024 of rank 900: (1024 x 900)(900 x 1024) mod p26, seeded

@@ -396,6 +396,12 @@ __global__ void __launch_bounds__(PQ_THREADS, 2) k_pluq_batched(PQArgs a) {
                 if (lr >= t) LW[(int64_t)(r0 + lr) * ldlw + c0 + t] = lr == t ? (int32_t)S.piv_val[t] : P[t * rs + lr];
             }
             __syncthreads();
+            // the multipliers, negated once for the substitution and the update: N - l (N for l = 0,
+            // which adds a multiple of N)
+            for (int idx = tid; idx < R * npiv; idx += blockDim.x) {
+                const int t = idx / R, lr = idx - t * R;
+                if (lr > t) P[t * rs + lr] = (int32_t)(N - (uint32_t)P[t * rs + lr]);
+            }
             if (npiv > 0) {
                 // the rows the panel's swaps moved, outside the panel: trailing columns (moves
                 // only; their scaling comes with the substitution below), L inside its swap
@@ -444,14 +450,14 @@ __global__ void __launch_bounds__(PQ_THREADS, 2) k_pluq_batched(PQArgs a) {
                     for (int t = 0; t < npiv; t++) {
                         uint64_t acc0 = (uint32_t)Us[t * PQ_CW + tid], acc1 = 0, acc2 = 0, acc3 = 0;
                         int s2 = 0;
-                        for (; s2 + 4 <= t; s2 += 4) {
-                            acc0 += (uint64_t)(N - (uint32_t)P[s2 * rs + t]) * (uint32_t)Us[s2 * PQ_CW + tid];
-                            acc1 += (uint64_t)(N - (uint32_t)P[(s2 + 1) * rs + t]) * (uint32_t)Us[(s2 + 1) * PQ_CW + tid];
-                            acc2 += (uint64_t)(N - (uint32_t)P[(s2 + 2) * rs + t]) * (uint32_t)Us[(s2 + 2) * PQ_CW + tid];
-                            acc3 += (uint64_t)(N - (uint32_t)P[(s2 + 3) * rs + t]) * (uint32_t)Us[(s2 + 3) * PQ_CW + tid];
+                        for (; s2 + 4 <= t; s2 += 4) {      // P holds the negated multipliers
+                            acc0 += (uint64_t)(uint32_t)P[s2 * rs + t] * (uint32_t)Us[s2 * PQ_CW + tid];
+                            acc1 += (uint64_t)(uint32_t)P[(s2 + 1) * rs + t] * (uint32_t)Us[(s2 + 1) * PQ_CW + tid];
+                            acc2 += (uint64_t)(uint32_t)P[(s2 + 2) * rs + t] * (uint32_t)Us[(s2 + 2) * PQ_CW + tid];
+                            acc3 += (uint64_t)(uint32_t)P[(s2 + 3) * rs + t] * (uint32_t)Us[(s2 + 3) * PQ_CW + tid];
                         }
                         for (; s2 < t; s2++)
-                            acc0 += (uint64_t)(N - (uint32_t)P[s2 * rs + t]) * (uint32_t)Us[s2 * PQ_CW + tid];
+                            acc0 += (uint64_t)(uint32_t)P[s2 * rs + t] * (uint32_t)Us[s2 * PQ_CW + tid];
                         const uint64_t acc = acc0 + acc1 + acc2 + acc3;
                         Us[t * PQ_CW + tid] = (int32_t)elim::mulmod(reduce_u64(acc, M), S.piv_inv[t], M);
                     }
@@ -461,45 +467,41 @@ __global__ void __launch_bounds__(PQ_THREADS, 2) k_pluq_batched(PQArgs a) {
                     int32_t *dst = W + (int64_t)(r0 + t) * ldw + cb;
                     for (int c = lane; c < cw; c += 32) dst[c] = Us[t * PQ_CW + c];
                 }
-                // rows below the pivots: W += (N - l) u over 4 x 4 tiles per thread, the tile's
+                // rows below the pivots: W += (N - l) u over 4 x 8 tiles per thread, the tile's
                 // W values fetched before the product loop; tiles start at a multiple of 4
                 // rows so the panel and pivot-row reads are 16-byte vectors
                 const int lr_base = npiv & ~3;
-                const int trows = (R - lr_base + 3) >> 2, tcols = (cw + 3) >> 2;
+                const int trows = (R - lr_base + 3) >> 2, tcols = (cw + 7) >> 3;
                 for (int tile = tid; tile < trows * tcols; tile += blockDim.x) {
                     const int tc = tile / trows, tr = tile - tc * trows;
-                    const int lr0 = lr_base + 4 * tr, cc0 = 4 * tc;
-                    uint32_t wv[4][4];
+                    const int lr0 = lr_base + 4 * tr, cc0 = 8 * tc;
+                    uint64_t acc[4][8];
 #pragma unroll
                     for (int x = 0; x < 4; x++) {
                         const bool rok = lr0 + x >= npiv && lr0 + x < R;
                         const int32_t *wrow = W + (int64_t)(r0 + lr0 + x) * ldw + cb + cc0;
 #pragma unroll
-                        for (int y = 0; y < 4; y++) wv[x][y] = (rok && cc0 + y < cw) ? (uint32_t)wrow[y] : 0u;
+                        for (int y = 0; y < 8; y++) acc[x][y] = (rok && cc0 + y < cw) ? (uint32_t)wrow[y] : 0u;
                     }
-                    uint64_t acc[4][4];
-#pragma unroll
-                    for (int x = 0; x < 4; x++)
-#pragma unroll
-                        for (int y = 0; y < 4; y++) acc[x][y] = wv[x][y];
 #pragma unroll 2
                     for (int t = 0; t < npiv; t++) {
-                        const int4 lq = *reinterpret_cast<const int4 *>(P + t * rs + lr0);
-                        const int4 uq = *reinterpret_cast<const int4 *>(Us + t * PQ_CW + cc0);
-                        const uint32_t lv[4] = {N - (uint32_t)lq.x, N - (uint32_t)lq.y, N - (uint32_t)lq.z,
-                                                N - (uint32_t)lq.w};
-                        const uint32_t uv[4] = {(uint32_t)uq.x, (uint32_t)uq.y, (uint32_t)uq.z, (uint32_t)uq.w};
+                        const int4 lq = *reinterpret_cast<const int4 *>(P + t * rs + lr0);   // negated multipliers
+                        const int4 u0 = *reinterpret_cast<const int4 *>(Us + t * PQ_CW + cc0);
+                        const int4 u1 = *reinterpret_cast<const int4 *>(Us + t * PQ_CW + cc0 + 4);
+                        const uint32_t lv[4] = {(uint32_t)lq.x, (uint32_t)lq.y, (uint32_t)lq.z, (uint32_t)lq.w};
+                        const uint32_t uv[8] = {(uint32_t)u0.x, (uint32_t)u0.y, (uint32_t)u0.z, (uint32_t)u0.w,
+                                                (uint32_t)u1.x, (uint32_t)u1.y, (uint32_t)u1.z, (uint32_t)u1.w};
 #pragma unroll
                         for (int x = 0; x < 4; x++)
 #pragma unroll
-                            for (int y = 0; y < 4; y++) acc[x][y] += (uint64_t)lv[x] * uv[y];
+                            for (int y = 0; y < 8; y++) acc[x][y] += (uint64_t)lv[x] * uv[y];
                     }
 #pragma unroll
                     for (int x = 0; x < 4; x++) {
                         if (lr0 + x >= npiv && lr0 + x < R) {
                             int32_t *wrow = W + (int64_t)(r0 + lr0 + x) * ldw + cb + cc0;
 #pragma unroll
-                            for (int y = 0; y < 4; y++)
+                            for (int y = 0; y < 8; y++)
                                 if (cc0 + y < cw) wrow[y] = (int32_t)reduce_u64(acc[x][y], M);
                         }
                     }

@@ -111,6 +111,31 @@ __global__ void k_colswap(int32_t *W, int64_t ldw, int m, int c1, int c2) {
     W[(int64_t)i * ldw + c2] = x;
 }
 
+// *flag = 1 if any W[r][c] != 0 for r >= r0, c >= c0 (flag zeroed by the caller)
+__global__ void __launch_bounds__(256) k_any_nonzero(const int32_t *__restrict__ W, int64_t ldw, int r0, int m, int c0,
+                                                     int n, int *flag) {
+    const int64_t cols = n - c0;
+    const int64_t total = (int64_t)(m - r0) * cols;
+    int found = 0;
+    for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+         idx += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = idx / cols, c = idx - r * cols;
+        found |= W[(int64_t)(r0 + r) * ldw + c0 + c] != 0;
+    }
+    if (__syncthreads_or(found) && threadIdx.x == 0) atomicExch(flag, 1);
+}
+
+// W[r][c0 + j] <- W[r][src[j]] for every row r and j < ncols: a column permutation of
+// [c0, c0 + ncols), one row per block through shared memory
+__global__ void __launch_bounds__(256) k_permute_cols(int32_t *__restrict__ W, int64_t ldw, int c0, int ncols,
+                                                      const int32_t *__restrict__ src) {
+    extern __shared__ int32_t rowbuf[];
+    int32_t *w = W + (int64_t)blockIdx.x * ldw;
+    for (int j = threadIdx.x; j < ncols; j += blockDim.x) rowbuf[j] = w[c0 + j];
+    __syncthreads();
+    for (int j = threadIdx.x; j < ncols; j += blockDim.x) w[c0 + j] = rowbuf[src[j] - c0];
+}
+
 // U (column-major) from W: multipliers below each pivot become 0.
 template <typename T>
 __global__ void __launch_bounds__(256) k_extract_u(const int32_t *__restrict__ W, int64_t ldw, int m, int n,
@@ -558,6 +583,43 @@ static int forward(Work &w, int m, int n, int64_t N, int mode, int lcols, cudaSt
         if (status == PS_BOUNDS)
             return set_error(GFFM_ERR_BOUNDS, "pluq: pivot column %d is outside L's padded width %d (the reference "
                                               "raises a BoundsError here)", col + 1, lcols);
+        if (status == PS_ZERO_COL && t == 0 && row < m) {
+            // A zero column with nothing eliminated: if everything below `row` is zero (a
+            // rank-deficient tail) every remaining column is a zero column -- finish in one
+            // step: the swap sequence (col, last), (col+1, last), ... as one permutation.
+            const int ncols = n - col;
+            if ((size_t)ncols * 4 <= 200 * 1024) {
+                GFFM_CUDA(cudaMemsetAsync(w.result, 0, sizeof(int), s));
+                const int64_t total = (int64_t)(m - row) * ncols;
+                const unsigned blocks = (unsigned)std::min<int64_t>((total + 255) / 256, 4 * sm_count());
+                k_any_nonzero<<<blocks, 256, 0, s>>>(w.W, w.ldw, row, m, col, n, w.result);
+                GFFM_LAUNCH_CHECK("k_any_nonzero");
+                int nz = 1;
+                GFFM_CUDA(cudaMemcpyAsync(&nz, w.result, sizeof(int), cudaMemcpyDeviceToHost, s));
+                GFFM_CUDA(cudaStreamSynchronize(s));
+                if (!nz) {
+                    if (mode == MODE_PLUQ) {
+                        std::vector<int32_t> src(ncols);
+                        for (int j = 0; j < ncols; j++) src[j] = col + j;
+                        for (int c = col; c <= last; c++) {
+                            std::swap(src[c - col], src[last - col]);
+                            res.col_swaps.push_back(c + 1);
+                            res.col_swaps.push_back(last + 1);
+                            skipped.push_back(c);
+                        }
+                        GFFM_CUDA(cudaMemcpyAsync(w.qlist, src.data(), ncols * sizeof(int32_t),
+                                                  cudaMemcpyHostToDevice, s));
+                        GFFM_CUDA(cudaFuncSetAttribute(k_permute_cols, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                       ncols * 4));
+                        k_permute_cols<<<m, 256, (size_t)ncols * 4, s>>>(w.W, w.ldw, col, ncols, w.qlist);
+                        GFFM_LAUNCH_CHECK("k_permute_cols");
+                        GFFM_CUDA(cudaStreamSynchronize(s));     // src outlives the copy
+                    }
+                    col = n;
+                    continue;
+                }
+            }
+        }
         if (status == PS_ZERO_COL && t == 0) {
             if (mode == MODE_PLUQ) {
                 // find_pivot: swap the zero column with the last column, push (col, cols), skip
