@@ -136,6 +136,17 @@ __global__ void __launch_bounds__(256) k_permute_cols(int32_t *__restrict__ W, i
     for (int j = threadIdx.x; j < ncols; j += blockDim.x) w[c0 + j] = rowbuf[src[j] - c0];
 }
 
+// [A | I] (n x 2n, column-major, ld) from A (n x n, column-major, lda)
+template <typename T>
+__global__ void __launch_bounds__(256) k_build_augmented(const T *__restrict__ A, int64_t lda, int n, T *__restrict__ X,
+                                                         int64_t ld) {
+    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t total = (int64_t)n * 2 * n;
+    if (idx >= total) return;
+    const int64_t c = idx / n, r = idx - c * n;
+    X[r + c * ld] = c < n ? A[r + c * lda] : (T)(c - n == r ? 1 : 0);
+}
+
 // U (column-major) from W: multipliers below each pivot become 0.
 template <typename T>
 __global__ void __launch_bounds__(256) k_extract_u(const int32_t *__restrict__ W, int64_t ldw, int m, int n,
@@ -741,6 +752,9 @@ int pluq(int64_t m, int64_t n, const T *A, int64_t lda, T *U, int64_t ldu, T *L,
     if (mode == MODE_PLUQ && (!row_swaps || !n_row_swaps || !col_swaps || !n_col_swaps))
         return set_error(GFFM_ERR_ARG, "swap stack buffers are NULL");
     if (mode == MODE_LU && !perm) return set_error(GFFM_ERR_ARG, "perm is NULL");
+    if (mode == MODE_RREF && !is_prime_u32((uint32_t)N))
+        return set_error(GFFM_ERR_NOT_PRIME, "the reduced row echelon form needs a prime modulus (%lld is composite)",
+                         (long long)N);
     if ((m > 0 && n > 0) && (!A || !U)) return set_error(GFFM_ERR_ARG, "null data pointer");
     *rank = 0;
     if (n_row_swaps) *n_row_swaps = 0;
@@ -828,9 +842,74 @@ int pluq(int64_t m, int64_t n, const T *A, int64_t lda, T *U, int64_t ldu, T *L,
     return GFFM_OK;
 }
 
+// A^{-1} mod N from the reduced row echelon form of [A | I]: A is invertible exactly when
+// the pivots of the RREF are the first n columns, and then the right half is A^{-1}
+// (unique, so any elimination order gives the reference's result).
+template <typename T>
+int inverse(int64_t n, const T *A, int64_t lda, T *Ainv, int64_t ldi, int64_t N, int *invertible, void *ws,
+            size_t ws_bytes, gffm_stream_t stream) {
+    using namespace gffm;
+    if (!invertible) return set_error(GFFM_ERR_ARG, "invertible is NULL");
+    *invertible = 0;
+    if (n < 0) return set_error(GFFM_ERR_ARG, "negative size");
+    if (lda < std::max<int64_t>(n, 1) || ldi < std::max<int64_t>(n, 1))
+        return set_error(GFFM_ERR_ARG, "leading dimension smaller than the number of rows");
+    if (n == 0) {
+        *invertible = 1;
+        return GFFM_OK;
+    }
+    if (!A || !Ainv) return set_error(GFFM_ERR_ARG, "null data pointer");
+    int st = check_device();
+    if (st) return st;
+    cudaStream_t s = as_stream(stream);
+    const int64_t ld = n;
+    const size_t aug_bytes = gffm::round_up((int64_t)((size_t)n * 2 * n * sizeof(T)), 256);
+    const size_t el_bytes = workspace_bytes(n, 2 * n, 1);
+    Scratch scr;
+    st = scr.acquire(ws, ws_bytes, aug_bytes + el_bytes, s);
+    if (st) return st;
+    T *X = static_cast<T *>(scr.ptr);
+    void *ews = static_cast<uint8_t *>(scr.ptr) + aug_bytes;
+    const int64_t total = n * 2 * n;
+    k_build_augmented<T><<<(unsigned)((total + 255) / 256), 256, 0, s>>>(A, lda, (int)n, X, ld);
+    GFFM_LAUNCH_CHECK("k_build_augmented");
+    std::vector<int64_t> piv((size_t)n);
+    int64_t rank = 0;
+    st = pluq<T>(n, 2 * n, X, ld, X, ld, nullptr, 1, 0, N, piv.data(), nullptr, nullptr, nullptr, &rank, ews,
+                 el_bytes, stream, MODE_RREF, nullptr);
+    if (st) return st;
+    bool ok = rank >= n;
+    for (int64_t i = 0; ok && i < n; i++) ok = piv[(size_t)i] == i + 1;
+    if (ok) {
+        GFFM_CUDA(cudaMemcpy2DAsync(Ainv, (size_t)ldi * sizeof(T), X + n * ld, (size_t)ld * sizeof(T),
+                                    (size_t)n * sizeof(T), (size_t)n, cudaMemcpyDeviceToDevice, s));
+    }
+    *invertible = ok ? 1 : 0;
+    return GFFM_OK;
+}
+
 }  // namespace elim
 
 extern "C" {
+
+int gffm_inverse_workspace_size(int64_t n, size_t *bytes) {
+    if (!bytes) return gffm::set_error(GFFM_ERR_ARG, "bytes is NULL");
+    if (n < 0) return gffm::set_error(GFFM_ERR_ARG, "negative size");
+    *bytes = n == 0 ? 0
+                    : gffm::round_up((int64_t)((size_t)n * 2 * n * sizeof(double)), 256) +
+                          elim::workspace_bytes(n, 2 * n, 1);
+    return GFFM_OK;
+}
+
+int gffm_inverse_f64(int64_t n, const double *A, int64_t lda, double *Ainv, int64_t ldi, int64_t N, int *invertible,
+                     void *ws, size_t ws_bytes, gffm_stream_t s) {
+    return elim::inverse<double>(n, A, lda, Ainv, ldi, N, invertible, ws, ws_bytes, s);
+}
+
+int gffm_inverse_f32(int64_t n, const float *A, int64_t lda, float *Ainv, int64_t ldi, int64_t N, int *invertible,
+                     void *ws, size_t ws_bytes, gffm_stream_t s) {
+    return elim::inverse<float>(n, A, lda, Ainv, ldi, N, invertible, ws, ws_bytes, s);
+}
 
 int gffm_elim_workspace_size(int64_t m, int64_t n, int64_t l_cols, size_t *bytes) {
     if (!bytes) return gffm::set_error(GFFM_ERR_ARG, "bytes is NULL");

@@ -17,6 +17,7 @@ from .cumod import (  # noqa: F401
 from .elimination import (  # noqa: F401,E402
     pluq_gpu_kernel, lu_gpu_type, rref_gpu_type, apply_col_perm_, apply_col_inv_perm_, apply_col_perm,
     apply_row_perm_, apply_row_inv_perm_, apply_row_perm, perm_array_to_matrix,
+    inverse, is_invertible, is_invertible_with_inverse, MatrixNotInvertibleException,
 )
 from . import cumod as _cumod, karatsuba as _karatsuba  # noqa: E402
 from .karatsuba import (  # noqa: F401,E402

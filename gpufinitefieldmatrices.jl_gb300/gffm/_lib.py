@@ -73,6 +73,9 @@ SIGNATURES.update({
     "gffm_tune_table_size": (_INT, [_PI64]),
     "gffm_matmul_limb_tuned_workspace_size": (_INT, [_I64, _I64, _I64, _I64, _P, _PSZ]),
     "gffm_matmul_limb_tuned_f64": (_INT, [_I64, _I64, _I64, _P, _I64, _P, _I64, _P, _I64, _I64, _P, _P, _SZ, _P]),
+    "gffm_inverse_workspace_size": (_INT, [_I64, _PSZ]),
+    "gffm_inverse_f64": (_INT, [_I64, _P, _I64, _P, _I64, _I64, _P, _P, _SZ, _P]),
+    "gffm_inverse_f32": (_INT, [_I64, _P, _I64, _P, _I64, _I64, _P, _P, _SZ, _P]),
     "gffm_batched_plan_create": (_INT, [_P, _I64, _P, _P]),
     "gffm_batched_plan_info": (_INT, [_P, _PI64]),
     "gffm_batched_run": (_INT, [_P, _P]),

@@ -12,8 +12,18 @@ import ctypes
 import numpy as np
 import torch
 
-from ._lib import call
-from .cumod import CuModArray, TILE_WIDTH, _ptr, _sfx, _stream, zeros
+from ._lib import GFFMError, call
+from .cumod import CuModArray, CuModMatrixModulusNotPrimeException, TILE_WIDTH, _ptr, _sfx, _stream, zeros
+
+
+def _call_prime(name, *args):
+    """A call defined over prime fields: status 9 becomes CuModMatrixModulusNotPrimeException."""
+    try:
+        return call(name, *args)
+    except GFFMError as e:
+        if e.status == 9:
+            raise CuModMatrixModulusNotPrimeException(str(e)) from None
+        raise
 
 
 def _swaps_buf(P):
@@ -85,11 +95,52 @@ def rref_gpu_type(A, mod_N=-1, return_pivots=False):
     R = CuModArray(torch.zeros_like(A.data), (rows, cols), N)
     piv = np.zeros(max(min(rows, cols), 1), dtype=np.int64)
     rk = ctypes.c_int64(0)
-    call("gffm_rref_" + _sfx(A.dtype), rows, cols, _ptr(A.data), A.ld, _ptr(R.data), R.ld, N, ctypes.byref(rk),
+    _call_prime("gffm_rref_" + _sfx(A.dtype), rows, cols, _ptr(A.data), A.ld, _ptr(R.data), R.ld, N, ctypes.byref(rk),
          piv.ctypes.data_as(ctypes.c_void_p), None, 0, _stream())
     if return_pivots:
         return R, rk.value, [int(p) for p in piv[:rk.value]]
     return R
+
+
+# -- inverse / invertibility (CuModMatrix.jl:335-502) ---------------------------
+class MatrixNotInvertibleException(Exception):
+    pass
+
+
+def _inverse(A):
+    from .cumod import CuModMatrixNotSquareException
+    if A.ndim != 2 or A.rows() != A.cols():
+        raise CuModMatrixNotSquareException("Matrix must be square to be inverted")
+    n = A.rows()
+    Ainv = zeros(A.dtype, n, n, A.N)
+    ok = ctypes.c_int(0)
+    _call_prime("gffm_inverse_" + _sfx(A.dtype), n, _ptr(A.data), A.ld, _ptr(Ainv.data), Ainv.ld, A.N,
+                ctypes.byref(ok), None, 0, _stream())
+    return bool(ok.value), Ainv
+
+
+def is_invertible_with_inverse(A, debug=False):
+    """is_invertible_with_inverse(A) -> (true, A^-1) or (false, None) (CuModMatrix.jl:356-422).
+
+    Invertibility is decided by the elimination's exact pivot count (the reference
+    computes a floating-point rank of U on the host)."""
+    ok, Ainv = _inverse(A)
+    return (True, Ainv) if ok else (False, None)
+
+
+def is_invertible(A):
+    """is_invertible(A) (CuModMatrix.jl:460-465): full rank mod N."""
+    if A.ndim == 2 and A.rows() == A.cols():
+        return _inverse(A)[0]
+    return pluq_rank(A) == min(A.size)
+
+
+def inverse(A):
+    """inverse(A) (CuModMatrix.jl:480-502): A^-1 mod N, or MatrixNotInvertibleException."""
+    ok, Ainv = _inverse(A)
+    if not ok:
+        raise MatrixNotInvertibleException("Matrix is not invertible mod %d" % A.N)
+    return Ainv
 
 
 # -- permutations.jl -----------------------------------------------------------

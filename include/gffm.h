@@ -229,13 +229,26 @@ GFFM_API int gffm_lu_f32(int64_t m, int64_t n, const float *A, int64_t lda, floa
 /* rref_gpu_type(A) (intended API, test/Experiments/rref_gpu_type.jl:8-51;
  * called by test/CuModMatrix/benchmark_test.jl:144): the reduced row echelon
  * form mod N into R (unique for prime N).  pivot_cols (host, capacity
- * min(m, n) int64, may be NULL) receives the 1-based pivot columns. */
+ * min(m, n) int64, may be NULL) receives the 1-based pivot columns.
+ * GFFM_ERR_NOT_PRIME for a composite N (the form is defined over a field). */
 GFFM_API int gffm_rref_f64(int64_t m, int64_t n, const double *A, int64_t lda, double *R, int64_t ldr, int64_t N,
                            int64_t *rank, int64_t *pivot_cols, void *workspace, size_t workspace_bytes,
                            gffm_stream_t stream);
 GFFM_API int gffm_rref_f32(int64_t m, int64_t n, const float *A, int64_t lda, float *R, int64_t ldr, int64_t N,
                            int64_t *rank, int64_t *pivot_cols, void *workspace, size_t workspace_bytes,
                            gffm_stream_t stream);
+
+/* inverse(A) / is_invertible_with_inverse(A) (src/CuModMatrix/CuModMatrix.jl:356-422,
+ * 480-502): *invertible = 1 and Ainv = A^{-1} mod N when A (n x n) is invertible,
+ * else *invertible = 0 and Ainv untouched.  Computed from the RREF of [A | I] (the
+ * inverse is unique; the reference composes U^{-1} L^{-1} from PLUQ).  Synchronizes.
+ * GFFM_ERR_NOT_PRIME for a composite N.
+ * Workspace: gffm_inverse_workspace_size(n) bytes (Float32 needs at most that), or NULL. */
+GFFM_API int gffm_inverse_workspace_size(int64_t n, size_t *bytes);
+GFFM_API int gffm_inverse_f64(int64_t n, const double *A, int64_t lda, double *Ainv, int64_t ldi, int64_t N,
+                              int *invertible, void *workspace, size_t workspace_bytes, gffm_stream_t stream);
+GFFM_API int gffm_inverse_f32(int64_t n, const float *A, int64_t lda, float *Ainv, int64_t ldi, int64_t N,
+                              int *invertible, void *workspace, size_t workspace_bytes, gffm_stream_t stream);
 
 /* ---- swap-stack permutations (src/CuModMatrix/rref_lu_pluq/permutations.jl) --
  * A is nrows x ncols, column-major; `swaps` is a HOST array of nswaps 1-based

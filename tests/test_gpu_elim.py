@@ -235,3 +235,64 @@ def test_pluq_8192_reconstruction(gffm):
     for i in idx:
         assert (Uh[i, :i] == 0).all() and (Lh[i, i + 1:] == 0).all()
     status_ok(gffm)
+
+
+# ---- inverse / is_invertible / is_invertible_with_inverse (CuModMatrix.jl:335-502) ----
+def test_kat_inverse(gffm):
+    """The reference's known answers: de Rham 10 x 10 mod 7, the 6 x 6 identity mod 11, a singular 3 x 3."""
+    with open(os.path.join(HERE, "golden", "reference_kat.json")) as f:
+        cases = [c for c in json.load(f)["cases"] if c["op"] == "invertible"]
+    for c in cases:
+        A = gffm.CuModMatrix(np.array(c["A"]) % c["N"], c["N"], elem_type=torch.float64)
+        ok, Ainv = gffm.is_invertible_with_inverse(A)
+        assert ok == c["expected_invertible"], c["src"]
+        assert gffm.is_invertible(A) == c["expected_invertible"]
+        if ok:
+            prod = oracle.matmul(np.array(c["A"]) % c["N"], as_int(Ainv), c["N"])
+            assert prod.tolist() == c["expected_product_with_inverse"]
+        else:
+            with pytest.raises(gffm.MatrixNotInvertibleException):
+                gffm.inverse(A)
+    status_ok(gffm)
+
+
+@pytest.mark.parametrize("n,N", [(1, 7), (5, 7), (64, 65521), (130, 1000003), (300, P26), (1024, P25)])
+def test_inverse_random(gffm, n, N):
+    import pyref
+    rng = np.random.default_rng(n + N % 1000)
+    A = rng.integers(0, N, size=(n, n))
+    while n <= 64 and pyref.inverse_mod(A.tolist(), N) is None:      # small fields: draw an invertible one
+        A = rng.integers(0, N, size=(n, n))
+    Ag = gffm.CuModMatrix(A, N, elem_type=torch.float64)
+    Ainv = gffm.inverse(Ag)
+    Ah = as_int(Ainv)
+    x = rng.integers(0, N, size=(n, 2))
+    assert np.array_equal(oracle.matmul(A, oracle.matmul(Ah, x, N), N), x)   # A A^-1 x = x
+    if n <= 64:
+        assert Ah.tolist() == pyref.inverse_mod(A.tolist(), N)
+    # the negative power goes through the same inverse (CuModMatrix.jl:307-329)
+    if n <= 130:
+        assert np.array_equal(as_int(Ag ** -1), Ah)
+    status_ok(gffm)
+
+
+@pytest.mark.parametrize("kind,n,N", [("rank30", 40, 13), ("zeros", 5, 7), ("rank1", 64, P26)])
+def test_inverse_singular(gffm, kind, n, N):
+    A = make(kind, n, n, N, np.random.default_rng(n))
+    Ag = gffm.CuModMatrix(A, N, elem_type=torch.float64)
+    assert gffm.is_invertible_with_inverse(Ag) == (False, None)
+    assert not gffm.is_invertible(Ag)
+    with pytest.raises(gffm.MatrixNotInvertibleException):
+        gffm.inverse(Ag)
+    status_ok(gffm)
+
+
+def test_rref_and_inverse_need_a_prime(gffm):
+    """Over a composite modulus the echelon form and the inverse are not defined: the
+    reference's CuModMatrixModulusNotPrimeException, raised before any launch."""
+    A = gffm.CuModMatrix(np.eye(4, dtype=np.int64), 2080639, elem_type=torch.float64)   # 11 * 189149
+    with pytest.raises(gffm.CuModMatrixModulusNotPrimeException):
+        gffm.rref_gpu_type(A)
+    with pytest.raises(gffm.CuModMatrixModulusNotPrimeException):
+        gffm.inverse(A)
+    status_ok(gffm)
