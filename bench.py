@@ -463,6 +463,25 @@ def pluq_run(args, L, sp, dev):
         t[name + "_ms"] = round(best * 1e3, 3)
     t["rank"] = elimination.pluq_rank(A)
     out["rank900_1024"] = t
+    # the CPU elimination beside it: the oracle's exact restatement of the reference's
+    # step-by-step algorithm (one host thread) on the same 1024 x 1024 rank-900 matrix
+    Ah = oracle.matmul(X, Y, P26)
+    t0 = time.perf_counter()
+    oracle.pluq(Ah, P26)
+    cpu_s = time.perf_counter() - t0
+    out["rank900_1024"]["cpu_pluq_ms"] = round(cpu_s * 1e3, 1)
+    out["rank900_1024"]["cpu_kind"] = "port (oracle/or_pluq, 1 thread)"
+    # inverse of a 4096 x 4096 matrix mod p26 (RREF of [A | I]) and of the config-2 size
+    g = torch.Generator(device=dev)
+    g.manual_seed(41)
+    for n in (1024, 4096):
+        B = gffm.rand(torch.float64, n, n, P26, generator=g)
+        gffm.inverse(B)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        gffm.inverse(B)
+        torch.cuda.synchronize()
+        out["inverse_%d_ms" % n] = round((time.perf_counter() - t0) * 1e3, 2)
     return out
 
 
