@@ -80,7 +80,7 @@ __global__ void __launch_bounds__(PANEL_THREADS, 1) k_panel(PanelArgs a) {
     __shared__ unsigned long long red[PANEL_WARPS];
     __shared__ unsigned long long s_best;
     __shared__ int s_stop, s_status, s_prow, s_bw;
-    __shared__ uint32_t s_pv, s_inv, s_cinv;
+    __shared__ uint32_t s_inv, s_cinv;
     const int b = blockIdx.x, G = gridDim.x, tid = threadIdx.x;
     const int lane = tid & 31, wid = tid >> 5;
     const int rbeg = a.R0 + b * a.R;
@@ -187,7 +187,6 @@ __global__ void __launch_bounds__(PANEL_THREADS, 1) k_panel(PanelArgs a) {
                     s_stop = 1;
                     s_status = PS_BOUNDS;
                 } else {
-                    s_pv = pv;
                     s_prow = pkey_row(wk);
                     s_bw = wg;
                     s_inv = invs[wg];

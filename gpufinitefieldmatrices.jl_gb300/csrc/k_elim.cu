@@ -265,7 +265,6 @@ struct Work {
 static size_t al(size_t x) { return (x + 255) & ~size_t(255); }
 
 static void layout_ws(int64_t m, int64_t n, int64_t lcols, size_t *total, size_t off[16], limb::Layout *gl) {
-    const int G = 160;
     const int64_t ldw = gffm::round_up(n > 0 ? n : 1, 32);
     // digit planes large enough for any trailing update / back substitution of
     // this problem: operands n x NB and NB x m (4 digits)

@@ -161,7 +161,7 @@ int matmul_plain(int64_t m, int64_t n, int64_t k, const T *A, int64_t lda, const
     if (m < 0 || n < 0 || k < 0) return set_error(GFFM_ERR_ARG, "negative matrix size");
     if (lda < (m > 1 ? m : 1) || ldb < (k > 1 ? k : 1) || ldc < (m > 1 ? m : 1))
         return set_error(GFFM_ERR_ARG, "leading dimension smaller than the number of rows");
-    int64_t M;
+    int64_t M = 0;
     int st = resolve_stripe<T>(N, stripe, &M);
     if (st) return st;
     if (m == 0 || n == 0) return GFFM_OK;
@@ -183,7 +183,7 @@ int matvec_plain(int64_t m, int64_t k, const T *A, int64_t lda, const T *x, T *z
     using namespace gffm;
     if (m < 0 || k < 0) return set_error(GFFM_ERR_ARG, "negative size");
     if (lda < (m > 1 ? m : 1)) return set_error(GFFM_ERR_ARG, "leading dimension smaller than the number of rows");
-    int64_t M;
+    int64_t M = 0;
     int st = resolve_stripe<T>(N, stripe, &M);
     if (st) return st;
     if (m == 0) return GFFM_OK;

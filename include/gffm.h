@@ -80,7 +80,7 @@ GFFM_API int gffm_profile_next_kernel(void *start_event, void *stop_event);
  * before a reduction.  bits = 53 (Float64), 24 (Float32), 11 (Float16). */
 GFFM_API int gffm_find_max_stripe_ops(int bits, int64_t N, int64_t *out);
 
-/* ---- elementwise modular kernels (src/CuModMatrix/kernel_ops/*.jl) ----
+/* ---- elementwise modular kernels (the .jl files of src/CuModMatrix/kernel_ops) ----
  * All act on `len` contiguous elements -- the whole padded data array, as the
  * reference's grid-stride kernels do -- with Julia mod semantics (result in
  * [0, N)).  In-place use (C == A or C == B) is allowed. */
