@@ -11,18 +11,21 @@
 // L's width is the reference's BoundsError (status 8).
 //
 // Blocking.  The instance lives in global memory as a row-major int32 copy W
-// (and LW for L).  A panel of nb columns is copied into shared memory and
-// eliminated step by step there (pivot search, row swap, scaling and the
-// rank-1 updates restricted to the panel).  The rest of every row is brought
-// up to date once per panel: the panel's row swaps composed into one set of
-// row moves, then the pivot rows of the trailing columns by forward
-// substitution
-//     U[t][c] = inv_t * (W[t][c] - sum_{s<t} l[t][s] U[s][c]),
-// then the rows below by one K = nb product accumulated exactly in 64 bits
-// (products below 2^52, at most 32 of them) and reduced once.  Columns left of
-// the panel only see the moves and the pivot-row scaling (they matter for the
-// stale columns a zero-column swap leaves behind).  A zero column ends the
-// panel early: the pending updates are applied first, so the last column it is
+// (and LW for L).  A panel of nb <= 32 columns is copied into shared memory and
+// factored left-looking: column t is brought up to date only when the pivot
+// search reaches it, its values above the pivot rows by the inverse of the
+// panel's lower-triangular factor L' (pivots on the diagonal, multipliers l
+// below; its inverse Linv grows by one row per pivot) and the rows below by one
+// exact dot product each,
+//     U[0:t][t] = Linv W[0:t][t],      v[r] = W[r][t] - sum_{s<t} l[r][s] U[s][t],
+// 64-bit sums of at most 32 products below 2^52, reduced once.  The rest of
+// every row is brought up to date once per panel: the panel's row swaps
+// composed into one set of row moves, the pivot rows of the trailing columns
+// by the same Linv product, and the rows below by one K = nb product.  Columns
+// left of the panel only see the moves and the pivot-row scaling (they matter
+// for the stale columns a zero-column swap leaves behind).  A zero column ends
+// the panel; it is final at that point (zero below the pivot rows), and the
+// panel's columns after it join the trailing update, so the last column it is
 // swapped with is current.
 #pragma once
 
@@ -35,6 +38,8 @@ constexpr int PQ_THREADS = 256;
 constexpr int PQ_CW = 128;          // trailing columns per chunk
 constexpr int PQ_MAX_NB = 32;
 constexpr int PQ_MAX_MOVES = 2 * PQ_MAX_NB;
+constexpr int PQ_INV_WARP = 7;       // the warp that computes pivot inverses (the last one)
+static_assert(PQ_INV_WARP * 32 + 32 == PQ_THREADS, "the inverse warp is the CTA's last warp");
 
 struct PQInst {
     int m, n, l_cols, lsw;       // lsw = min(32*cld(m, 32), l_cols): L's row-swap width
@@ -78,7 +83,8 @@ struct PQShared {
     int mv_dst[PQ_MAX_MOVES], mv_src[PQ_MAX_MOVES];
     uint32_t mv_scale[PQ_MAX_MOVES];   // 0: plain move; else the pivot inverse of a pivot row
     unsigned long long red[PQ_THREADS / 32];
-    int nmv, inst, stop, zero_hit;
+    uint32_t inv;                // the pending pivot's inverse
+    int nmv, inst;
 };
 
 __device__ __forceinline__ uint32_t reduce_u64(uint64_t x, const elim::ModP &M) {
@@ -203,38 +209,19 @@ __device__ __forceinline__ void scatter_moves(int32_t *X, int ldx, int c_lo, int
     }
 }
 
-__device__ __forceinline__ unsigned long long pkey32(uint32_t v, int lr) {
-    return ((unsigned long long)v << 32) | (0xFFFFFFFFu - (uint32_t)lr);
+__device__ __forceinline__ void named_sync(int id, int nthreads) {
+    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
 }
 
-// Warp-wide: the pivot of panel column j from the lanes' best keys; lane 0 records
-// it (pivot row, value, inverse) as pivot number `t`, or flags a zero column, or the
-// reference's out-of-bounds L column.
-__device__ __forceinline__ void decide_pivot(unsigned long long best, int t, int r0, int j, int c0, int l_cols,
-                                             const elim::Mont &mont, PQShared &S) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        const unsigned long long other = __shfl_xor_sync(0xffffffffu, best, o);
-        best = other > best ? other : best;
-    }
-    if ((threadIdx.x & 31) == 0) {
-        const uint32_t pv = (uint32_t)(best >> 32);
-        if (pv == 0) {
-            S.zero_hit = 1;
-        } else if (c0 + j >= l_cols) {
-            S.stop = 8;              // the reference indexes L out of bounds here
-        } else {
-            S.piv_prow[t] = r0 + (int)(0xFFFFFFFFu - (uint32_t)(best & 0xFFFFFFFFu));
-            S.piv_val[t] = pv;
-            S.piv_inv[t] = elim::mod_inverse(pv, mont);
-        }
-    }
+__device__ __forceinline__ unsigned long long pkey32(uint32_t v, int lr) {
+    return ((unsigned long long)v << 32) | (0xFFFFFFFFu - (uint32_t)lr);
 }
 
 __global__ void __launch_bounds__(PQ_THREADS, 2) k_pluq_batched(PQArgs a) {
     extern __shared__ __align__(16) int32_t pq_smem[];
     __shared__ PQShared S;
-    __shared__ uint32_t s_u[PQ_MAX_NB], s_us[PQ_MAX_NB];   // scaled pivot row of the panel and its Shoup factors
+    __shared__ uint32_t Lv[PQ_MAX_NB * 33];   // Linv[t][s] at Lv[t * 33 + s], zero above the diagonal
+    __shared__ uint32_t s_ut[PQ_MAX_NB];      // the current column's values above its pivot rows
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int rs = a.rcap + 4;                        // panel column stride (words), a multiple of 4
     int32_t *P = pq_smem;                             // P[j * rs + lr]: panel column j, local row lr
@@ -272,81 +259,136 @@ __global__ void __launch_bounds__(PQ_THREADS, 2) k_pluq_batched(PQArgs a) {
                 const int lr = idx / nbc, j = idx - lr * nbc;
                 P[j * rs + lr] = W[(int64_t)(r0 + lr) * ldw + c0 + j];
             }
-            if (tid == 0) {
-                S.stop = 0;
-                S.zero_hit = 0;
-            }
             __syncthreads();
-            int npiv = 0;
-            // Warp 0 decides the pivot of column j (search, inverse) while the other warps
-            // finish the previous step's update of columns j+1.. : the inverse is off the
-            // critical path except for the panel's first column.
-            if (warp == 0) {
+            int npiv = 0, zero_hit = 0, stop = 0;
+            // Left-looking: column t is brought up to date only when it is reached.
+            //   above the pivot rows  U[s][t] = sum_{s' <= s} Linv[s][s'] P[t][s']       (s < t)
+            //   below                 v[lr]   = P[t][lr] + sum_{s < t} (N - l[lr][s]) U[s][t]
+            // Linv, the inverse of the panel's lower-triangular factor (the pivots on its
+            // diagonal, the multipliers below), grows by one row per pivot.  Columns left of t
+            // hold U above the diagonal, pv * inv on it and the negated multipliers below it.
+            // Pivot t-1 is applied while column t is prepared: warp 7 computes the pivot's
+            // inverse; meanwhile warp 0 swaps the rows and forms the sums that do not need it
+            // (Linv's new row before scaling, U[s][t] for s < t-1) and warps 0-6 the partial
+            // values y[lr] = P[t][lr] + sum_{s < t-1} (N - l[lr][s]) U[s][t]; once the inverse
+            // is known, v = y + (N - l[lr][t-1]) * inv * y[t-1].
+            uint32_t ppv = 0;     // pending pivot (value, local row); uniform over the block
+            int pplr = 0;
+            for (int t = 0;; t++) {
+                uint32_t g = 0;   // U[t-1][t]
+                if (t > 0) {
+                    const int tp = t - 1;
+                    const bool nxt = t < nbc && r0 + t < m;
+                    uint64_t lsum = 0;
+                    if (warp == PQ_INV_WARP) {
+                        const uint32_t inv = elim::mod_inverse(ppv, mont);
+                        if (lane == 0) S.inv = inv;
+                    } else {
+                        if (warp == 0) {
+                            if (lane < nbc) {
+                                int32_t *col = P + lane * rs;
+                                if (lane == tp) {
+                                    col[pplr] = col[tp];
+                                } else if (pplr != tp) {
+                                    const int32_t x = col[tp];
+                                    col[tp] = col[pplr];
+                                    col[pplr] = x;
+                                }
+                            }
+                            __syncwarp();
+                            if (nxt) {   // U[s][t] for s < t-1 (lanes past t-2: unused)
+                                uint64_t a0 = 0, a1 = 0;
+                                int s2 = 0;
+                                for (; s2 + 2 <= tp; s2 += 2) {
+                                    a0 += (uint64_t)Lv[lane * 33 + s2] * (uint32_t)P[t * rs + s2];
+                                    a1 += (uint64_t)Lv[lane * 33 + s2 + 1] * (uint32_t)P[t * rs + s2 + 1];
+                                }
+                                if (s2 < tp) a0 += (uint64_t)Lv[lane * 33 + s2] * (uint32_t)P[t * rs + s2];
+                                s_ut[lane] = reduce_u64(a0 + a1, M);
+                            }
+                            {   // Linv's row t-1 before the inverse: sum_{s' < t-1} (N - l[t-1][s']) Linv[s'][lane]
+                                uint64_t a0 = 0, a1 = 0;
+                                int s2 = 0;
+                                for (; s2 + 2 <= tp; s2 += 2) {
+                                    a0 += (uint64_t)(uint32_t)P[s2 * rs + tp] * Lv[s2 * 33 + lane];
+                                    a1 += (uint64_t)(uint32_t)P[(s2 + 1) * rs + tp] * Lv[(s2 + 1) * 33 + lane];
+                                }
+                                if (s2 < tp) a0 += (uint64_t)(uint32_t)P[s2 * rs + tp] * Lv[s2 * 33 + lane];
+                                lsum = a0 + a1;
+                            }
+                        }
+                        if (nxt) {
+                            named_sync(1, PQ_INV_WARP * 32);
+                            for (int lr = tp + tid; lr < R; lr += PQ_INV_WARP * 32) {
+                                uint64_t a0 = (uint32_t)P[t * rs + lr], a1 = 0;
+                                int s2 = 0;
+                                for (; s2 + 2 <= tp; s2 += 2) {
+                                    a0 += (uint64_t)(uint32_t)P[s2 * rs + lr] * s_ut[s2];
+                                    a1 += (uint64_t)(uint32_t)P[(s2 + 1) * rs + lr] * s_ut[s2 + 1];
+                                }
+                                if (s2 < tp) a0 += (uint64_t)(uint32_t)P[s2 * rs + lr] * s_ut[s2];
+                                P[t * rs + lr] = (int32_t)reduce_u64(a0 + a1, M);
+                            }
+                        }
+                    }
+                    __syncthreads();
+                    const uint32_t inv = S.inv;
+                    if (warp == 0) {
+                        Lv[tp * 33 + lane] =
+                            lane < tp ? elim::mulmod(reduce_u64(lsum, M), inv, M) : (lane == tp ? inv : 0u);
+                        if (lane == 0) {
+                            P[tp * rs + tp] = (int32_t)elim::mulmod(ppv, inv, M);   // U's diagonal
+                            S.piv_inv[tp] = inv;
+                        }
+                    }
+                    if (!nxt) break;
+                    g = elim::mulmod((uint32_t)P[t * rs + tp], inv, M);
+                    if (warp == 0 && lane == 0) s_ut[tp] = g;
+                }
+                // column t below its pivot rows, and its largest residue (lowest row on ties)
                 unsigned long long best = 0;
-                for (int lr = lane; lr < R; lr += 32) {
-                    const unsigned long long key = pkey32((uint32_t)P[lr], lr);
+                for (int lr = t + tid; lr < R; lr += PQ_THREADS) {
+                    uint32_t v = (uint32_t)P[t * rs + lr];
+                    if (t > 0) v = reduce_u64((uint64_t)v + (uint64_t)(uint32_t)P[(t - 1) * rs + lr] * g, M);
+                    P[t * rs + lr] = v ? (int32_t)(N - v) : 0;
+                    const unsigned long long key = pkey32(v, lr);
                     best = key > best ? key : best;
                 }
-                decide_pivot(best, 0, r0, 0, c0, l_cols, mont, S);
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) {
+                    const unsigned long long other = __shfl_xor_sync(0xffffffffu, best, o);
+                    best = other > best ? other : best;
+                }
+                if (lane == 0) S.red[warp] = best;
+                __syncthreads();
+                // every warp takes the same decision from the eight warp maxima
+                best = lane < PQ_THREADS / 32 ? S.red[lane] : 0ull;
+#pragma unroll
+                for (int o = 4; o > 0; o >>= 1) {
+                    const unsigned long long other = __shfl_xor_sync(0xffffffffu, best, o);
+                    best = other > best ? other : best;
+                }
+                best = __shfl_sync(0xffffffffu, best, 0);
+                const uint32_t pv = (uint32_t)(best >> 32);
+                // the column's values above the pivot rows are final either way
+                if (warp == 0 && lane < t) P[t * rs + lane] = (int32_t)s_ut[lane];
+                if (pv == 0) {
+                    zero_hit = 1;
+                    break;
+                }
+                if (c0 + t >= l_cols) {
+                    stop = 8;    // the reference indexes L out of bounds here
+                    break;
+                }
+                pplr = (int)(0xFFFFFFFFu - (uint32_t)(best & 0xFFFFFFFFu));
+                ppv = pv;
+                if (tid == 0) {
+                    S.piv_prow[t] = r0 + pplr;
+                    S.piv_val[t] = pv;
+                }
+                npiv = t + 1;
             }
             __syncthreads();
-            for (int j = 0; j < nbc; j++) {
-                if (S.zero_hit || S.stop) break;
-                const int plr = S.piv_prow[npiv] - r0;
-                const uint32_t inv = S.piv_inv[npiv];
-                // ---- swap panel rows npiv <-> plr over every panel column, scaling the pivot
-                //      row of the columns not eliminated yet ----
-                for (int jj = tid; jj < nbc; jj += blockDim.x) {
-                    const int32_t x = P[jj * rs + plr];
-                    const int32_t y = P[jj * rs + npiv];
-                    P[jj * rs + plr] = y;
-                    if (jj >= j) {
-                        const uint32_t u = elim::mulmod((uint32_t)x, inv, M);
-                        P[jj * rs + npiv] = (int32_t)u;
-                        s_u[jj] = u;
-                        s_us[jj] = elim::shoup_pre(u, M);
-                    } else {
-                        P[jj * rs + npiv] = x;
-                    }
-                }
-                __syncthreads();
-                npiv++;
-                const bool more = j + 1 < nbc && r0 + npiv < m;
-                if (warp == 0) {
-                    // column j+1 first, then its pivot
-                    unsigned long long best = 0;
-                    if (more) {
-                        for (int lr = npiv + lane; lr < R; lr += 32) {
-                            const uint32_t l = (uint32_t)P[j * rs + lr];
-                            uint32_t v = (uint32_t)P[(j + 1) * rs + lr];
-                            if (l) {
-                                v += elim::shoup_mul(N - l, s_u[j + 1], s_us[j + 1], N);
-                                v = v >= N ? v - N : v;
-                                P[(j + 1) * rs + lr] = (int32_t)v;
-                            }
-                            const unsigned long long key = pkey32(v, lr);
-                            best = key > best ? key : best;
-                        }
-                        decide_pivot(best, npiv, r0, j + 1, c0, l_cols, mont, S);
-                    }
-                } else {
-                    // columns j+2 .. of the panel, rows below the pivot
-                    const int nw = blockDim.x - 32;
-                    for (int lr = npiv + tid - 32; lr < R; lr += nw) {
-                        const uint32_t l = (uint32_t)P[j * rs + lr];
-                        if (!l) continue;
-                        const uint32_t nl = N - l;
-                        for (int jj = j + 2; jj < nbc; jj++) {
-                            const uint32_t v = (uint32_t)P[jj * rs + lr] + elim::shoup_mul(nl, s_u[jj], s_us[jj], N);
-                            P[jj * rs + lr] = (int32_t)(v >= N ? v - N : v);
-                        }
-                    }
-                }
-                __syncthreads();
-                if (!more) break;
-            }
-            const int zero_hit = S.zero_hit;
-            const int stop = S.stop;
             // ---- compose the panel's swaps into row moves (local rows; `at` and the marks in Us) ----
             if (tid == 0) {
                 int *at = Us;                       // at[lr]: local row whose content sits at lr
@@ -393,18 +435,15 @@ __global__ void __launch_bounds__(PQ_THREADS, 2) k_pluq_batched(PQArgs a) {
             // ---- L: this panel's columns (pivot, then the multipliers as swapped so far) ----
             for (int idx = tid; idx < R * npiv; idx += blockDim.x) {
                 const int lr = idx / npiv, t = idx - lr * npiv;
-                if (lr >= t) LW[(int64_t)(r0 + lr) * ldlw + c0 + t] = lr == t ? (int32_t)S.piv_val[t] : P[t * rs + lr];
+                if (lr >= t) {
+                    const uint32_t x = (uint32_t)P[t * rs + lr];   // negated multiplier
+                    LW[(int64_t)(r0 + lr) * ldlw + c0 + t] = (int32_t)(lr == t ? S.piv_val[t] : (x ? N - x : 0u));
+                }
             }
             __syncthreads();
-            // the multipliers, negated once for the substitution and the update: N - l (N for l = 0,
-            // which adds a multiple of N)
-            for (int idx = tid; idx < R * npiv; idx += blockDim.x) {
-                const int t = idx / R, lr = idx - t * R;
-                if (lr > t) P[t * rs + lr] = (int32_t)(N - (uint32_t)P[t * rs + lr]);
-            }
             if (npiv > 0) {
                 // the rows the panel's swaps moved, outside the panel: trailing columns (moves
-                // only; their scaling comes with the substitution below), L inside its swap
+                // only; their scaling comes with the Linv product below), L inside its swap
                 // width, and -- only once a zero column has been skipped, the one way a column
                 // left of the panel holds non-zeros below its pivot row -- the left columns
                 // with the pivot-row scaling
@@ -437,8 +476,9 @@ __global__ void __launch_bounds__(PQ_THREADS, 2) k_pluq_batched(PQArgs a) {
                 }
             }
             __syncthreads();
-            // ---- trailing columns: pivot rows by substitution, rows below by one product ----
-            const int ct0 = c0 + nbc;
+            // ---- trailing columns: pivot rows by the Linv product, rows below by one product ----
+            // (a zero column that ended the panel is final already)
+            const int ct0 = c0 + npiv + (zero_hit ? 1 : 0);
             for (int cb = ct0; npiv > 0 && cb < n; cb += PQ_CW) {
                 const int cw = min(PQ_CW, n - cb);
                 for (int t = warp; t < npiv; t += PQ_THREADS / 32) {
@@ -446,20 +486,37 @@ __global__ void __launch_bounds__(PQ_THREADS, 2) k_pluq_batched(PQArgs a) {
                     for (int c = lane; c < cw; c += 32) Us[t * PQ_CW + c] = src[c];
                 }
                 __syncthreads();
-                if (tid < cw) {
-                    for (int t = 0; t < npiv; t++) {
-                        uint64_t acc0 = (uint32_t)Us[t * PQ_CW + tid], acc1 = 0, acc2 = 0, acc3 = 0;
-                        int s2 = 0;
-                        for (; s2 + 4 <= t; s2 += 4) {      // P holds the negated multipliers
-                            acc0 += (uint64_t)(uint32_t)P[s2 * rs + t] * (uint32_t)Us[s2 * PQ_CW + tid];
-                            acc1 += (uint64_t)(uint32_t)P[(s2 + 1) * rs + t] * (uint32_t)Us[(s2 + 1) * PQ_CW + tid];
-                            acc2 += (uint64_t)(uint32_t)P[(s2 + 2) * rs + t] * (uint32_t)Us[(s2 + 2) * PQ_CW + tid];
-                            acc3 += (uint64_t)(uint32_t)P[(s2 + 3) * rs + t] * (uint32_t)Us[(s2 + 3) * PQ_CW + tid];
+                {
+                    // U = Linv * (pivot rows) over 2 x 8 tiles: 16 row pairs x 16 column octets
+                    const int i0 = 2 * (tid & 15), cc0 = 8 * (tid >> 4);
+                    const bool act = i0 < npiv && cc0 < cw;
+                    uint64_t acc[2][8];
+#pragma unroll
+                    for (int y = 0; y < 8; y++) acc[0][y] = acc[1][y] = 0;
+                    if (act) {
+                        const int smax = min(i0 + 1, npiv - 1);
+                        for (int s2 = 0; s2 <= smax; s2++) {
+                            const uint32_t l0 = Lv[i0 * 33 + s2], l1 = Lv[(i0 + 1) * 33 + s2];
+                            const int4 u0 = *reinterpret_cast<const int4 *>(Us + s2 * PQ_CW + cc0);
+                            const int4 u1 = *reinterpret_cast<const int4 *>(Us + s2 * PQ_CW + cc0 + 4);
+                            const uint32_t uv[8] = {(uint32_t)u0.x, (uint32_t)u0.y, (uint32_t)u0.z, (uint32_t)u0.w,
+                                                    (uint32_t)u1.x, (uint32_t)u1.y, (uint32_t)u1.z, (uint32_t)u1.w};
+#pragma unroll
+                            for (int y = 0; y < 8; y++) {
+                                acc[0][y] += (uint64_t)l0 * uv[y];
+                                acc[1][y] += (uint64_t)l1 * uv[y];
+                            }
                         }
-                        for (; s2 < t; s2++)
-                            acc0 += (uint64_t)(uint32_t)P[s2 * rs + t] * (uint32_t)Us[s2 * PQ_CW + tid];
-                        const uint64_t acc = acc0 + acc1 + acc2 + acc3;
-                        Us[t * PQ_CW + tid] = (int32_t)elim::mulmod(reduce_u64(acc, M), S.piv_inv[t], M);
+                    }
+                    __syncthreads();
+                    if (act) {
+#pragma unroll
+                        for (int x = 0; x < 2; x++) {
+                            if (i0 + x >= npiv) break;
+#pragma unroll
+                            for (int y = 0; y < 8; y++)
+                                if (cc0 + y < cw) Us[(i0 + x) * PQ_CW + cc0 + y] = (int32_t)reduce_u64(acc[x][y], M);
+                        }
                     }
                 }
                 __syncthreads();
