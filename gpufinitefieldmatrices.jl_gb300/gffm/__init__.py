@@ -11,6 +11,7 @@ from .cumod import (  # noqa: F401
     add_, sub_, elementwise_multiply_, scalar_add_, scalar_sub_, rscalar_sub_, scalar_mul_, negate_,
     mod_, mod_elements_, fill_, zero_, copy_, change_modulus, change_modulus_no_alloc_,
     mul_, stripe_mul_, mat_mul_gpu_type, mat_mul_type_inplace_, find_max_stripe_ops, limbs_for, LimbTuning,
+    matmul_host, host_matrix,
     CuModArraySizeMismatchException, CuModArrayModulusMismatchException, CuModMatrixNotSquareException,
     CuModMatrixModulusNotPrimeException,
 )

@@ -47,6 +47,8 @@ SIGNATURES = {
     "gffm_apply_col_swaps_f32": (_INT, [_P, _I64, _I64, _I64, _P, _I64, _INT, _P]),
     "gffm_matmul_limb_static_max_bytes": (_INT, [_PSZ]),
     "gffm_matmul_limb_static_f64": (_INT, [_I64, _I64, _I64, _P, _I64, _P, _I64, _P, _I64, _I64, _P]),
+    "gffm_matmul_host_workspace_size": (_INT, [_I64, _I64, _I64, _I64, _PSZ]),
+    "gffm_matmul_host_f64": (_INT, [_I64, _I64, _I64, _P, _I64, _P, _I64, _P, _I64, _I64, _P, _SZ, _P]),
 }
 for _op in ("add", "sub", "mul_elementwise"):
     SIGNATURES["gffm_%s_f64" % _op] = (_INT, [_P, _P, _P, _I64, _I64, _P])

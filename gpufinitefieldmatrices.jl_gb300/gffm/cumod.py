@@ -450,6 +450,36 @@ def mat_mul_gpu_type(A, B, mod_N=-1, method="auto", tuning=None):
     return _gemm(C, A, B, N, method, tuning=tuning)
 
 
+def host_matrix(A, pinned=True):
+    """A host matrix (numpy array or CPU tensor of integer residues) as column-major
+    Float64 storage for gffm_matmul_host_f64: a CPU tensor of shape (cols, rows),
+    page-locked when ``pinned``."""
+    t = torch.as_tensor(A).to(torch.float64).t().contiguous()
+    return t.pin_memory() if pinned else t
+
+
+def matmul_host(A, B, N, pinned=True):
+    """C = A*B mod N for host matrices through gffm_matmul_host_f64 (the round trip
+    CuModMatrix(A, N) * CuModMatrix(B, N) |> Array of the reference, with the copies
+    overlapped with the block products).  A, B: numpy arrays or CPU tensors of
+    integer values; returns an int64 numpy array."""
+    A = np.asarray(A) if not torch.is_tensor(A) else A
+    B = np.asarray(B) if not torch.is_tensor(B) else B
+    m, k = A.shape
+    k2, n = B.shape
+    if k != k2:
+        raise CuModArraySizeMismatchException(
+            "Matrix dimensions do not match. A has %d rows and %d cols, B has %d rows and %d cols." % (m, k, k2, n))
+    hA, hB = host_matrix(A, pinned), host_matrix(B, pinned)
+    hC = torch.empty((n, m), dtype=torch.float64)
+    if pinned:
+        hC = hC.pin_memory()
+    call("gffm_matmul_host_f64", m, n, k, _ptr(hA), max(m, 1), _ptr(hB), max(k, 1), _ptr(hC), max(m, 1), N,
+         None, 0, _stream())
+    torch.cuda.current_stream().synchronize()
+    return hC.t().numpy().astype(np.int64)
+
+
 def mat_mul_type_inplace_(C, A, B, mod_N=-1, method="auto"):
     """mat_mul_type_inplace!(C, A, B, mod_N) (mat_mul_gpu_direct.jl:49-85), exact, without the debug print."""
     N = mod_N if mod_N > 0 else A.N

@@ -63,6 +63,20 @@ def test_host_side_argument_errors(lib):
     assert ws.value == 4 * (8192 + 8192) * 8192 * 2
 
 
+def test_host_gemm_workspace_and_argument_errors(lib):
+    """gffm_matmul_host_*: the workspace holds staging copies of A, B and C and the
+    digit planes of A's and B's blocks; bad sizes and moduli are refused on the host."""
+    ws = ctypes.c_size_t(0)
+    assert lib.gffm_matmul_host_workspace_size(8192, 8192, 8192, 67108859, ctypes.byref(ws)) == 0
+    staging = 3 * 8192 * 8192 * 8
+    digits = 2 * 4 * 8192 * 8192 * 2          # 4 fp16 digits per residue at this modulus
+    assert staging + digits <= ws.value <= staging + digits + 64 * 1024
+    assert lib.gffm_matmul_host_workspace_size(0, 5, 5, 7, ctypes.byref(ws)) == 0 and ws.value == 0
+    assert lib.gffm_matmul_host_f64(-1, 4, 4, None, 4, None, 4, None, 4, 7, None, 0, None) == 1
+    assert lib.gffm_matmul_host_f64(4, 4, 4, None, 4, None, 4, None, 4, 2 ** 26, None, 0, None) == 3
+    assert lib.gffm_matmul_host_f64(4, 4, 4, None, 3, None, 4, None, 4, 7, None, 0, None) == 1
+
+
 def test_tuning_structs_match_header():
     """ctypes layouts of gffm_limb_tuning, gffm_tune_entry, gffm_batch_tuning and gffm_batch_desc."""
     import ctypes
