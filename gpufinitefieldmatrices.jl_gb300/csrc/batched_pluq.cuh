@@ -217,6 +217,60 @@ __device__ __forceinline__ unsigned long long pkey32(uint32_t v, int lr) {
     return ((unsigned long long)v << 32) | (0xFFFFFFFFu - (uint32_t)lr);
 }
 
+// The trailing update's 4 x 4 tiles: item i covers rows lr0 .. lr0+3 (local) and
+// columns cc .. cc+3 of the current chunk, cc = 8 * (column octet) + 4 * (i & 1).
+struct UpdCtx {
+    int32_t *W;
+    int ldw, r0, cb, npiv, R, cw, lr_base, trows;
+    const int32_t *P;
+    int rs;
+    const int32_t *Us;
+};
+__device__ __forceinline__ void upd_pos(const UpdCtx &c, int item, int &lr0, int &cc) {
+    const int tile = item >> 1, tc = tile / c.trows, tr = tile - tc * c.trows;
+    lr0 = c.lr_base + 4 * tr;
+    cc = 8 * tc + 4 * (item & 1);
+}
+__device__ __forceinline__ void upd_load(uint64_t (&a)[4][4], const UpdCtx &c, int item) {
+    int lr0, cc;
+    upd_pos(c, item, lr0, cc);
+#pragma unroll
+    for (int x = 0; x < 4; x++) {
+        const bool rok = lr0 + x >= c.npiv && lr0 + x < c.R;
+        const int32_t *w = c.W + (int64_t)(c.r0 + lr0 + x) * c.ldw + c.cb + cc;
+#pragma unroll
+        for (int y = 0; y < 4; y++) a[x][y] = (rok && cc + y < c.cw) ? (uint32_t)w[y] : 0u;
+    }
+}
+__device__ __forceinline__ void upd_mul(uint64_t (&a)[4][4], const UpdCtx &c, int item) {
+    int lr0, cc;
+    upd_pos(c, item, lr0, cc);
+#pragma unroll 4
+    for (int t = 0; t < c.npiv; t++) {
+        const int4 lq = *reinterpret_cast<const int4 *>(c.P + t * c.rs + lr0);   // negated multipliers
+        const int4 uq = *reinterpret_cast<const int4 *>(c.Us + t * PQ_CW + cc);
+        const uint32_t lv[4] = {(uint32_t)lq.x, (uint32_t)lq.y, (uint32_t)lq.z, (uint32_t)lq.w};
+        const uint32_t uv[4] = {(uint32_t)uq.x, (uint32_t)uq.y, (uint32_t)uq.z, (uint32_t)uq.w};
+#pragma unroll
+        for (int x = 0; x < 4; x++)
+#pragma unroll
+            for (int y = 0; y < 4; y++) a[x][y] += (uint64_t)lv[x] * uv[y];
+    }
+}
+__device__ __forceinline__ void upd_store(const uint64_t (&a)[4][4], const UpdCtx &c, int item, const elim::ModP &M) {
+    int lr0, cc;
+    upd_pos(c, item, lr0, cc);
+#pragma unroll
+    for (int x = 0; x < 4; x++) {
+        if (lr0 + x >= c.npiv && lr0 + x < c.R) {
+            int32_t *w = c.W + (int64_t)(c.r0 + lr0 + x) * c.ldw + c.cb + cc;
+#pragma unroll
+            for (int y = 0; y < 4; y++)
+                if (cc + y < c.cw) w[y] = (int32_t)reduce_u64(a[x][y], M);
+        }
+    }
+}
+
 __global__ void __launch_bounds__(PQ_THREADS, 2) k_pluq_batched(PQArgs a) {
     extern __shared__ __align__(16) int32_t pq_smem[];
     __shared__ PQShared S;
@@ -524,44 +578,26 @@ __global__ void __launch_bounds__(PQ_THREADS, 2) k_pluq_batched(PQArgs a) {
                     int32_t *dst = W + (int64_t)(r0 + t) * ldw + cb;
                     for (int c = lane; c < cw; c += 32) dst[c] = Us[t * PQ_CW + c];
                 }
-                // rows below the pivots: W += (N - l) u over 4 x 8 tiles per thread, the tile's
-                // W values fetched before the product loop; tiles start at a multiple of 4
-                // rows so the panel and pivot-row reads are 16-byte vectors
+                // rows below the pivots: W += (N - l) u over 4 x 4 tiles, two per thread in
+                // flight: the W values of the next tile load while the current one multiplies.
+                // Tiles start at a multiple of 4 rows (16-byte panel and pivot-row reads).
                 const int lr_base = npiv & ~3;
-                const int trows = (R - lr_base + 3) >> 2, tcols = (cw + 7) >> 3;
-                for (int tile = tid; tile < trows * tcols; tile += blockDim.x) {
-                    const int tc = tile / trows, tr = tile - tc * trows;
-                    const int lr0 = lr_base + 4 * tr, cc0 = 8 * tc;
-                    uint64_t acc[4][8];
-#pragma unroll
-                    for (int x = 0; x < 4; x++) {
-                        const bool rok = lr0 + x >= npiv && lr0 + x < R;
-                        const int32_t *wrow = W + (int64_t)(r0 + lr0 + x) * ldw + cb + cc0;
-#pragma unroll
-                        for (int y = 0; y < 8; y++) acc[x][y] = (rok && cc0 + y < cw) ? (uint32_t)wrow[y] : 0u;
-                    }
-#pragma unroll 2
-                    for (int t = 0; t < npiv; t++) {
-                        const int4 lq = *reinterpret_cast<const int4 *>(P + t * rs + lr0);   // negated multipliers
-                        const int4 u0 = *reinterpret_cast<const int4 *>(Us + t * PQ_CW + cc0);
-                        const int4 u1 = *reinterpret_cast<const int4 *>(Us + t * PQ_CW + cc0 + 4);
-                        const uint32_t lv[4] = {(uint32_t)lq.x, (uint32_t)lq.y, (uint32_t)lq.z, (uint32_t)lq.w};
-                        const uint32_t uv[8] = {(uint32_t)u0.x, (uint32_t)u0.y, (uint32_t)u0.z, (uint32_t)u0.w,
-                                                (uint32_t)u1.x, (uint32_t)u1.y, (uint32_t)u1.z, (uint32_t)u1.w};
-#pragma unroll
-                        for (int x = 0; x < 4; x++)
-#pragma unroll
-                            for (int y = 0; y < 8; y++) acc[x][y] += (uint64_t)lv[x] * uv[y];
-                    }
-#pragma unroll
-                    for (int x = 0; x < 4; x++) {
-                        if (lr0 + x >= npiv && lr0 + x < R) {
-                            int32_t *wrow = W + (int64_t)(r0 + lr0 + x) * ldw + cb + cc0;
-#pragma unroll
-                            for (int y = 0; y < 8; y++)
-                                if (cc0 + y < cw) wrow[y] = (int32_t)reduce_u64(acc[x][y], M);
-                        }
-                    }
+                const int trows = (R - lr_base + 3) >> 2;
+                const int nitems = 2 * trows * ((cw + 7) >> 3);
+                const UpdCtx uc{W, ldw, r0, cb, npiv, R, cw, lr_base, trows, P, rs, Us};
+                uint64_t a0[4][4], a1[4][4];
+                int it = tid;
+                if (it < nitems) upd_load(a0, uc, it);
+                for (; it < nitems; it += 2 * PQ_THREADS) {
+                    const int it1 = it + PQ_THREADS;
+                    if (it1 < nitems) upd_load(a1, uc, it1);
+                    upd_mul(a0, uc, it);
+                    upd_store(a0, uc, it, M);
+                    if (it1 >= nitems) break;
+                    const int it2 = it1 + PQ_THREADS;
+                    if (it2 < nitems) upd_load(a0, uc, it2);
+                    upd_mul(a1, uc, it1);
+                    upd_store(a1, uc, it1, M);
                 }
                 __syncthreads();
             }

@@ -51,19 +51,29 @@ int streams_for(HostStreams *hs) {
 
 constexpr int64_t kAlign = 1024;
 
-// block sizes: rows of A in multiples of 128, columns of B in multiples of 64, about
-// 2048 each (a 2048 x 2048 product block is 512 output tiles, over three waves of SMs)
+// Block boundaries: rows of A in multiples of 128, columns of B in multiples of 64,
+// about 2048 wide (a 2048 x 2048 product block is 512 output tiles, over three waves
+// of SMs).  Narrower first blocks would start the products sooner but run them
+// below full waves, which costs more than it saves (1024-wide first blocks: 12.06
+// instead of 11.58 ms at 8192^3).
+std::vector<int64_t> cuts(int64_t len, int64_t quantum) {
+    std::vector<int64_t> c{0};
+    const int64_t t = std::max<int64_t>(1, (len + 2047) / 2048);
+    const int64_t w = gffm::round_up((len + t - 1) / t, quantum);
+    for (int64_t at = 0; at < len;) c.push_back(at = std::min(len, at + w));
+    return c;
+}
+
 struct Blocks {
-    int64_t bm, bn;
+    std::vector<int64_t> ra, cb;   // row cuts of A, column cuts of B (first 0, last m / n)
     int na, nb;
 };
 Blocks blocks_for(int64_t m, int64_t n) {
     Blocks b;
-    const int64_t ta = std::max<int64_t>(1, (m + 2047) / 2048), tb = std::max<int64_t>(1, (n + 2047) / 2048);
-    b.bm = gffm::round_up((m + ta - 1) / ta, 128);
-    b.bn = gffm::round_up((n + tb - 1) / tb, 64);
-    b.na = (int)((m + b.bm - 1) / b.bm);
-    b.nb = (int)((n + b.bn - 1) / b.bn);
+    b.ra = cuts(m, 128);
+    b.cb = cuts(n, 64);
+    b.na = (int)b.ra.size() - 1;
+    b.nb = (int)b.cb.size() - 1;
     return b;
 }
 
@@ -96,14 +106,10 @@ HostLayout host_layout(int64_t m, int64_t n, int64_t k, int64_t N) {
     h.off_b = take((size_t)h.ldb_d * (size_t)std::max<int64_t>(n, 1) * 8);
     h.off_c = take((size_t)h.ldc_d * (size_t)std::max<int64_t>(n, 1) * 8);
     if (k > 0) {
-        for (int i = 0; i < h.b.na; i++) {
-            const int64_t rows = std::min(h.b.bm, m - i * h.b.bm);
-            h.off_da.push_back(take(limb::layout_bits(rows, 1, k, N, h.bits).a_bytes));
-        }
-        for (int j = 0; j < h.b.nb; j++) {
-            const int64_t cols = std::min(h.b.bn, n - j * h.b.bn);
-            h.off_db.push_back(take(limb::layout_bits(1, cols, k, N, h.bits).b_bytes));
-        }
+        for (int i = 0; i < h.b.na; i++)
+            h.off_da.push_back(take(limb::layout_bits(h.b.ra[i + 1] - h.b.ra[i], 1, k, N, h.bits).a_bytes));
+        for (int j = 0; j < h.b.nb; j++)
+            h.off_db.push_back(take(limb::layout_bits(1, h.b.cb[j + 1] - h.b.cb[j], k, N, h.bits).b_bytes));
     }
     h.total = off;
     return h;
@@ -139,8 +145,8 @@ int enqueue(const HostLayout &h, const HostStreams &hs, uint8_t *base, int64_t m
     }
 
     const Blocks &b = h.b;
-    auto rows_of = [&](int i) { return std::min(b.bm, m - i * b.bm); };
-    auto cols_of = [&](int j) { return std::min(b.bn, n - j * b.bn); };
+    auto rows_of = [&](int i) { return b.ra[i + 1] - b.ra[i]; };
+    auto cols_of = [&](int j) { return b.cb[j + 1] - b.cb[j]; };
     std::vector<cudaEvent_t> a_in(b.na), b_in(b.nb), a_sp(b.na), b_sp(b.nb);
     for (auto *v : {&a_in, &a_sp})
         for (auto &e : *v)
@@ -152,13 +158,13 @@ int enqueue(const HostLayout &h, const HostStreams &hs, uint8_t *base, int64_t m
     // copies in: A_0, B_0, A_1, B_1, ...
     for (int q = 0; q < std::max(b.na, b.nb); q++) {
         if (q < b.na) {
-            const int64_t r0 = q * b.bm;
+            const int64_t r0 = b.ra[q];
             GFFM_CUDA(cudaMemcpy2DAsync(dA + r0, (size_t)h.lda_d * 8, hA + r0, (size_t)lda * 8, (size_t)rows_of(q) * 8,
                                         (size_t)k, cudaMemcpyHostToDevice, hs.in));
             GFFM_CUDA(cudaEventRecord(a_in[q], hs.in));
         }
         if (q < b.nb) {
-            const int64_t c0 = q * b.bn;
+            const int64_t c0 = b.cb[q];
             GFFM_CUDA(cudaMemcpy2DAsync(dB + c0 * h.ldb_d, (size_t)h.ldb_d * 8, hB + c0 * ldb, (size_t)ldb * 8,
                                         (size_t)k * 8, (size_t)cols_of(q), cudaMemcpyHostToDevice, hs.in));
             GFFM_CUDA(cudaEventRecord(b_in[q], hs.in));
@@ -185,7 +191,7 @@ int enqueue(const HostLayout &h, const HostStreams &hs, uint8_t *base, int64_t m
         __half *Bd = reinterpret_cast<__half *>(base + h.off_db[j]);
         if (a_on[i] < 0) {
             GFFM_CUDA(cudaStreamWaitEvent(c, a_in[i], 0));
-            st = limb::split_a<double>(dA + i * b.bm, h.lda_d, rows, k, Ad, g, N, c);
+            st = limb::split_a<double>(dA + b.ra[i], h.lda_d, rows, k, Ad, g, N, c);
             if (st) return st;
             GFFM_CUDA(cudaEventRecord(a_sp[i], c));
             a_on[i] = which;
@@ -194,21 +200,21 @@ int enqueue(const HostLayout &h, const HostStreams &hs, uint8_t *base, int64_t m
         }
         if (b_on[j] < 0) {
             GFFM_CUDA(cudaStreamWaitEvent(c, b_in[j], 0));
-            st = limb::split_b<double>(dB + j * b.bn * h.ldb_d, h.ldb_d, k, cols, Bd, g, N, c);
+            st = limb::split_b<double>(dB + b.cb[j] * h.ldb_d, h.ldb_d, k, cols, Bd, g, N, c);
             if (st) return st;
             GFFM_CUDA(cudaEventRecord(b_sp[j], c));
             b_on[j] = which;
         } else if (b_on[j] != which) {
             GFFM_CUDA(cudaStreamWaitEvent(c, b_sp[j], 0));
         }
-        double *Cij = dC + i * b.bm + j * b.bn * h.ldc_d;
+        double *Cij = dC + b.ra[i] + b.cb[j] * h.ldc_d;
         st = limb::gemm_digits(g, Ad, Bd, rows, cols, k, N, Cij, h.ldc_d, limb::EPI_STORE_F64, 0, c);
         if (st) return st;
         cudaEvent_t e_c;
         if ((st = evs.make(&e_c))) return st;
         GFFM_CUDA(cudaEventRecord(e_c, c));
         GFFM_CUDA(cudaStreamWaitEvent(hs.out, e_c, 0));
-        GFFM_CUDA(cudaMemcpy2DAsync(hC + i * b.bm + j * b.bn * ldc, (size_t)ldc * 8, Cij, (size_t)h.ldc_d * 8,
+        GFFM_CUDA(cudaMemcpy2DAsync(hC + b.ra[i] + b.cb[j] * ldc, (size_t)ldc * 8, Cij, (size_t)h.ldc_d * 8,
                                     (size_t)rows * 8, (size_t)cols, cudaMemcpyDeviceToHost, hs.out));
         which ^= 1;
     }

@@ -396,10 +396,10 @@ GFFM_API int gffm_matmul_limb_static_f64(int64_t m, int64_t n, int64_t k, const 
  * C = A*B mod N with A (m x k, lda), B (k x n, ldb) and C (m x n, ldc) in HOST
  * memory, column-major Float64, 2 <= N < 2^26, the same results as
  * gffm_matmul_limb_f64.  A is cut into row blocks and B into column blocks of
- * about 2048; the blocks are copied in on one stream while the block products
- * already resident run on two others, and each finished block of C is copied
- * back on a fourth, so only the first block pair's copy and the last block's
- * copy back are not hidden behind the products.  The library's internal
+ * about 2048; the blocks are copied in on one stream while the block products already resident run on
+ * two others, and each finished block of C is copied back on a fourth, so
+ * only the first block pair's copy and the last block's copy back are not
+ * hidden behind the products.  The library's internal
  * streams wait for the work already on `stream`, and `stream` waits for all of
  * the call: C is complete once `stream` is.  The host buffers must stay
  * valid until then; page-locked buffers (cudaHostAlloc / cudaHostRegister)

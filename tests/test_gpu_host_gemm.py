@@ -30,6 +30,7 @@ def status_ok(gffm):
     (2100, 300, 70, P26),           # two row blocks of A (1152 + 948)
     (300, 2200, 64, P26),           # two column blocks of B (1152 + 1048)
     (2200, 4200, 40, 65521),        # 2 x 3 blocks, ragged in both
+    (4500, 300, 20, 65521),         # row blocks of 1536, 1536, 1428
 ])
 def test_host_gemm_matches_oracle(gffm, m, n, k, N):
     rng = np.random.default_rng(m * 7 + n * 3 + k)
