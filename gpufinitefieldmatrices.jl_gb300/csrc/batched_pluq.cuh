@@ -209,6 +209,25 @@ __device__ __forceinline__ void scatter_moves(int32_t *X, int ldx, int c_lo, int
     }
 }
 
+// sum_{s < n8} a[s * sa] * b[s * sb] for n8 a multiple of 8 (at most 32 products below
+// 2^52): four accumulators, the eight loads of a chunk issued together
+__device__ __forceinline__ uint64_t dot8(const uint32_t *a, int sa, const uint32_t *b, int sb, int n8) {
+    uint64_t x0 = 0, x1 = 0, x2 = 0, x3 = 0;
+    for (int s = 0; s < n8; s += 8) {
+        uint32_t va[8], vb[8];
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+            va[k] = a[(s + k) * sa];
+            vb[k] = b[(s + k) * sb];
+        }
+        x0 += (uint64_t)va[0] * vb[0] + (uint64_t)va[4] * vb[4];
+        x1 += (uint64_t)va[1] * vb[1] + (uint64_t)va[5] * vb[5];
+        x2 += (uint64_t)va[2] * vb[2] + (uint64_t)va[6] * vb[6];
+        x3 += (uint64_t)va[3] * vb[3] + (uint64_t)va[7] * vb[7];
+    }
+    return (x0 + x1) + (x2 + x3);
+}
+
 __device__ __forceinline__ void named_sync(int id, int nthreads) {
     asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
 }
@@ -313,6 +332,7 @@ __global__ void __launch_bounds__(PQ_THREADS, 2) k_pluq_batched(PQArgs a) {
                 const int lr = idx / nbc, j = idx - lr * nbc;
                 P[j * rs + lr] = W[(int64_t)(r0 + lr) * ldw + c0 + j];
             }
+            for (int idx = tid; idx < PQ_MAX_NB * 33; idx += blockDim.x) Lv[idx] = 0;   // rows not applied yet
             __syncthreads();
             int npiv = 0, zero_hit = 0, stop = 0;
             // Left-looking: column t is brought up to date only when it is reached.
@@ -322,10 +342,10 @@ __global__ void __launch_bounds__(PQ_THREADS, 2) k_pluq_batched(PQArgs a) {
             // diagonal, the multipliers below), grows by one row per pivot.  Columns left of t
             // hold U above the diagonal, pv * inv on it and the negated multipliers below it.
             // Pivot t-1 is applied while column t is prepared: warp 7 computes the pivot's
-            // inverse; meanwhile warp 0 swaps the rows and forms the sums that do not need it
-            // (Linv's new row before scaling, U[s][t] for s < t-1) and warps 0-6 the partial
-            // values y[lr] = P[t][lr] + sum_{s < t-1} (N - l[lr][s]) U[s][t]; once the inverse
-            // is known, v = y + (N - l[lr][t-1]) * inv * y[t-1].
+            // inverse; meanwhile warps 0 and 2 swap the rows (columns from t-1 on / left of
+            // it), warp 1 forms U[s][t] for s < t-1 and warp 2 Linv's new row before scaling,
+            // then warps 0-6 the partial values y[lr] = P[t][lr] + sum_{s < t-1} (N - l[lr][s])
+            // U[s][t]; once the inverse is known, v = y + (N - l[lr][t-1]) * inv * y[t-1].
             uint32_t ppv = 0;     // pending pivot (value, local row); uniform over the block
             int pplr = 0;
             for (int t = 0;; t++) {
@@ -333,13 +353,17 @@ __global__ void __launch_bounds__(PQ_THREADS, 2) k_pluq_batched(PQArgs a) {
                 if (t > 0) {
                     const int tp = t - 1;
                     const bool nxt = t < nbc && r0 + t < m;
+                    // the sums run over tp8 terms: Lv rows from tp on, and s_ut from tp on, are zero
+                    const int tp8 = (tp + 7) & ~7;
+                    const uint32_t *Pu = reinterpret_cast<const uint32_t *>(P);
                     uint64_t lsum = 0;
                     if (warp == PQ_INV_WARP) {
                         const uint32_t inv = elim::mod_inverse(ppv, mont);
                         if (lane == 0) S.inv = inv;
                     } else {
                         if (warp == 0) {
-                            if (lane < nbc) {
+                            // rows tp <-> pplr over the panel's columns from tp on
+                            if (lane >= tp && lane < nbc) {
                                 int32_t *col = P + lane * rs;
                                 if (lane == tp) {
                                     col[pplr] = col[tp];
@@ -349,51 +373,37 @@ __global__ void __launch_bounds__(PQ_THREADS, 2) k_pluq_batched(PQArgs a) {
                                     col[pplr] = x;
                                 }
                             }
+                        } else if (warp == 1) {
+                            if (nxt) {   // U[s][t] for s < t-1 (rows above the swapped ones); zero from t-1 on
+                                const uint64_t acc = dot8(Lv + lane * 33, 1, Pu + t * rs, 1, tp8);
+                                s_ut[lane] = lane < tp ? reduce_u64(acc, M) : 0u;
+                            }
+                        } else if (warp == 2) {
+                            // rows tp <-> pplr over the columns left of tp, then Linv's row tp before
+                            // the inverse: sum_{s' < tp} (N - l[tp][s']) Linv[s'][lane]
+                            if (lane < tp && pplr != tp) {
+                                int32_t *col = P + lane * rs;
+                                const int32_t x = col[tp];
+                                col[tp] = col[pplr];
+                                col[pplr] = x;
+                            }
                             __syncwarp();
-                            if (nxt) {   // U[s][t] for s < t-1 (lanes past t-2: unused)
-                                uint64_t a0 = 0, a1 = 0;
-                                int s2 = 0;
-                                for (; s2 + 2 <= tp; s2 += 2) {
-                                    a0 += (uint64_t)Lv[lane * 33 + s2] * (uint32_t)P[t * rs + s2];
-                                    a1 += (uint64_t)Lv[lane * 33 + s2 + 1] * (uint32_t)P[t * rs + s2 + 1];
-                                }
-                                if (s2 < tp) a0 += (uint64_t)Lv[lane * 33 + s2] * (uint32_t)P[t * rs + s2];
-                                s_ut[lane] = reduce_u64(a0 + a1, M);
-                            }
-                            {   // Linv's row t-1 before the inverse: sum_{s' < t-1} (N - l[t-1][s']) Linv[s'][lane]
-                                uint64_t a0 = 0, a1 = 0;
-                                int s2 = 0;
-                                for (; s2 + 2 <= tp; s2 += 2) {
-                                    a0 += (uint64_t)(uint32_t)P[s2 * rs + tp] * Lv[s2 * 33 + lane];
-                                    a1 += (uint64_t)(uint32_t)P[(s2 + 1) * rs + tp] * Lv[(s2 + 1) * 33 + lane];
-                                }
-                                if (s2 < tp) a0 += (uint64_t)(uint32_t)P[s2 * rs + tp] * Lv[s2 * 33 + lane];
-                                lsum = a0 + a1;
-                            }
+                            lsum = dot8(Pu + tp, rs, Lv + lane, 33, tp8);
                         }
                         if (nxt) {
                             named_sync(1, PQ_INV_WARP * 32);
-                            for (int lr = tp + tid; lr < R; lr += PQ_INV_WARP * 32) {
-                                uint64_t a0 = (uint32_t)P[t * rs + lr], a1 = 0;
-                                int s2 = 0;
-                                for (; s2 + 2 <= tp; s2 += 2) {
-                                    a0 += (uint64_t)(uint32_t)P[s2 * rs + lr] * s_ut[s2];
-                                    a1 += (uint64_t)(uint32_t)P[(s2 + 1) * rs + lr] * s_ut[s2 + 1];
-                                }
-                                if (s2 < tp) a0 += (uint64_t)(uint32_t)P[s2 * rs + lr] * s_ut[s2];
-                                P[t * rs + lr] = (int32_t)reduce_u64(a0 + a1, M);
-                            }
+                            for (int lr = tp + tid; lr < R; lr += PQ_INV_WARP * 32)
+                                P[t * rs + lr] = (int32_t)reduce_u64((uint32_t)P[t * rs + lr] + dot8(Pu + lr, rs, s_ut, 1, tp8), M);
                         }
                     }
                     __syncthreads();
                     const uint32_t inv = S.inv;
-                    if (warp == 0) {
+                    if (warp == 2)
                         Lv[tp * 33 + lane] =
                             lane < tp ? elim::mulmod(reduce_u64(lsum, M), inv, M) : (lane == tp ? inv : 0u);
-                        if (lane == 0) {
-                            P[tp * rs + tp] = (int32_t)elim::mulmod(ppv, inv, M);   // U's diagonal
-                            S.piv_inv[tp] = inv;
-                        }
+                    if (tid == 0) {
+                        P[tp * rs + tp] = (int32_t)elim::mulmod(ppv, inv, M);   // U's diagonal
+                        S.piv_inv[tp] = inv;
                     }
                     if (!nxt) break;
                     g = elim::mulmod((uint32_t)P[t * rs + tp], inv, M);
