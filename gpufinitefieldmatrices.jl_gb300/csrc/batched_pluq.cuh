@@ -68,11 +68,12 @@ struct PQArgs {
     int tmp_ldw, tmp_ldlw;       // their row strides (>= every ldw / ldlw)
 };
 
-// shared-memory words a CTA needs for panel height rcap (panel + trailing pivot
-// rows; at least the 8 transpose tiles of 32 x 33 words the conversions use)
+// shared-memory words a CTA needs for panel height rcap: panel, trailing pivot rows
+// and the panel's row source map (rcap words); at least the 8 transpose tiles of
+// 32 x 33 words the conversions use
 __host__ __device__ constexpr size_t pq_smem_words(int rcap) {
-    return (size_t)PQ_MAX_NB * (rcap + 4) + (size_t)PQ_MAX_NB * PQ_CW > (size_t)8 * 32 * 33
-               ? (size_t)PQ_MAX_NB * (rcap + 4) + (size_t)PQ_MAX_NB * PQ_CW
+    return (size_t)PQ_MAX_NB * (rcap + 4) + (size_t)PQ_MAX_NB * PQ_CW + (size_t)rcap > (size_t)8 * 32 * 33
+               ? (size_t)PQ_MAX_NB * (rcap + 4) + (size_t)PQ_MAX_NB * PQ_CW + (size_t)rcap
                : (size_t)8 * 32 * 33;
 }
 
@@ -238,12 +239,17 @@ __device__ __forceinline__ unsigned long long pkey32(uint32_t v, int lr) {
 
 // The trailing update's 4 x 4 tiles: item i covers rows lr0 .. lr0+3 (local) and
 // columns cc .. cc+3 of the current chunk, cc = 8 * (column octet) + 4 * (i & 1).
+// In a chunk past the panel (moved), the columns have not seen the panel's row moves
+// yet: a row's W values come from row srcmap[lr] (local rows; the identity except for
+// the moved rows, whose sources are pivot-block rows still holding their old contents).
 struct UpdCtx {
     int32_t *W;
     int ldw, r0, cb, npiv, R, cw, lr_base, trows;
     const int32_t *P;
     int rs;
     const int32_t *Us;
+    const int *srcmap;
+    bool moved;
 };
 __device__ __forceinline__ void upd_pos(const UpdCtx &c, int item, int &lr0, int &cc) {
     const int tile = item >> 1, tc = tile / c.trows, tr = tile - tc * c.trows;
@@ -256,7 +262,8 @@ __device__ __forceinline__ void upd_load(uint64_t (&a)[4][4], const UpdCtx &c, i
 #pragma unroll
     for (int x = 0; x < 4; x++) {
         const bool rok = lr0 + x >= c.npiv && lr0 + x < c.R;
-        const int32_t *w = c.W + (int64_t)(c.r0 + lr0 + x) * c.ldw + c.cb + cc;
+        const int lr = (rok && c.moved) ? c.srcmap[lr0 + x] : lr0 + x;
+        const int32_t *w = c.W + (int64_t)(c.r0 + lr) * c.ldw + c.cb + cc;
 #pragma unroll
         for (int y = 0; y < 4; y++) a[x][y] = (rok && cc + y < c.cw) ? (uint32_t)w[y] : 0u;
     }
@@ -299,6 +306,7 @@ __global__ void __launch_bounds__(PQ_THREADS, 2) k_pluq_batched(PQArgs a) {
     const int rs = a.rcap + 4;                        // panel column stride (words), a multiple of 4
     int32_t *P = pq_smem;                             // P[j * rs + lr]: panel column j, local row lr
     int32_t *Us = pq_smem + (size_t)PQ_MAX_NB * rs;   // Us[t * PQ_CW + c]: pivot rows of a trailing chunk
+    int *srcmap = Us + PQ_MAX_NB * PQ_CW;             // srcmap[lr]: the panel's row moves, local rows
 
     for (;;) {
         if (tid == 0) {
@@ -491,6 +499,7 @@ __global__ void __launch_bounds__(PQ_THREADS, 2) k_pluq_batched(PQArgs a) {
                 }
                 S.nmv = k;
             }
+            for (int lr = tid; lr < R; lr += blockDim.x) srcmap[lr] = lr;
             // ---- panel back to W: eliminated columns keep the pivot and above, zero below ----
             for (int idx = tid; idx < R * nbc; idx += blockDim.x) {
                 const int lr = idx / nbc, j = idx - lr * nbc;
@@ -505,22 +514,20 @@ __global__ void __launch_bounds__(PQ_THREADS, 2) k_pluq_batched(PQArgs a) {
                 }
             }
             __syncthreads();
+            for (int k = tid; k < S.nmv; k += blockDim.x) srcmap[S.mv_dst[k] - r0] = S.mv_src[k] - r0;
             if (npiv > 0) {
-                // the rows the panel's swaps moved, outside the panel: trailing columns (moves
-                // only; their scaling comes with the Linv product below), L inside its swap
-                // width, and -- only once a zero column has been skipped, the one way a column
-                // left of the panel holds non-zeros below its pivot row -- the left columns
-                // with the pivot-row scaling
+                // the rows the panel's swaps moved, left of the panel: L inside its swap width,
+                // and -- only once a zero column has been skipped, the one way a column left of
+                // the panel holds non-zeros below its pivot row -- W with the pivot-row scaling.
+                // (The trailing columns take their moves inside the update through srcmap.)
                 int32_t *TW = a.tmp + (size_t)blockIdx.x * PQ_MAX_MOVES * (a.tmp_ldw + a.tmp_ldlw);
                 int32_t *TL = TW + (size_t)PQ_MAX_MOVES * a.tmp_ldw;
                 const int lsw_left = min(c0, lsw);
                 const int left = nc > 0 ? c0 : 0;
                 gather_moves(W, ldw, 0, left, TW, a.tmp_ldw, S);
-                gather_moves(W, ldw, c0 + nbc, n, TW, a.tmp_ldw, S);
                 gather_moves(LW, ldlw, 0, lsw_left, TL, a.tmp_ldlw, S);
                 __syncthreads();
                 scatter_moves(W, ldw, 0, left, TW, a.tmp_ldw, S, true, M);
-                scatter_moves(W, ldw, c0 + nbc, n, TW, a.tmp_ldw, S, false, M);
                 scatter_moves(LW, ldlw, 0, lsw_left, TL, a.tmp_ldlw, S, false, M);
             }
             // L columns at or past the swap width must not see the swaps after their own step
@@ -543,10 +550,15 @@ __global__ void __launch_bounds__(PQ_THREADS, 2) k_pluq_batched(PQArgs a) {
             // ---- trailing columns: pivot rows by the Linv product, rows below by one product ----
             // (a zero column that ended the panel is final already)
             const int ct0 = c0 + npiv + (zero_hit ? 1 : 0);
-            for (int cb = ct0; npiv > 0 && cb < n; cb += PQ_CW) {
-                const int cw = min(PQ_CW, n - cb);
+            // Chunks: the panel's own columns left over after an early end (already in their
+            // final row order) alone, then chunks of PQ_CW from the panel's end on, whose
+            // columns take the panel's row moves on the way in.
+            const int cmove = c0 + nbc;
+            for (int cb = ct0, cw = 0; npiv > 0 && cb < n; cb += cw) {
+                const bool moved = cb >= cmove;
+                cw = moved ? min(PQ_CW, n - cb) : min(cmove, n) - cb;
                 for (int t = warp; t < npiv; t += PQ_THREADS / 32) {
-                    const int32_t *src = W + (int64_t)(r0 + t) * ldw + cb;
+                    const int32_t *src = W + (int64_t)(r0 + (moved ? srcmap[t] : t)) * ldw + cb;
                     for (int c = lane; c < cw; c += 32) Us[t * PQ_CW + c] = src[c];
                 }
                 __syncthreads();
@@ -584,17 +596,13 @@ __global__ void __launch_bounds__(PQ_THREADS, 2) k_pluq_batched(PQArgs a) {
                     }
                 }
                 __syncthreads();
-                for (int t = warp; t < npiv; t += PQ_THREADS / 32) {
-                    int32_t *dst = W + (int64_t)(r0 + t) * ldw + cb;
-                    for (int c = lane; c < cw; c += 32) dst[c] = Us[t * PQ_CW + c];
-                }
                 // rows below the pivots: W += (N - l) u over 4 x 4 tiles, two per thread in
                 // flight: the W values of the next tile load while the current one multiplies.
                 // Tiles start at a multiple of 4 rows (16-byte panel and pivot-row reads).
                 const int lr_base = npiv & ~3;
                 const int trows = (R - lr_base + 3) >> 2;
                 const int nitems = 2 * trows * ((cw + 7) >> 3);
-                const UpdCtx uc{W, ldw, r0, cb, npiv, R, cw, lr_base, trows, P, rs, Us};
+                const UpdCtx uc{W, ldw, r0, cb, npiv, R, cw, lr_base, trows, P, rs, Us, srcmap, moved};
                 uint64_t a0[4][4], a1[4][4];
                 int it = tid;
                 if (it < nitems) upd_load(a0, uc, it);
@@ -608,6 +616,12 @@ __global__ void __launch_bounds__(PQ_THREADS, 2) k_pluq_batched(PQArgs a) {
                     if (it2 < nitems) upd_load(a0, uc, it2);
                     upd_mul(a1, uc, it1);
                     upd_store(a1, uc, it1, M);
+                }
+                __syncthreads();
+                // U to the pivot rows, after the update has read their old contents
+                for (int t = warp; t < npiv; t += PQ_THREADS / 32) {
+                    int32_t *dst = W + (int64_t)(r0 + t) * ldw + cb;
+                    for (int c = lane; c < cw; c += 32) dst[c] = Us[t * PQ_CW + c];
                 }
                 __syncthreads();
             }
