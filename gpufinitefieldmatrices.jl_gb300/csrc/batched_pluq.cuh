@@ -44,7 +44,6 @@ static_assert(PQ_INV_WARP * 32 + 32 == PQ_THREADS, "the inverse warp is the CTA'
 struct PQInst {
     int m, n, l_cols, lsw;       // lsw = min(32*cld(m, 32), l_cols): L's row-swap width
     elim::ModP M;                // N, floor((2^64-1)/N)
-    elim::Mont mont;             // pivot inverse (Fermat for prime N, else the reference's Euclid)
     const double *A;
     int64_t lda;
     double *U;
@@ -320,7 +319,6 @@ __global__ void __launch_bounds__(PQ_THREADS, 2) k_pluq_batched(PQArgs a) {
         const PQInst *Ip = a.inst + ii;
         const int m = Ip->m, n = Ip->n, l_cols = Ip->l_cols, lsw = Ip->lsw;
         const elim::ModP M{Ip->M.n, Ip->M.minv};
-        const elim::Mont mont{Ip->mont.n, Ip->mont.nprime, Ip->mont.r2, Ip->mont.prime};
         const uint32_t N = M.n;
         int32_t *const W = Ip->W;
         int32_t *const LW = Ip->LW;
@@ -366,7 +364,7 @@ __global__ void __launch_bounds__(PQ_THREADS, 2) k_pluq_batched(PQArgs a) {
                     const uint32_t *Pu = reinterpret_cast<const uint32_t *>(P);
                     uint64_t lsum = 0;
                     if (warp == PQ_INV_WARP) {
-                        const uint32_t inv = elim::mod_inverse(ppv, mont);
+                        const uint32_t inv = elim::mod_inv_euclid_alu(ppv, N);
                         if (lane == 0) S.inv = inv;
                     } else {
                         if (warp == 0) {

@@ -584,7 +584,6 @@ int create(const gffm_batch_desc *descs, int64_t count, const gffm_batch_tuning 
         I.lsw = (int)std::min<int64_t>((d.m + 31) / 32 * 32, d.l_cols);
         I.M.n = (uint32_t)d.N;
         I.M.minv = ~uint64_t(0) / (uint64_t)d.N;
-        I.mont = elim::make_mont((uint32_t)d.N);
         I.A = d.A;
         I.lda = d.lda;
         I.U = d.C;
