@@ -244,11 +244,11 @@ __device__ __forceinline__ unsigned long long pkey32(uint32_t v, int lr) {
 struct UpdCtx {
     int32_t *W;
     int ldw, r0, cb, npiv, R, cw, lr_base, trows;
-    const int32_t *P;
+    const int32_t *P;            // the panel; Us and srcmap follow it in shared memory
     int rs;
-    const int32_t *Us;
-    const int *srcmap;
     bool moved;
+    __device__ __forceinline__ const int32_t *us() const { return P + PQ_MAX_NB * rs; }
+    __device__ __forceinline__ const int *srcmap() const { return us() + PQ_MAX_NB * PQ_CW; }
 };
 __device__ __forceinline__ void upd_pos(const UpdCtx &c, int item, int &lr0, int &cc) {
     const int tile = item >> 1, tc = tile / c.trows, tr = tile - tc * c.trows;
@@ -261,7 +261,7 @@ __device__ __forceinline__ void upd_load(uint64_t (&a)[4][4], const UpdCtx &c, i
 #pragma unroll
     for (int x = 0; x < 4; x++) {
         const bool rok = lr0 + x >= c.npiv && lr0 + x < c.R;
-        const int lr = (rok && c.moved) ? c.srcmap[lr0 + x] : lr0 + x;
+        const int lr = (rok && c.moved) ? c.srcmap()[lr0 + x] : lr0 + x;
         const int32_t *w = c.W + (int64_t)(c.r0 + lr) * c.ldw + c.cb + cc;
 #pragma unroll
         for (int y = 0; y < 4; y++) a[x][y] = (rok && cc + y < c.cw) ? (uint32_t)w[y] : 0u;
@@ -273,7 +273,7 @@ __device__ __forceinline__ void upd_mul(uint64_t (&a)[4][4], const UpdCtx &c, in
 #pragma unroll 4
     for (int t = 0; t < c.npiv; t++) {
         const int4 lq = *reinterpret_cast<const int4 *>(c.P + t * c.rs + lr0);   // negated multipliers
-        const int4 uq = *reinterpret_cast<const int4 *>(c.Us + t * PQ_CW + cc);
+        const int4 uq = *reinterpret_cast<const int4 *>(c.us() + t * PQ_CW + cc);
         const uint32_t lv[4] = {(uint32_t)lq.x, (uint32_t)lq.y, (uint32_t)lq.z, (uint32_t)lq.w};
         const uint32_t uv[4] = {(uint32_t)uq.x, (uint32_t)uq.y, (uint32_t)uq.z, (uint32_t)uq.w};
 #pragma unroll
@@ -600,7 +600,7 @@ __global__ void __launch_bounds__(PQ_THREADS, 2) k_pluq_batched(PQArgs a) {
                 const int lr_base = npiv & ~3;
                 const int trows = (R - lr_base + 3) >> 2;
                 const int nitems = 2 * trows * ((cw + 7) >> 3);
-                const UpdCtx uc{W, ldw, r0, cb, npiv, R, cw, lr_base, trows, P, rs, Us, srcmap, moved};
+                const UpdCtx uc{W, ldw, r0, cb, npiv, R, cw, lr_base, trows, P, rs, moved};
                 uint64_t a0[4][4], a1[4][4];
                 int it = tid;
                 if (it < nitems) upd_load(a0, uc, it);
