@@ -1,13 +1,14 @@
 // k_elementwise.cu -- the reference's grid-stride elementwise kernels
-// (src/CuModMatrix/kernel_ops/{add,sub,mul,mod}_ops.jl) over the whole padded
+// (src/CuModMatrix/kernel_ops/{add,sub,mul,div,mod}_ops.jl) over the whole padded
 // data array, HBM-bound.  Values are converted to 64-bit integers, combined
 // exactly and reduced with Julia mod semantics (result in [0, N)), so results
 // equal the reference's whenever its floating-point arithmetic is exact.
 #include "gffm_common.cuh"
+#include "modarith.cuh"
 
 namespace {
 
-enum Op { OP_ADD, OP_SUB, OP_MULE, OP_SADD, OP_SSUB, OP_RSSUB, OP_SMUL, OP_MOD };
+enum Op { OP_ADD, OP_SUB, OP_MULE, OP_SADD, OP_SSUB, OP_RSSUB, OP_SMUL, OP_MOD, OP_TDIV };
 
 struct ModN {
     int64_t n;
@@ -38,6 +39,10 @@ __global__ void __launch_bounds__(256) k_elementwise(T *__restrict__ C, const T 
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     int64_t stride = (int64_t)gridDim.x * blockDim.x;
     for (; i < len; i += stride) {
+        if (OP == OP_TDIV) {   // div(A, N): truncating integer division, no reduction
+            C[i] = (T)(to_i64(A[i]) / M.n);
+            continue;
+        }
         int64_t a = mod_i64(to_i64(A[i]), M);
         int64_t r;
         if (OP == OP_ADD) {
@@ -124,5 +129,30 @@ int gffm_mod_f64(double *C, const double *A, int64_t len, int64_t N, gffm_stream
 }
 int gffm_mod_f32(float *C, const float *A, int64_t len, int64_t N, gffm_stream_t s) {
     return launch<float, OP_MOD>(C, A, nullptr, 0.0, len, N, s);
+}
+
+int gffm_mod_inv(int64_t p, int64_t P, int64_t *out) {
+    if (!out) return gffm::set_error(GFFM_ERR_ARG, "out is NULL");
+    if (P < 1 || P > (int64_t(1) << 52)) return gffm::set_error(GFFM_ERR_MODULUS, "Modulus %lld is outside [1, 2^52]", (long long)P);
+    *out = elim::ref_mod_inv(p, P);
+    return GFFM_OK;
+}
+
+// div!(C, A, s, mod_N): C = A * mod_inv(s, N) mod N
+int gffm_div_scalar_f64(double *C, const double *A, int64_t s, int64_t len, int64_t N, gffm_stream_t st) {
+    if (N < 1 || N > (int64_t(1) << 52)) return gffm::set_error(GFFM_ERR_MODULUS, "Modulus %lld is outside [1, 2^52]", (long long)N);
+    return launch<double, OP_SMUL>(C, A, nullptr, (double)elim::ref_mod_inv(s, N), len, N, st);
+}
+int gffm_div_scalar_f32(float *C, const float *A, int64_t s, int64_t len, int64_t N, gffm_stream_t st) {
+    if (N < 1 || N > (int64_t(1) << 52)) return gffm::set_error(GFFM_ERR_MODULUS, "Modulus %lld is outside [1, 2^52]", (long long)N);
+    return launch<float, OP_SMUL>(C, A, nullptr, (double)elim::ref_mod_inv(s, N), len, N, st);
+}
+
+// div.(A, N) elementwise (divide_elements!): truncating integer division
+int gffm_trunc_div_f64(double *C, const double *A, int64_t len, int64_t N, gffm_stream_t s) {
+    return launch<double, OP_TDIV>(C, A, nullptr, 0.0, len, N, s);
+}
+int gffm_trunc_div_f32(float *C, const float *A, int64_t len, int64_t N, gffm_stream_t s) {
+    return launch<float, OP_TDIV>(C, A, nullptr, 0.0, len, N, s);
 }
 }

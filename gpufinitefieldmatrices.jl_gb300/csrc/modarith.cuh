@@ -51,6 +51,24 @@ __device__ __forceinline__ uint32_t mod_inv_euclid(uint32_t p, uint32_t P) {
     return (uint32_t)inv;
 }
 
+// mod_inv(p, P) of the reference (src/CuModMatrix/rref_lu_pluq/pluq_kernels.jl:11-31)
+// for any 64-bit p and P > 0 (|P| < 2^62): the extended Euclid sequence with
+// truncating division (Julia's div), 0 for p = 0, a non-inverse when gcd(p, P) > 1.
+__host__ __device__ inline int64_t ref_mod_inv(int64_t p, int64_t P) {
+    int64_t inv = 0, new_inv = 1, rem = P, new_rem = p;
+    while (new_rem != 0) {
+        const int64_t q = rem / new_rem;
+        const int64_t t = inv - q * new_inv;
+        inv = new_inv;
+        new_inv = t;
+        const int64_t r = rem - q * new_rem;
+        rem = new_rem;
+        new_rem = r;
+    }
+    if (inv < 0) inv += P;
+    return inv;
+}
+
 // The same extended Euclid sequence as mod_inv_euclid (so the same result for any
 // P), with the quotients 1, 2 and 3 -- about two thirds of them -- found by
 // comparisons instead of a division: the loop stays on the integer ALU, away from

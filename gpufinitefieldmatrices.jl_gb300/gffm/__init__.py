@@ -9,7 +9,7 @@ from .build import build  # noqa: F401
 from .cumod import (  # noqa: F401
     TILE_WIDTH, DEFAULT_TYPE, CuModArray, CuModMatrix, CuModVector, wrap, zeros, eye, rand, similar, copy,
     add_, sub_, elementwise_multiply_, scalar_add_, scalar_sub_, rscalar_sub_, scalar_mul_, negate_,
-    mod_, mod_elements_, fill_, zero_, copy_, change_modulus, change_modulus_no_alloc_,
+    mod_, mod_elements_, fill_, zero_, copy_, change_modulus, change_modulus_no_alloc_, div_,
     mul_, stripe_mul_, mat_mul_gpu_type, mat_mul_type_inplace_, find_max_stripe_ops, limbs_for, LimbTuning,
     matmul_host, host_matrix,
     CuModArraySizeMismatchException, CuModArrayModulusMismatchException, CuModMatrixNotSquareException,
@@ -24,7 +24,7 @@ from . import cumod as _cumod, karatsuba as _karatsuba  # noqa: E402
 from .karatsuba import (  # noqa: F401,E402
     KaratsubaArray, KaratsubaMatrix, KaratsubaVector, KaratsubaZeros, KaratsubaMatrix_from, Karatsubacopy,
     initialize_plan_, KMatMul_, KMatMul_gemv_, MatToKMat, KMatToMat, poly_karatsuba_matmul, scalar_multiply_,
-    find_max_ops, find_max_ops_karatsuba, nKMuls,
+    find_max_ops, find_max_ops_karatsuba, nKMuls, divide_elements_,
 )
 
 
@@ -47,3 +47,7 @@ zero_ = _dispatch("zero_")
 copy_ = _dispatch("copy_")
 from .batched import BatchPlan, Tuning as BatchTuning, batched_plan  # noqa: F401,E402
 from . import autotune  # noqa: F401,E402
+from .triangular import (  # noqa: F401,E402
+    InverseNotDefinedException, mod_inv, forward_sub_gpu_type_32, backward_sub_gpu_type_32,
+    upper_triangular_inverse_no_copy, lower_triangular_inverse_no_copy, triangular_inverse_into_,
+)

@@ -48,6 +48,16 @@ SIGNATURES = {
     "gffm_matmul_limb_static_max_bytes": (_INT, [_PSZ]),
     "gffm_matmul_limb_static_f64": (_INT, [_I64, _I64, _I64, _P, _I64, _P, _I64, _P, _I64, _I64, _P]),
     "gffm_matmul_host_workspace_size": (_INT, [_I64, _I64, _I64, _I64, _PSZ]),
+    "gffm_div_scalar_f64": (_INT, [_P, _P, _I64, _I64, _I64, _P]),
+    "gffm_div_scalar_f32": (_INT, [_P, _P, _I64, _I64, _I64, _P]),
+    "gffm_trunc_div_f64": (_INT, [_P, _P, _I64, _I64, _P]),
+    "gffm_trunc_div_f32": (_INT, [_P, _P, _I64, _I64, _P]),
+    "gffm_mod_inv": (_INT, [_I64, _I64, ctypes.POINTER(ctypes.c_int64)]),
+    "gffm_tri_sub32_f64": (_INT, [ctypes.c_int, _I64, _I64, _P, _I64, _I64, _I64, _P, _I64, _I64, _P]),
+    "gffm_tri_sub32_f32": (_INT, [ctypes.c_int, _I64, _I64, _P, _I64, _I64, _I64, _P, _I64, _I64, _P]),
+    "gffm_triangular_inverse_workspace_size": (_INT, [ctypes.c_int, _I64, _I64, _I64, _PSZ]),
+    "gffm_triangular_inverse_f64": (_INT, [ctypes.c_int, _I64, _I64, _P, _I64, _P, _I64, _I64, _P, _SZ, _P]),
+    "gffm_triangular_inverse_f32": (_INT, [ctypes.c_int, _I64, _I64, _P, _I64, _P, _I64, _I64, _P, _SZ, _P]),
     "gffm_matmul_host_f64": (_INT, [_I64, _I64, _I64, _P, _I64, _P, _I64, _P, _I64, _I64, _P, _SZ, _P]),
 }
 for _op in ("add", "sub", "mul_elementwise"):

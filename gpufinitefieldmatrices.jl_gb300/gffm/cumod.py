@@ -150,6 +150,12 @@ class CuModArray:
     def __rmul__(self, s):
         return self.__mul__(s)
 
+    def __truediv__(self, s):
+        """A / s (div_ops.jl:24-28): A times the reference's mod_inv(s, N)."""
+        C = similar(self)
+        div_(C, self, s)
+        return C
+
     def __matmul__(self, other):
         return self.__mul__(other)
 
@@ -313,6 +319,13 @@ def negate_(B, A, mod_N=-1):
     if mod_N <= 0 and A.N != B.N:
         raise CuModArrayModulusMismatchException("Both matrices must have the same modulus N or provide an override mod_N")
     return _scalar("rscalar_sub", B, A, 0, mod_N)
+
+
+def div_(C, A, s, mod_N=-1):
+    """div!(C, A, s, mod_N) (kernel_ops/div_ops.jl:13-22): C = A * mod_inv(s, N) mod N."""
+    N = mod_N if mod_N > 0 else C.N
+    call("gffm_div_scalar_%s" % _sfx(C.dtype), _ptr(C.data), _ptr(A.data), int(s), A.padded_len, N, _stream())
+    return C
 
 
 def mod_(C, A, m):

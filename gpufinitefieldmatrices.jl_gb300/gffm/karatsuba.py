@@ -331,6 +331,13 @@ def copy_(B, A):
     return B
 
 
+def divide_elements_(B, A, N):
+    """divide_elements!(B, A, N) (KaratsubaMatrix.jl:733-736): B.data = div.(A.data, N),
+    truncating integer division over the padded data; returns A, as the reference does."""
+    call("gffm_trunc_div_%s" % cumod._sfx(B.dtype), _ptr(B.data), _ptr(A.data), A.padded_len, int(N), _stream())
+    return A
+
+
 def Karatsubacopy(A):
     """Karatsubacopy(A) (KaratsubaMatrix.jl:738-744)."""
     B = KaratsubaArray(cumod.copy(A.data1), cumod.copy(A.data2), A.N1, A.N2, A.N1 * A.N2)

@@ -109,6 +109,17 @@ GFFM_API int gffm_scalar_mul_f32(float *C, const float *A, float s, int64_t len,
 /* mod!(C, A, N) / mod_elements! -> k_mod! (mod_ops.jl:3-11,13-21) */
 GFFM_API int gffm_mod_f64(double *C, const double *A, int64_t len, int64_t N, gffm_stream_t stream);
 GFFM_API int gffm_mod_f32(float *C, const float *A, int64_t len, int64_t N, gffm_stream_t stream);
+/* div!(C, A, s, mod_N) and A / s (div_ops.jl:13-29): C = A * mod_inv(s, N) mod N */
+GFFM_API int gffm_div_scalar_f64(double *C, const double *A, int64_t s, int64_t len, int64_t N, gffm_stream_t stream);
+GFFM_API int gffm_div_scalar_f32(float *C, const float *A, int64_t s, int64_t len, int64_t N, gffm_stream_t stream);
+/* divide_elements!(B, A, N) (KaratsubaMatrix.jl:733-736): C = div.(A, N), Julia's
+ * truncating integer division, no reduction */
+GFFM_API int gffm_trunc_div_f64(double *C, const double *A, int64_t len, int64_t N, gffm_stream_t stream);
+GFFM_API int gffm_trunc_div_f32(float *C, const float *A, int64_t len, int64_t N, gffm_stream_t stream);
+/* mod_inv(p, P) (rref_lu_pluq/pluq_kernels.jl:11-31), on the host: the extended
+ * Euclid sequence with truncating division; 0 for p = 0 and a non-inverse when
+ * gcd(p, P) > 1, as the reference returns.  1 <= P <= 2^52. */
+GFFM_API int gffm_mod_inv(int64_t p, int64_t P, int64_t *out);
 
 /* ---- plain modular GEMM / GEMV: the reference's own method ---------------
  * C = A*B mod N with A (m x k, lda), B (k x n, ldb), C (m x n, ldc).
@@ -388,6 +399,41 @@ GFFM_API int gffm_batched_plan_destroy(gffm_batch_plan plan);
 GFFM_API int gffm_matmul_limb_static_max_bytes(size_t *bytes);
 GFFM_API int gffm_matmul_limb_static_f64(int64_t m, int64_t n, int64_t k, const double *A, int64_t lda,
                                          const double *B, int64_t ldb, double *C, int64_t ldc, int64_t N,
+                                         gffm_stream_t stream);
+
+/* ---- triangular inverses and substitutions (src/CuModMatrix/triangular) ----
+ * 2 <= N < 2^26.  A is m x n (lda); the result X is n x m (ldx >= n), the
+ * reference's transposed shape.  Only A's triangle is read (diagonal and the
+ * upper or lower side); entries outside A count as zero, as the reference's
+ * zero padding does.  The pivot inverses are the reference's mod_inv (0 for a
+ * zero diagonal entry).
+ *
+ * gffm_tri_sub32_*: forward_sub_gpu_type_32 (upper = 0) / backward_sub_gpu_type_32
+ * (upper = 1) (substitution_inplace.jl:6-88): the inverse of the 32 x 32
+ * triangular window of A at (row_shift, col_shift), the diagonal read at
+ * (row_shift + r, row_shift + r) as the reference does, written to
+ * X[0:min(32, n)][0:min(32, m)]; the rest of X is not touched.
+ *
+ * gffm_triangular_inverse_*: upper_triangular_inverse_no_copy (upper = 1) /
+ * lower_triangular_inverse_no_copy (upper = 0) (triangular_inverse_no_copy.jl:
+ * 18-477): the reference's block recursion on the leading k x k triangle, k =
+ * min(m, n) (halves split at multiples of 32, 32-blocks by substitution, the
+ * off-diagonal blocks -X11 A12 X22 / -X22 A21 X11 by the limb GEMM), written to
+ * X's leading k x k, zero elsewhere in X: the inverse for an invertible diagonal,
+ * the inverse of the leading square block zero-extended for tall / wide input.
+ * Lower and tall (m > n > 32) is GFFM_ERR_SIZE, the reference's
+ * InverseNotDefinedException.  Workspace: gffm_triangular_inverse_workspace_size
+ * bytes, or NULL. */
+GFFM_API int gffm_tri_sub32_f64(int upper, int64_t m, int64_t n, const double *A, int64_t lda, int64_t row_shift,
+                                int64_t col_shift, double *X, int64_t ldx, int64_t N, gffm_stream_t stream);
+GFFM_API int gffm_tri_sub32_f32(int upper, int64_t m, int64_t n, const float *A, int64_t lda, int64_t row_shift,
+                                int64_t col_shift, float *X, int64_t ldx, int64_t N, gffm_stream_t stream);
+GFFM_API int gffm_triangular_inverse_workspace_size(int upper, int64_t m, int64_t n, int64_t N, size_t *bytes);
+GFFM_API int gffm_triangular_inverse_f64(int upper, int64_t m, int64_t n, const double *A, int64_t lda, double *X,
+                                         int64_t ldx, int64_t N, void *workspace, size_t workspace_bytes,
+                                         gffm_stream_t stream);
+GFFM_API int gffm_triangular_inverse_f32(int upper, int64_t m, int64_t n, const float *A, int64_t lda, float *X,
+                                         int64_t ldx, int64_t N, void *workspace, size_t workspace_bytes,
                                          gffm_stream_t stream);
 
 /* ---- limb GEMM on host buffers (the round trip Array -> CuModMatrix -> * ->

@@ -60,6 +60,10 @@ def lib():
         L.or_karatsuba_addsub.argtypes = [_i64, _p, _p, _p, _p, _p, _p, _i64, _i64, ctypes.c_int]
         L.or_karatsuba_scale.restype = None
         L.or_karatsuba_scale.argtypes = [_i64, _p, _p, _i64, ctypes.c_int, _p, _p, _i64, _i64]
+        L.or_tri_window.restype = None
+        L.or_tri_window.argtypes = [ctypes.c_int, _i64, _i64, _p, _i64, _i64, _i64, _i64, _p]
+        L.or_tri_inverse.restype = ctypes.c_int
+        L.or_tri_inverse.argtypes = [ctypes.c_int, _i64, _i64, _p, _i64, _i64, _p]
         _lib = L
     return _lib
 
@@ -198,3 +202,35 @@ def apply_col_swaps(M, swaps, inverse=False):
     for (i, j) in seq:
         M[:, [i - 1, j - 1]] = M[:, [j - 1, i - 1]]
     return M
+
+
+def tri_window(A, N, row_shift, col_shift, upper):
+    """forward_sub_kernel_32 / backward_sub_kernel_32 (src/CuModMatrix/triangular/
+    substitution_inplace.jl:6-35, 63-88): the 32 x 32 window inverse (exact)."""
+    A = _f(A)
+    m, n = A.shape
+    W = np.zeros((32, 32), dtype=np.int64, order="F")
+    lib().or_tri_window(1 if upper else 0, m, n, _ptr(A), max(m, 1), int(row_shift), int(col_shift), int(N), _ptr(W))
+    return W
+
+
+def tri_sub32(A, N, row_shift, col_shift, upper):
+    """forward_sub_gpu_type_32 / backward_sub_gpu_type_32: the window inverse in the
+    top-left of an (n x m) zero matrix."""
+    m, n = np.asarray(A).shape
+    X = np.zeros((n, m), dtype=np.int64)
+    W = tri_window(A, N, row_shift, col_shift, upper)
+    r, c = min(32, n), min(32, m)
+    X[:r, :c] = W[:r, :c]
+    return X
+
+
+def tri_inverse(A, N, upper):
+    """upper_triangular_inverse_no_copy / lower_triangular_inverse_no_copy
+    (src/CuModMatrix/triangular/triangular_inverse_no_copy.jl:197-245, 450-477):
+    returns (X (n x m), status); status 2 is the reference's InverseNotDefinedException."""
+    A = _f(A)
+    m, n = A.shape
+    X = np.zeros((n, m), dtype=np.int64, order="F")
+    st = lib().or_tri_inverse(1 if upper else 0, m, n, _ptr(A), max(m, 1), int(N), _ptr(X))
+    return X, st

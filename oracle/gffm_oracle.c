@@ -448,3 +448,113 @@ void or_karatsuba_scale(int64_t len, const int64_t *A1, const int64_t *A2, int64
         C2[i] = (int64_t)(c / N1);
     }
 }
+
+/* ---- triangular inverses (src/CuModMatrix/triangular) ---- */
+
+static int64_t or_tri_at(const int64_t *A, int64_t lda, int64_t m, int64_t n, int64_t i, int64_t j, int64_t N) {
+    return (i >= 0 && j >= 0 && i < m && j < n) ? or_modi(A[i + j * lda], N) : 0; /* the zero padding */
+}
+
+/* forward_sub_kernel_32 (upper = 0) / backward_sub_kernel_32 (upper = 1)
+ * (substitution_inplace.jl:6-35, 63-88), in exact arithmetic: the inverse of the
+ * 32 x 32 triangular window of A (m x n) at (rs, cs), one result column c per
+ * reference thread, rows in order (forward) or reverse order (backward):
+ *   X[r][c] = mod_inv(A[rs + r][rs + r]) * ([r == c] - sum_k A[rs + r][cs + k] X[k][c]) mod N,
+ * k < r (forward) or k > r (backward).  X is 32 x 32, column-major. */
+void or_tri_window(int upper, int64_t m, int64_t n, const int64_t *A, int64_t lda, int64_t rs, int64_t cs,
+                   int64_t N, int64_t *X) {
+    for (int c = 0; c < 32; c++) {
+        for (int q = 0; q < 32; q++) {
+            const int r = upper ? 31 - q : q;
+            i128 sum = 0;
+            if (upper) {
+                for (int k = r + 1; k < 32; k++) sum += (i128)or_tri_at(A, lda, m, n, rs + r, cs + k, N) * X[k + 32 * c];
+            } else {
+                for (int k = 0; k < r; k++) sum += (i128)or_tri_at(A, lda, m, n, rs + r, cs + k, N) * X[k + 32 * c];
+            }
+            const int64_t rhs = (r == c) ? 1 : 0;
+            const int64_t d = or_mod_inv(or_tri_at(A, lda, m, n, rs + r, rs + r, N), N);
+            X[r + 32 * c] = or_mulmod(d, or_mod128((i128)rhs - sum, N), N);
+        }
+    }
+}
+
+/* _recursive_upper/lower_triangular_inverse_no_copy (triangular_inverse_no_copy.jl:
+ * 18-195, 246-448) on the square block [lo, hi) of the leading triangle: a block
+ * of at most 32 by its window; otherwise the split mid = lo + 32 * q with
+ * q = floor(size / 64 + 1/2), both halves (the reference's second branch does
+ * them by window directly, its third by recursion -- the same blocks), then
+ *   upper: X[lo:mid][mid:hi] = -(X11 A12 mod N) X22 mod N
+ *   lower: X[mid:hi][lo:mid] = -(X22 A21 mod N) X11 mod N.
+ * X is column-major with leading dimension ldx. */
+static void or_tri_rec(int upper, int64_t m, int64_t n, const int64_t *A, int64_t lda, int64_t N, int64_t lo,
+                       int64_t hi, int64_t *X, int64_t ldx) {
+    const int64_t s = hi - lo;
+    if (s <= 32) {
+        int64_t W[32 * 32];
+        or_tri_window(upper, m, n, A, lda, lo, lo, N, W);
+        for (int64_t c = 0; c < s; c++)
+            for (int64_t r = 0; r < s; r++) X[(lo + r) + (lo + c) * ldx] = W[r + 32 * c];
+        return;
+    }
+    int64_t q = (int64_t)((double)s / 64.0 + 0.5);
+    if (q < 1) q = 1;
+    const int64_t mid = lo + 32 * q, s1 = mid - lo, s2 = hi - mid;
+    or_tri_rec(upper, m, n, A, lda, N, lo, mid, X, ldx);
+    or_tri_rec(upper, m, n, A, lda, N, mid, hi, X, ldx);
+    /* T = first product (s1 x s2 upper, s2 x s1 lower), then the block */
+    int64_t *T = (int64_t *)malloc(sizeof(int64_t) * (size_t)(s1 * s2));
+    if (upper) {
+        for (int64_t j = 0; j < s2; j++)
+            for (int64_t i = 0; i < s1; i++) {
+                i128 acc = 0;
+                for (int64_t t = 0; t < s1; t++)
+                    acc += (i128)X[(lo + i) + (lo + t) * ldx] * or_tri_at(A, lda, m, n, lo + t, mid + j, N);
+                T[i + j * s1] = or_mod128(acc, N);
+            }
+        for (int64_t j = 0; j < s2; j++)
+            for (int64_t i = 0; i < s1; i++) {
+                i128 acc = 0;
+                for (int64_t t = 0; t < s2; t++) acc += (i128)T[i + t * s1] * X[(mid + t) + (mid + j) * ldx];
+                X[(lo + i) + (mid + j) * ldx] = or_mod128(-acc, N);
+            }
+    } else {
+        for (int64_t j = 0; j < s1; j++)
+            for (int64_t i = 0; i < s2; i++) {
+                i128 acc = 0;
+                for (int64_t t = 0; t < s2; t++)
+                    acc += (i128)X[(mid + i) + (mid + t) * ldx] * or_tri_at(A, lda, m, n, mid + t, lo + j, N);
+                T[i + j * s2] = or_mod128(acc, N);
+            }
+        for (int64_t j = 0; j < s1; j++)
+            for (int64_t i = 0; i < s2; i++) {
+                i128 acc = 0;
+                for (int64_t t = 0; t < s1; t++) acc += (i128)T[i + t * s2] * X[(lo + t) + (lo + j) * ldx];
+                X[(mid + i) + (lo + j) * ldx] = or_mod128(-acc, N);
+            }
+    }
+    free(T);
+}
+
+/* upper_triangular_inverse_no_copy (upper = 1, triangular_inverse_no_copy.jl:197-245)
+ * / lower_triangular_inverse_no_copy (upper = 0, :450-477) of A (m x n): X is
+ * n x m (ld n), zero-initialised here.  A single window when rows (upper) or
+ * columns (lower) are at most 32 (the window fills X's leading min(32, n) x
+ * min(32, m)); lower and tall beyond that is the reference's
+ * InverseNotDefinedException (returns 2); otherwise the recursion on the leading
+ * min(m, n) square. */
+int or_tri_inverse(int upper, int64_t m, int64_t n, const int64_t *A, int64_t lda, int64_t N, int64_t *X) {
+    const int64_t ldx = n;
+    for (int64_t e = 0; e < n * m; e++) X[e] = 0;
+    if (upper ? m <= 32 : n <= 32) {
+        int64_t W[32 * 32];
+        or_tri_window(upper, m, n, A, lda, 0, 0, N, W);
+        for (int64_t c = 0; c < (m < 32 ? m : 32); c++)
+            for (int64_t r = 0; r < (n < 32 ? n : 32); r++) X[r + c * ldx] = W[r + 32 * c];
+        return 0;
+    }
+    if (!upper && m > n) return 2;
+    const int64_t k = m < n ? m : n;
+    or_tri_rec(upper, m, n, A, lda, N, 0, k, X, ldx);
+    return 0;
+}

@@ -167,3 +167,74 @@ def kara_matmul(A1, A2, B1, B2, N1, N2):
             R1[i][j] = cc1 % N1
             R2[i][j] = cc2 % N2
     return R1, R2
+
+
+def tri_window(A, N, rs, cs, upper):
+    """forward_sub_kernel_32 / backward_sub_kernel_32 (src/CuModMatrix/triangular/
+    substitution_inplace.jl:6-35, 63-88) on a list-of-rows matrix, entries outside
+    A read as the zero padding; returns the 32 x 32 window result."""
+    m, n = len(A), (len(A[0]) if A else 0)
+
+    def at(i, j):
+        return A[i][j] % N if 0 <= i < m and 0 <= j < n else 0
+
+    X = [[0] * 32 for _ in range(32)]
+    for c in range(32):
+        rows = range(31, -1, -1) if upper else range(32)
+        for r in rows:
+            ks = range(r + 1, 32) if upper else range(r)
+            s = sum(at(rs + r, cs + k) * X[k][c] for k in ks) % N
+            rhs = 1 if r == c else 0
+            X[r][c] = mod_inv(at(rs + r, rs + r), N) * (rhs - s + N) % N
+    return X
+
+
+def tri_inverse(A, N, upper):
+    """upper/lower_triangular_inverse_no_copy (triangular_inverse_no_copy.jl:18-477),
+    following the reference's three branches literally; returns the (n x m) result
+    as a list of rows, or None for the InverseNotDefinedException case."""
+    m, n = len(A), len(A[0])
+    X = [[0] * m for _ in range(n)]
+    if (m <= 32) if upper else (n <= 32):
+        W = tri_window(A, N, 0, 0, upper)
+        for r in range(min(32, n)):
+            for c in range(min(32, m)):
+                X[r][c] = W[r][c]
+        return X
+    if not upper and m > n:
+        return None
+
+    def put_window(lo, size):
+        W = tri_window(A, N, lo, lo, upper)
+        for r in range(size):
+            for c in range(size):
+                X[lo + r][lo + c] = W[r][c]
+
+    def combine(lo, mid, hi):
+        if upper:      # X12 = -(X11 A12) X22
+            T = [[sum(X[i][t] * A[t][j] for t in range(lo, mid)) % N for j in range(mid, hi)] for i in range(lo, mid)]
+            for i in range(lo, mid):
+                for j in range(mid, hi):
+                    X[i][j] = (N - sum(T[i - lo][t - mid] * X[t][j] for t in range(mid, hi)) % N) % N
+        else:          # X21 = -(X22 A21) X11
+            T = [[sum(X[i][t] * A[t][j] for t in range(mid, hi)) % N for j in range(lo, mid)] for i in range(mid, hi)]
+            for i in range(mid, hi):
+                for j in range(lo, mid):
+                    X[i][j] = (N - sum(T[i - mid][t - lo] * X[t][j] for t in range(lo, mid)) % N) % N
+
+    def rec(lo, hi):
+        if hi - lo <= 32:                                  # first branch
+            put_window(lo, hi - lo)
+            return
+        q = max(int((hi - lo) / 64 + 0.5), 1)
+        mid = lo + 32 * q
+        if mid - lo <= 32 and hi - mid <= 32:              # second branch: both halves by window
+            put_window(lo, mid - lo)
+            put_window(mid, hi - mid)
+        else:                                              # third branch
+            rec(lo, mid)
+            rec(mid, hi)
+        combine(lo, mid, hi)
+
+    rec(0, min(m, n))
+    return X

@@ -236,3 +236,65 @@ def test_karatsuba_reference_formula_is_not_the_product_when_n2_does_not_divide_
     x, y = 57 + N1 * 88, 91 + N1 * 77
     assert int(c1[0, 0]) + N1 * int(c2[0, 0]) == (x * y) % (N1 * N2)
     assert (R1[0][0], R2[0][0]) != (int(c1[0, 0]), int(c2[0, 0]))
+
+
+# ---- triangular inverses (src/CuModMatrix/triangular) ----
+
+@pytest.mark.parametrize("upper", [True, False])
+def test_triangular_oracle_kats(upper):
+    """The reference's own cases (test/CuModMatrix/triangular_test.jl): the 2 x 2
+    matrices mod 7, the identity mod 2, random triangles mod 13 (A * A_inv = I)."""
+    A = np.array([[1, 3], [0, 2]]) if upper else np.array([[1, 0], [3, 2]])
+    X, st = oracle.tri_inverse(A, 7, upper)
+    assert st == 0 and ((A @ X) % 7 == np.eye(2, dtype=np.int64)).all()
+    assert X.tolist() == ([[1, 2], [0, 4]] if upper else [[1, 0], [2, 4]])
+    X, st = oracle.tri_inverse(np.eye(200, dtype=np.int64), 2, upper)
+    assert st == 0 and (X == np.eye(200, dtype=np.int64)).all()
+    rng = np.random.default_rng(3)
+    for n in (33, 64, 65, 97, 160):
+        A = rng.integers(1, 13, size=(n, n))
+        A = np.triu(A) if upper else np.tril(A)
+        X, st = oracle.tri_inverse(A, 13, upper)
+        assert st == 0 and ((A @ X) % 13 == np.eye(n, dtype=np.int64)).all()
+
+
+def test_triangular_oracle_rectangular_and_errors():
+    rng = np.random.default_rng(4)
+    A = np.triu(rng.integers(1, 13, size=(100, 400)))            # wide upper: a right inverse
+    X, st = oracle.tri_inverse(A, 13, True)
+    assert st == 0 and X.shape == (400, 100) and ((A @ X) % 13 == np.eye(100, dtype=np.int64)).all()
+    A = np.triu(rng.integers(1, 13, size=(300, 90)))              # tall upper: the top square's inverse
+    X, st = oracle.tri_inverse(A, 13, True)
+    assert st == 0 and ((X @ A) % 13 == np.eye(90, dtype=np.int64)).all()
+    A = np.tril(rng.integers(1, 13, size=(90, 40)))               # tall lower beyond one window: exception
+    assert oracle.tri_inverse(A, 13, False)[1] == 2
+
+
+@pytest.mark.parametrize("seed", range(12))
+def test_triangular_oracle_matches_literal_restatement(seed):
+    """The C oracle against the three-branch Python restatement, including zero
+    diagonal entries (mod_inv(0) = 0) and composite moduli."""
+    rng = np.random.default_rng(100 + seed)
+    upper = bool(seed % 2)
+    m, n = int(rng.integers(1, 100)), int(rng.integers(1, 100))
+    if seed % 3 == 0:
+        n = m
+    N = int(rng.choice([2, 13, 1000, 65521, 67108859]))
+    A = rng.integers(0, N, size=(m, n))
+    A = np.triu(A) if upper else np.tril(A)
+    k = min(m, n)
+    A[rng.choice(k, size=max(1, k // 6), replace=False)[:, None].repeat(2, 1).T.tolist()] = 0
+    X, st = oracle.tri_inverse(A, N, upper)
+    P = pyref.tri_inverse(A.tolist(), N, upper)
+    assert (P is None and st == 2) or (st == 0 and (np.array(P, dtype=np.int64) == X).all())
+
+
+def test_triangular_window_shift_quirk():
+    """The window's diagonal is read at (row_shift + r, row_shift + r), its other
+    entries at column col_shift + k, as the reference's kernels do."""
+    rng = np.random.default_rng(8)
+    A = rng.integers(0, 97, size=(70, 70))
+    for upper in (True, False):
+        W = oracle.tri_window(A, 97, 5, 11, upper)
+        P = pyref.tri_window(A.tolist(), 97, 5, 11, upper)
+        assert W.tolist() == P
