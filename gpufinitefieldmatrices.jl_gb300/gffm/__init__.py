@@ -50,4 +50,5 @@ from . import autotune  # noqa: F401,E402
 from .triangular import (  # noqa: F401,E402
     InverseNotDefinedException, mod_inv, forward_sub_gpu_type_32, backward_sub_gpu_type_32,
     upper_triangular_inverse_no_copy, lower_triangular_inverse_no_copy, triangular_inverse_into_,
+    hensel_pseudoinverse,
 )

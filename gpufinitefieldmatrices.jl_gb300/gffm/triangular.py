@@ -89,5 +89,27 @@ def triangular_inverse_into_(X, A, upper):
     return X
 
 
+def hensel_pseudoinverse(N, precision, A, T):
+    """hensel_pseudoinverse(N, precision, A, T) (src/CuModMatrix/triangular/hensel.jl:13-20):
+    the Newton iteration T <- 2T - T(AT), doubling the precision, that lifts a
+    solution of AT = I mod N to one mod N^precision.  A and T are CuModMatrices;
+    all arithmetic is mod M = N^precision (2 <= M < 2^26 for the exact GEMM).
+    The reference returns a Nemo matrix over ZZ/M; here the result is a
+    CuModMatrix with modulus M."""
+    M = int(N) ** int(precision)
+    i = 1
+    T = cumod.change_modulus(T, M) if T.N != M else T
+    while i < precision:
+        AT = cumod.mat_mul_gpu_type(A, T, M)
+        TAT = cumod.mat_mul_gpu_type(T, AT, M)
+        T2 = cumod.similar(T, M)
+        cumod.scalar_mul_(T2, T, 2, M)
+        cumod.sub_(T2, T2, TAT, M)
+        T = T2
+        i *= 2
+    return T
+
+
 __all__ = ["InverseNotDefinedException", "mod_inv", "forward_sub_gpu_type_32", "backward_sub_gpu_type_32",
-           "upper_triangular_inverse_no_copy", "lower_triangular_inverse_no_copy", "triangular_inverse_into_"]
+           "upper_triangular_inverse_no_copy", "lower_triangular_inverse_no_copy", "triangular_inverse_into_",
+           "hensel_pseudoinverse"]

@@ -125,3 +125,27 @@ def test_divide_elements(gffm):
     out = gffm.divide_elements_(B, A, 7)
     assert out is A
     assert as_int(B).tolist() == [[0, 1, 1], [2, 0, 0]]
+
+
+@pytest.mark.parametrize("p,k,n", [(13, 4, 70), (101, 3, 40), (5, 9, 33)])
+def test_hensel_pseudoinverse(gffm, p, k, n):
+    """hensel_pseudoinverse (triangular/hensel.jl:13-20): lift A T = I mod p to mod p^k."""
+    M = p ** k
+    rng = np.random.default_rng(p + k + n)
+    Lo = np.tril(rng.integers(0, p, size=(n, n)))
+    Up = np.triu(rng.integers(0, p, size=(n, n)))
+    d = np.arange(n)
+    Lo[d, d] = rng.integers(1, p, size=n)
+    Up[d, d] = rng.integers(1, p, size=n)
+    A = oracle.matmul(Lo, Up, M)                                   # invertible mod p
+    T0 = oracle.matmul(oracle.tri_inverse(Up % p, p, True)[0], oracle.tri_inverse(Lo % p, p, False)[0], p)
+    assert (oracle.matmul(A % p, T0, p) == np.eye(n, dtype=np.int64)).all()
+    want, i = T0 % M, 1
+    while i < k:                                                   # the iteration itself, on the oracle's GEMM
+        want = (2 * want - oracle.matmul(want, oracle.matmul(A, want, M), M)) % M
+        i *= 2
+    got = gffm.hensel_pseudoinverse(p, k, gffm.CuModMatrix(A, M, elem_type=torch.float64),
+                                    gffm.CuModMatrix(T0, M, elem_type=torch.float64))
+    assert got.N == M
+    np.testing.assert_array_equal(as_int(got), want)
+    assert (oracle.matmul(A, want, M) == np.eye(n, dtype=np.int64)).all()
