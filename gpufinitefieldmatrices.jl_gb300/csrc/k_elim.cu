@@ -257,6 +257,7 @@ struct Work {
     int32_t *ptmp;                               // MAX_PERM_ROWS x n row-permutation scratch
     int32_t *qlist;                              // [n] skipped columns
     __half *dA, *dB;                             // digit planes
+    __half *dA2;                                 // digit planes of the next panel's columns (lookahead)
     limb::Layout gl;
     int plain = 0;                               // trailing products on the plain Float64 method
     int64_t stripe = 1;                          // its stripe: find_max_stripe_ops(Float64, N)
@@ -264,12 +265,12 @@ struct Work {
 
 static size_t al(size_t x) { return (x + 255) & ~size_t(255); }
 
-static void layout_ws(int64_t m, int64_t n, int64_t lcols, size_t *total, size_t off[16], limb::Layout *gl) {
+static void layout_ws(int64_t m, int64_t n, int64_t lcols, size_t *total, size_t off[17], limb::Layout *gl) {
     const int64_t ldw = gffm::round_up(n > 0 ? n : 1, 32);
     // digit planes large enough for any trailing update / back substitution of
     // this problem: operands n x NB and NB x m (4 digits)
     *gl = limb::layout(std::max<int64_t>(n, 1), std::max<int64_t>(m, 1), NB, int64_t(1) << 25);
-    size_t sizes[16] = {
+    size_t sizes[17] = {
         (size_t)std::max<int64_t>(m, 1) * ldw * 4,      // W
         (size_t)2 * MAX_PANEL_CTAS * sizeof(Rec),       // rec
         (size_t)NB * NB * 4,                            // linv
@@ -282,9 +283,10 @@ static void layout_ws(int64_t m, int64_t n, int64_t lcols, size_t *total, size_t
         (size_t)std::max<int64_t>(std::min(m, n), 1) * 4,  // pcol
         (size_t)std::max<int64_t>(m, 1) * NB * 4,       // gather
         gl->a_bytes, gl->b_bytes,
-        (size_t)NB * NB * 4 + (size_t)std::max<int64_t>(n, 1) * 4};  // coef, qlist
+        (size_t)NB * NB * 4 + (size_t)std::max<int64_t>(n, 1) * 4,  // coef, qlist
+        limb::layout(NB, std::max<int64_t>(m, 1), NB, int64_t(1) << 25).a_bytes};  // dA2
     size_t o = 0;
-    for (int i = 0; i < 16; i++) {
+    for (int i = 0; i < 17; i++) {
         off[i] = o;
         o += al(sizes[i]);
     }
@@ -292,7 +294,7 @@ static void layout_ws(int64_t m, int64_t n, int64_t lcols, size_t *total, size_t
 }
 
 static void bind_ws(void *base, int64_t m, int64_t n, int64_t lcols, Work *w) {
-    size_t total, off[16];
+    size_t total, off[17];
     layout_ws(m, n, lcols, &total, off, &w->gl);
     uint8_t *b = static_cast<uint8_t *>(base);
     w->W = (int32_t *)(b + off[0]);
@@ -315,10 +317,11 @@ static void bind_ws(void *base, int64_t m, int64_t n, int64_t lcols, Work *w) {
     w->dB = (__half *)(b + off[14]);
     w->coef = (int32_t *)(b + off[15]);
     w->qlist = w->coef + NB * NB;
+    w->dA2 = (__half *)(b + off[16]);
 }
 
 size_t workspace_bytes(int64_t m, int64_t n, int64_t lcols) {
-    size_t total, off[16];
+    size_t total, off[17];
     limb::Layout gl;
     layout_ws(m, n, lcols, &total, off, &gl);
     return total;
@@ -458,15 +461,21 @@ static int permute_rows(Work &w, const PermArgs &perm, int c_lo, int c_hi, cudaS
 }
 
 static int run_panel(Work &w, int m, int n, int R0, int C0, int nbw, const ModP &M, int lcols_check,
-                     cudaStream_t s, int h_res[2], std::vector<int32_t> &h_prow, std::vector<int32_t> &h_pv) {
+                     cudaStream_t s, int h_res[2], std::vector<int32_t> &h_prow, std::vector<int32_t> &h_pv,
+                     int max_g = 0) {
     using namespace gffm;
     const int rows = m - R0;
     const int sms = sm_count();
-    // rows per CTA: at least 64, and at most 64 CTAs while the rows fit (the per-step
-    // exchange moves G candidate rows into every CTA)
+    // rows per CTA: at least 64, and at most 128 CTAs while the rows fit (the per-step
+    // exchange moves G candidate rows into every CTA); at most max_g CTAs when the
+    // panel shares the GPU with a trailing update
     int R = 64;
-    while ((rows + R - 1) / R > std::min(sms, 128) && R < 640) R += 32;
-    while ((rows + R - 1) / R > std::min(sms, MAX_PANEL_CTAS)) R += 32;
+    if (max_g > 0) {
+        while ((rows + R - 1) / R > max_g) R += 32;
+    } else {
+        while ((rows + R - 1) / R > std::min(sms, 128) && R < 640) R += 32;
+        while ((rows + R - 1) / R > std::min(sms, MAX_PANEL_CTAS)) R += 32;
+    }
     const int G = std::max(1, (rows + R - 1) / R);
     const size_t smem = (size_t)R * NB * 4;
     if (smem > 200 * 1024)
@@ -502,6 +511,61 @@ static int run_panel(Work &w, int m, int n, int R0, int C0, int nbw, const ModP 
 }
 
 // Forward elimination shared by PLUQ / LU / RREF.
+// Lookahead: while the next panel factors on a few CTAs, the trailing update of the
+// columns past it runs beside it on the other SMs (a second stream).  The next
+// panel's own columns are updated first, on the whole GPU.
+static int look_ctas(int rows) {
+    const int gmin = (rows + 383) / 384;   // the panel keeps at most 384 rows per CTA
+    return std::max(gmin, std::min(32, (rows + 63) / 64));
+}
+
+struct Lookahead {
+    cudaStream_t s = nullptr, s2 = nullptr;
+    cudaEvent_t ea = nullptr, eb = nullptr;
+    bool pending = false;   // the side update is in flight on s2
+    int next_g = 0;         // CTA cap of the panel that runs beside it
+    ~Lookahead() {          // every exit path: s (and the workspace's release on it) follows s2
+        if (pending) cudaStreamWaitEvent(s, eb, 0);
+        if (ea) cudaEventDestroy(ea);
+        if (eb) cudaEventDestroy(eb);
+        if (s2) cudaStreamDestroy(s2);
+    }
+    int join() {
+        if (pending) GFFM_CUDA(cudaStreamWaitEvent(s, eb, 0));
+        pending = false;
+        next_g = 0;
+        return GFFM_OK;
+    }
+};
+
+// A22 -= L21 U12 for the rows below the panel: the next panel's NB columns on s with
+// every SM, then the remaining columns on s2 with all SMs but the next panel's.  The
+// digit planes of L21 are split once and shared.
+static int update_lookahead(Work &w, int64_t N, int row, int t, int col, int cs, int m, int n, Lookahead &la) {
+    const int rows_b = m - row - t, look = NB, rest = n - cs - NB;
+    const int32_t *X = w.W + (int64_t)(row + t) * w.ldw + col;   // L21: rows_b x t
+    const int32_t *Y = w.W + (int64_t)row * w.ldw + cs;          // U12: t x (n - cs)
+    int32_t *C = w.W + (int64_t)(row + t) * w.ldw + cs;
+    const limb::Layout ga = limb::layout(look, rows_b, t, N), gb = limb::layout(rest, rows_b, t, N);
+    int st = limb::split_b<int32_t>(X, w.ldw, t, rows_b, w.dB, gb, N, la.s);
+    if (st) return st;
+    st = limb::split_a<int32_t>(Y, w.ldw, look, t, w.dA2, ga, N, la.s);
+    if (st) return st;
+    st = limb::split_a<int32_t>(Y + look, w.ldw, rest, t, w.dA, gb, N, la.s);
+    if (st) return st;
+    st = limb::gemm_digits(ga, w.dA2, w.dB, look, rows_b, t, N, C, w.ldw, limb::EPI_SUB_I32, 0, la.s);
+    if (st) return st;
+    GFFM_CUDA(cudaEventRecord(la.ea, la.s));
+    GFFM_CUDA(cudaStreamWaitEvent(la.s2, la.ea, 0));
+    la.next_g = look_ctas(rows_b);
+    st = limb::gemm_digits(gb, w.dA, w.dB, rest, rows_b, t, N, C + look, w.ldw, limb::EPI_SUB_I32,
+                           gffm::sm_count() - la.next_g, la.s2);
+    if (st) return st;
+    GFFM_CUDA(cudaEventRecord(la.eb, la.s2));
+    la.pending = true;
+    return GFFM_OK;
+}
+
 static int forward(Work &w, int m, int n, int64_t N, int mode, int lcols, cudaStream_t s, Result &res) {
     using namespace gffm;
     ModP M{(uint32_t)N, ~uint64_t(0) / (uint64_t)N};
@@ -512,9 +576,21 @@ static int forward(Work &w, int m, int n, int64_t N, int mode, int lcols, cudaSt
     int row = 0, col = 0;
     res.perm.resize(m);
     for (int i = 0; i < m; i++) res.perm[i] = i;
+    Lookahead la;
+    la.s = s;
+    const bool use_look = !w.plain;
+    if (use_look) {
+        GFFM_CUDA(cudaStreamCreateWithFlags(&la.s2, cudaStreamNonBlocking));
+        GFFM_CUDA(cudaEventCreateWithFlags(&la.ea, cudaEventDisableTiming));
+        GFFM_CUDA(cudaEventCreateWithFlags(&la.eb, cudaEventDisableTiming));
+    }
     while (row < m && col < n) {
         const int nbw = std::min(NB, n - col);
-        int st = run_panel(w, m, n, row, col, nbw, M, mode == MODE_PLUQ ? lcols : 0, s, h_res, h_prow, h_pv);
+        int st = run_panel(w, m, n, row, col, nbw, M, mode == MODE_PLUQ ? lcols : 0, s, h_res, h_prow, h_pv,
+                           la.pending ? la.next_g : 0);
+        if (st) return st;
+        // everything after the panel may touch the columns the side update writes
+        st = la.join();
         if (st) return st;
         const int t = h_res[0], status = h_res[1];
         if (status == PS_TIMEOUT) return set_error(GFFM_ERR_TIMEOUT, "elimination panel: a device-side wait gave up");
@@ -580,10 +656,13 @@ static int forward(Work &w, int m, int n, int64_t N, int mode, int lcols, cudaSt
                                    w.W + (int64_t)row * w.ldw + cs, w.ldw, t, n - cs, t, limb::EPI_STORE_I32, s);
                 if (st) return st;
                 if (row + t < m) {
-                    st = rowmajor_gemm(w, N, w.W + (int64_t)(row + t) * w.ldw + cs, w.ldw,
-                                       w.W + (int64_t)(row + t) * w.ldw + col, w.ldw,
-                                       w.W + (int64_t)row * w.ldw + cs, w.ldw, m - row - t, n - cs, t,
-                                       limb::EPI_SUB_I32, s);
+                    if (use_look && t == nbw && n - cs > NB && m - row - t >= 1024)
+                        st = update_lookahead(w, N, row, t, col, cs, m, n, la);
+                    else
+                        st = rowmajor_gemm(w, N, w.W + (int64_t)(row + t) * w.ldw + cs, w.ldw,
+                                           w.W + (int64_t)(row + t) * w.ldw + col, w.ldw,
+                                           w.W + (int64_t)row * w.ldw + cs, w.ldw, m - row - t, n - cs, t,
+                                           limb::EPI_SUB_I32, s);
                     if (st) return st;
                 }
             }

@@ -92,6 +92,27 @@ def test_pluq_matches_oracle(gffm, case):
     status_ok(gffm)
 
 
+# Sizes where the next panel factors beside the previous panel's trailing update
+# (at least 1024 rows below the panel and more than one panel of columns left).
+LOOKAHEAD = [("uniform", 1400, 1400, P26), ("uniform", 1500, 700, 65521), ("uniform", 1300, 2000, P25),
+             ("rank1200", 1400, 1400, P26), ("zero_cols", 1300, 1350, 13), ("ties", 1200, 1200, 3)]
+
+
+@pytest.mark.parametrize("case", LOOKAHEAD, ids=lambda c: "%s-%dx%d-%d" % c)
+def test_pluq_lookahead_sizes_match_oracle(gffm, case):
+    test_pluq_matches_oracle(gffm, case)
+
+
+def test_rref_lookahead_size_matches_oracle(gffm):
+    rng = np.random.default_rng(77)
+    A = make("rank1100", 1300, 1400, P26, rng)
+    R, rank, piv = gffm.rref_gpu_type(gffm.CuModMatrix(A, P26, elem_type=torch.float64), return_pivots=True)
+    R0, rank0, piv0 = oracle.rref(A, P26)
+    assert rank == rank0 == 1100 and piv == [c + 1 for c in piv0]
+    assert np.array_equal(as_int(R), R0)
+    status_ok(gffm)
+
+
 def test_pluq_config2_rank900(gffm):
     """1024 x 1024 of rank 900 mod the largest prime below 2^26: (1024x900)(900x1024)."""
     rng = np.random.default_rng(900)
