@@ -44,6 +44,7 @@ struct PanelArgs {
     Rec *rec;          // [2][G], keys zero at launch
     int32_t *old_row;  // [2][NB]
     int32_t *piv_row, *piv_val, *piv_inv;  // [NB]
+    int32_t *linv;     // k_panel1: L11^{-1} of the panel's pivots, row-major, ld NB
     int *result;       // [0] pivots, [1] status
     int *err;
 };
@@ -299,6 +300,198 @@ __global__ void __launch_bounds__(PANEL_THREADS, 1) k_panel(PanelArgs a) {
     if (b == 0 && tid == 0) {
         a.result[0] = t;
         a.result[1] = s_status;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Single-CTA panel: the same factorization step as k_panel for a panel of at
+// most P1_NB columns whose rows (at most P1_MAX_ROWS) fit one CTA's shared
+// memory, without the grid-wide exchange.  Left-looking: column t is brought up
+// to date when the pivot search reaches it,
+//   U[0:t][t] = Linv W[0:t][t],    v[r] = W[r][t] + sum_{s<t} (N - l[r][s]) U[s][t],
+// Linv the inverse of the panel's lower-triangular factor (pivots on its
+// diagonal), grown by one row per pivot.  Pivot t-1 is applied while column t is
+// prepared: warp 7 computes its inverse, warps 0 and 2 swap the rows, warp 1
+// forms U[s][t] for s < t-1, warp 2 Linv's new row before scaling, warps 0-6 the
+// partial values of column t.  The panel is written back as k_panel leaves it:
+// pivot rows scaled (U), the multipliers unscaled below the pivots, the columns
+// after a stop brought up to date.  No waits outside CTA barriers.
+constexpr int P1_NB = 32;
+constexpr int P1_THREADS = 256;
+constexpr int P1_INV_WARP = 7;
+constexpr int P1_MAX_ROWS = 1536;
+__host__ __device__ constexpr size_t p1_smem_bytes(int rows) { return (size_t)P1_NB * (size_t)(rows + 4) * 4; }
+
+__device__ __forceinline__ uint32_t p1_red(uint64_t x, const ModP &M) {
+    return (uint32_t)gffm_dev::barrett64(x, M.n, M.minv);
+}
+// sum_{s < n8} a[s * sa] * b[s * sb], n8 a multiple of 8, at most 32 products below 2^52
+__device__ __forceinline__ uint64_t p1_dot8(const uint32_t *a, int sa, const uint32_t *b, int sb, int n8) {
+    uint64_t x0 = 0, x1 = 0, x2 = 0, x3 = 0;
+    for (int q = 0; q < n8; q += 8) {
+        uint32_t va[8], vb[8];
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+            va[k] = a[(q + k) * sa];
+            vb[k] = b[(q + k) * sb];
+        }
+        x0 += (uint64_t)va[0] * vb[0] + (uint64_t)va[4] * vb[4];
+        x1 += (uint64_t)va[1] * vb[1] + (uint64_t)va[5] * vb[5];
+        x2 += (uint64_t)va[2] * vb[2] + (uint64_t)va[6] * vb[6];
+        x3 += (uint64_t)va[3] * vb[3] + (uint64_t)va[7] * vb[7];
+    }
+    return (x0 + x1) + (x2 + x3);
+}
+__device__ __forceinline__ void p1_named_sync(int id, int nthreads) {
+    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
+}
+
+__global__ void __launch_bounds__(P1_THREADS, 1) k_panel1(PanelArgs a) {
+    extern __shared__ __align__(16) int32_t p1s[];
+    __shared__ uint32_t Lv[P1_NB * 33];   // Linv[t][s] at Lv[t * 33 + s], zero above the diagonal
+    __shared__ uint32_t s_ut[P1_NB];
+    __shared__ unsigned long long red[P1_THREADS / 32];
+    __shared__ uint32_t s_inv;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int r0 = a.R0, c0 = a.C0, m = a.m, R = m - r0, nbc = a.nbw;
+    const int rs = R + 4;
+    const ModP M = a.M;
+    const uint32_t N = M.n;
+    int32_t *P = p1s;                       // P[j * rs + lr]: panel column j, local row lr
+    const uint32_t *Pu = reinterpret_cast<const uint32_t *>(P);
+    for (int idx = tid; idx < R * nbc; idx += blockDim.x) {
+        const int lr = idx / nbc, j = idx - lr * nbc;
+        P[j * rs + lr] = a.W[(int64_t)(r0 + lr) * a.ldw + c0 + j];
+    }
+    for (int idx = tid; idx < P1_NB * 33; idx += blockDim.x) Lv[idx] = 0;
+    __syncthreads();
+
+    int npiv = 0, status = PS_DONE;
+    uint32_t ppv = 0;
+    int pplr = 0;
+    for (int t = 0;; t++) {
+        uint32_t g = 0;   // U[t-1][t]
+        if (t > 0) {
+            const int tp = t - 1;
+            const bool nxt = t < nbc && r0 + t < m;
+            const int tp8 = (tp + 7) & ~7;
+            uint64_t lsum = 0;
+            if (warp == P1_INV_WARP) {
+                const uint32_t inv = mod_inv_euclid_alu(ppv, N);
+                if (lane == 0) s_inv = inv;
+            } else {
+                if (warp == 0) {
+                    if (lane >= tp && lane < nbc) {
+                        int32_t *colp = P + lane * rs;
+                        if (lane == tp) {
+                            colp[pplr] = colp[tp];
+                        } else if (pplr != tp) {
+                            const int32_t x = colp[tp];
+                            colp[tp] = colp[pplr];
+                            colp[pplr] = x;
+                        }
+                    }
+                } else if (warp == 1) {
+                    if (nxt) {
+                        const uint64_t acc = p1_dot8(Lv + lane * 33, 1, Pu + t * rs, 1, tp8);
+                        s_ut[lane] = lane < tp ? p1_red(acc, M) : 0u;
+                    }
+                } else if (warp == 2) {
+                    if (lane < tp && pplr != tp) {
+                        int32_t *colp = P + lane * rs;
+                        const int32_t x = colp[tp];
+                        colp[tp] = colp[pplr];
+                        colp[pplr] = x;
+                    }
+                    __syncwarp();
+                    lsum = p1_dot8(Pu + tp, rs, Lv + lane, 33, tp8);
+                }
+                if (nxt) {
+                    p1_named_sync(1, P1_INV_WARP * 32);
+                    for (int lr = tp + tid; lr < R; lr += P1_INV_WARP * 32)
+                        P[t * rs + lr] = (int32_t)p1_red((uint32_t)P[t * rs + lr] + p1_dot8(Pu + lr, rs, s_ut, 1, tp8), M);
+                }
+            }
+            __syncthreads();
+            const uint32_t inv = s_inv;
+            if (warp == 2)
+                Lv[tp * 33 + lane] = lane < tp ? mulmod(p1_red(lsum, M), inv, M) : (lane == tp ? inv : 0u);
+            if (tid == 0) {
+                P[tp * rs + tp] = (int32_t)mulmod(ppv, inv, M);   // U's diagonal
+                a.piv_inv[tp] = (int32_t)inv;
+            }
+            if (!nxt) break;
+            g = mulmod((uint32_t)P[t * rs + tp], inv, M);
+            if (warp == 0 && lane == 0) s_ut[tp] = g;
+        }
+        // column t below its pivot rows, and its largest residue (lowest row on ties)
+        unsigned long long best = 0;
+        for (int lr = t + tid; lr < R; lr += P1_THREADS) {
+            uint32_t v = (uint32_t)P[t * rs + lr];
+            if (t > 0) v = p1_red((uint64_t)v + (uint64_t)(uint32_t)P[(t - 1) * rs + lr] * g, M);
+            P[t * rs + lr] = v ? (int32_t)(N - v) : 0;
+            const unsigned long long key = ((unsigned long long)v << 32) | (0xFFFFFFFFu - (uint32_t)lr);
+            best = key > best ? key : best;
+        }
+        best = warp_max_u64(best);
+        if (lane == 0) red[warp] = best;
+        __syncthreads();
+        best = lane < P1_THREADS / 32 ? red[lane] : 0ull;
+#pragma unroll
+        for (int o = 4; o > 0; o >>= 1) {
+            const unsigned long long x = __shfl_xor_sync(0xffffffffu, best, o);
+            best = x > best ? x : best;
+        }
+        best = __shfl_sync(0xffffffffu, best, 0);
+        const uint32_t pv = (uint32_t)(best >> 32);
+        if (warp == 0 && lane < t) P[t * rs + lane] = (int32_t)s_ut[lane];
+        if (pv == 0) {
+            status = PS_ZERO_COL;
+            break;
+        }
+        if (a.l_cols > 0 && c0 + t >= a.l_cols) {
+            status = PS_BOUNDS;
+            break;
+        }
+        pplr = (int)(0xFFFFFFFFu - (uint32_t)(best & 0xFFFFFFFFu));
+        ppv = pv;
+        if (tid == 0) {
+            a.piv_row[t] = r0 + pplr;
+            a.piv_val[t] = (int32_t)pv;
+        }
+        npiv = t + 1;
+    }
+    __syncthreads();
+    // the columns after a stop (a zero column is final already): values above the
+    // pivot rows by Linv, the rows below by the multipliers
+    const int np8 = (npiv + 7) & ~7;
+    for (int j = npiv + (status == PS_ZERO_COL ? 1 : 0); npiv > 0 && j < nbc; j++) {
+        if (warp == 0) {
+            const uint64_t acc = p1_dot8(Lv + lane * 33, 1, Pu + j * rs, 1, np8);
+            s_ut[lane] = lane < npiv ? p1_red(acc, M) : 0u;
+        }
+        __syncthreads();
+        for (int lr = npiv + tid; lr < R; lr += P1_THREADS)
+            P[j * rs + lr] = (int32_t)p1_red((uint32_t)P[j * rs + lr] + p1_dot8(Pu + lr, rs, s_ut, 1, np8), M);
+        if (tid < npiv) P[j * rs + tid] = (int32_t)s_ut[tid];
+        __syncthreads();
+    }
+    // back to W: pivot columns hold U on and above the diagonal and the unscaled
+    // multipliers below it; the other columns their current residues
+    for (int idx = tid; idx < R * nbc; idx += blockDim.x) {
+        const int lr = idx / nbc, j = idx - lr * nbc;
+        uint32_t x = (uint32_t)P[j * rs + lr];
+        if (j < npiv && lr > j) x = x ? N - x : 0u;
+        a.W[(int64_t)(r0 + lr) * a.ldw + c0 + j] = (int32_t)x;
+    }
+    // L11^{-1} for the U12 product (what k_linv computes for the cooperative panel)
+    for (int idx = tid; idx < npiv * npiv; idx += blockDim.x) {
+        const int i = idx / npiv, j = idx - i * npiv;
+        a.linv[i * NB + j] = (int32_t)Lv[i * 33 + j];
+    }
+    if (tid == 0) {
+        a.result[0] = npiv;
+        a.result[1] = status;
     }
 }
 

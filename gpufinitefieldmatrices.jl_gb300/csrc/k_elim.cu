@@ -477,10 +477,11 @@ static int run_panel(Work &w, int m, int n, int R0, int C0, int nbw, const ModP 
         while ((rows + R - 1) / R > std::min(sms, MAX_PANEL_CTAS)) R += 32;
     }
     const int G = std::max(1, (rows + R - 1) / R);
-    const size_t smem = (size_t)R * NB * 4;
+    const bool one = rows <= P1_MAX_ROWS && nbw <= P1_NB;   // the whole panel in one CTA
+    const size_t smem = one ? p1_smem_bytes(rows) : (size_t)R * NB * 4;
     if (smem > 200 * 1024)
         return set_error(GFFM_ERR_UNSUPPORTED, "elimination panel: %d rows exceed the panel kernel's capacity", rows);
-    GFFM_CUDA(cudaMemsetAsync(w.rec, 0, (size_t)2 * G * sizeof(Rec), s));
+    if (!one) GFFM_CUDA(cudaMemsetAsync(w.rec, 0, (size_t)2 * G * sizeof(Rec), s));
     PanelArgs a;
     a.W = w.W;
     a.ldw = w.ldw;
@@ -498,11 +499,18 @@ static int run_panel(Work &w, int m, int n, int R0, int C0, int nbw, const ModP 
     a.piv_row = w.piv_row;
     a.piv_val = w.piv_val;
     a.piv_inv = w.piv_inv;
+    a.linv = w.linv;
     a.result = w.result;
     a.err = device_error_flag();
-    GFFM_CUDA(cudaFuncSetAttribute(k_panel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    void *args[] = {&a};
-    GFFM_CUDA(cudaLaunchCooperativeKernel((void *)k_panel, dim3(G), dim3(PANEL_THREADS), args, smem, s));
+    if (one) {
+        GFFM_CUDA(cudaFuncSetAttribute(k_panel1, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        k_panel1<<<1, P1_THREADS, smem, s>>>(a);
+        GFFM_LAUNCH_CHECK("k_panel1");
+    } else {
+        GFFM_CUDA(cudaFuncSetAttribute(k_panel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        void *args[] = {&a};
+        GFFM_CUDA(cudaLaunchCooperativeKernel((void *)k_panel, dim3(G), dim3(PANEL_THREADS), args, smem, s));
+    }
     GFFM_CUDA(cudaMemcpyAsync(h_res, w.result, 2 * sizeof(int), cudaMemcpyDeviceToHost, s));
     GFFM_CUDA(cudaMemcpyAsync(h_prow.data(), w.piv_row, NB * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
     GFFM_CUDA(cudaMemcpyAsync(h_pv.data(), w.piv_val, NB * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
@@ -511,7 +519,8 @@ static int run_panel(Work &w, int m, int n, int R0, int C0, int nbw, const ModP 
 }
 
 // Forward elimination shared by PLUQ / LU / RREF.
-// Lookahead: while the next panel factors on a few CTAs, the trailing update of the
+// Lookahead: while the next panel factors on a few CTAs (one CTA once its rows fit
+// one), the trailing update of the
 // columns past it runs beside it on the other SMs (a second stream).  The next
 // panel's own columns are updated first, on the whole GPU.
 static int look_ctas(int rows) {
@@ -541,8 +550,9 @@ struct Lookahead {
 // A22 -= L21 U12 for the rows below the panel: the next panel's NB columns on s with
 // every SM, then the remaining columns on s2 with all SMs but the next panel's.  The
 // digit planes of L21 are split once and shared.
-static int update_lookahead(Work &w, int64_t N, int row, int t, int col, int cs, int m, int n, Lookahead &la) {
-    const int rows_b = m - row - t, look = NB, rest = n - cs - NB;
+static int update_lookahead(Work &w, int64_t N, int row, int t, int col, int cs, int m, int n, int look,
+                            Lookahead &la) {
+    const int rows_b = m - row - t, rest = n - cs - look;
     const int32_t *X = w.W + (int64_t)(row + t) * w.ldw + col;   // L21: rows_b x t
     const int32_t *Y = w.W + (int64_t)row * w.ldw + cs;          // U12: t x (n - cs)
     int32_t *C = w.W + (int64_t)(row + t) * w.ldw + cs;
@@ -557,7 +567,7 @@ static int update_lookahead(Work &w, int64_t N, int row, int t, int col, int cs,
     if (st) return st;
     GFFM_CUDA(cudaEventRecord(la.ea, la.s));
     GFFM_CUDA(cudaStreamWaitEvent(la.s2, la.ea, 0));
-    la.next_g = look_ctas(rows_b);
+    la.next_g = rows_b <= P1_MAX_ROWS ? 1 : look_ctas(rows_b);   // the next panel's CTAs
     st = limb::gemm_digits(gb, w.dA, w.dB, rest, rows_b, t, N, C + look, w.ldw, limb::EPI_SUB_I32,
                            gffm::sm_count() - la.next_g, la.s2);
     if (st) return st;
@@ -585,7 +595,8 @@ static int forward(Work &w, int m, int n, int64_t N, int mode, int lcols, cudaSt
         GFFM_CUDA(cudaEventCreateWithFlags(&la.eb, cudaEventDisableTiming));
     }
     while (row < m && col < n) {
-        const int nbw = std::min(NB, n - col);
+        // panels of 32 in one CTA once the rows fit it, of NB across CTAs before
+        const int nbw = std::min(m - row <= P1_MAX_ROWS ? P1_NB : NB, n - col);
         int st = run_panel(w, m, n, row, col, nbw, M, mode == MODE_PLUQ ? lcols : 0, s, h_res, h_prow, h_pv,
                            la.pending ? la.next_g : 0);
         if (st) return st;
@@ -648,16 +659,19 @@ static int forward(Work &w, int m, int n, int64_t N, int mode, int lcols, cudaSt
             if (cs < n) {
                 st = permute_rows(w, perm, cs, n, s);
                 if (st) return st;
-                // U12 = L11^{-1} P A12
-                GFFM_CUDA(cudaFuncSetAttribute(k_linv, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)LINV_SMEM));
-                k_linv<<<NB / 32, 1024, LINV_SMEM, s>>>(w.W, w.ldw, row, col, t, w.piv_inv, w.linv, M);
-                GFFM_LAUNCH_CHECK("k_linv");
+                // U12 = L11^{-1} P A12 (a single-CTA panel has written L11^{-1} already)
+                if (nbw > P1_NB || m - row > P1_MAX_ROWS) {
+                    GFFM_CUDA(cudaFuncSetAttribute(k_linv, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)LINV_SMEM));
+                    k_linv<<<NB / 32, 1024, LINV_SMEM, s>>>(w.W, w.ldw, row, col, t, w.piv_inv, w.linv, M);
+                    GFFM_LAUNCH_CHECK("k_linv");
+                }
                 st = rowmajor_gemm(w, N, w.W + (int64_t)row * w.ldw + cs, w.ldw, w.linv, NB,
                                    w.W + (int64_t)row * w.ldw + cs, w.ldw, t, n - cs, t, limb::EPI_STORE_I32, s);
                 if (st) return st;
                 if (row + t < m) {
-                    if (use_look && t == nbw && n - cs > NB && m - row - t >= 1024)
-                        st = update_lookahead(w, N, row, t, col, cs, m, n, la);
+                    const int look = m - row - t <= P1_MAX_ROWS ? P1_NB : NB;   // the next panel's width
+                    if (use_look && t == nbw && n - cs > look && m - row - t >= 1024)
+                        st = update_lookahead(w, N, row, t, col, cs, m, n, look, la);
                     else
                         st = rowmajor_gemm(w, N, w.W + (int64_t)(row + t) * w.ldw + cs, w.ldw,
                                            w.W + (int64_t)(row + t) * w.ldw + col, w.ldw,
