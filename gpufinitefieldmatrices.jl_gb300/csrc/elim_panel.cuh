@@ -552,22 +552,25 @@ struct PermArgs {
     int32_t src[MAX_PERM_ROWS];
 };
 
-// Two passes through a K x ncols scratch copy (both fully parallel and coalesced):
-// k_rows_gather: tmp[k][j] = W[rows[k]][c_lo + j];  k_rows_scatter: W[rows[k]][c_lo + j] = tmp[src[k]][j].
-__global__ void __launch_bounds__(256) k_rows_gather(const int32_t *__restrict__ W, int64_t ldw, int c_lo, int ncols,
-                                                     int32_t *__restrict__ tmp, const __grid_constant__ PermArgs p) {
-    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= (int64_t)p.K * ncols) return;
-    const int k = (int)(e / ncols), j = (int)(e - (int64_t)k * ncols);
-    tmp[e] = W[(int64_t)p.rows[k] * ldw + c_lo + j];
-}
-__global__ void __launch_bounds__(256) k_rows_scatter(int32_t *__restrict__ W, int64_t ldw, int c_lo, int ncols,
-                                                      const int32_t *__restrict__ tmp,
-                                                      const __grid_constant__ PermArgs p) {
-    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= (int64_t)p.K * ncols) return;
-    const int k = (int)(e / ncols), j = (int)(e - (int64_t)k * ncols);
-    W[(int64_t)p.rows[k] * ldw + c_lo + j] = tmp[(int64_t)p.src[k] * ncols + j];
+// Columns [0, c_left) and [c_lo, c_hi) in one launch: block b stages the K moved
+// rows' values of 32 consecutive columns in shared memory (K x 32 words), then
+// writes row rows[k] <- staged row src[k].
+__global__ void __launch_bounds__(256) k_rows_permute(int32_t *__restrict__ W, int64_t ldw, int c_left, int c_lo,
+                                                      int c_hi, const __grid_constant__ PermArgs p) {
+    extern __shared__ int32_t staged[];
+    const int nleft = (c_left + 31) / 32;
+    const int g = blockIdx.x;
+    const int cbase = g < nleft ? 32 * g : c_lo + 32 * (g - nleft);
+    const int width = min(32, (g < nleft ? c_left : c_hi) - cbase);
+    for (int e = threadIdx.x; e < p.K * 32; e += blockDim.x) {
+        const int k = e >> 5, j = e & 31;
+        if (j < width) staged[e] = W[(int64_t)p.rows[k] * ldw + cbase + j];
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < p.K * 32; e += blockDim.x) {
+        const int k = e >> 5, j = e & 31;
+        if (j < width) W[(int64_t)p.rows[k] * ldw + cbase + j] = staged[p.src[k] * 32 + j];
+    }
 }
 
 }  // namespace elim

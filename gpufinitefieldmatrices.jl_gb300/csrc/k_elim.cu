@@ -79,7 +79,7 @@ __global__ void __launch_bounds__(256) k_to_rowmajor(const T *__restrict__ A, in
 }
 
 // Skipped (swapped-in, never eliminated) columns: the panel's row swaps for
-// columns at or beyond lo (those below lo were covered by permute_rows), then the
+// columns at or beyond lo (those below lo were covered by permute_rows2), then the
 // scaling of every new pivot row, as swap_rows_and_mod does over all columns.
 __global__ void k_skipped(int32_t *W, int64_t ldw, const int32_t *qlist, int nq, int lo, int R0, int t,
                           const int32_t *prow, const int32_t *inv, ModP M) {
@@ -254,7 +254,6 @@ struct Work {
     int32_t *gather;                             // m x NB
     int32_t *coef;                               // NB x NB
     int32_t *linv;                               // NB x NB, inverse of the panel's L11
-    int32_t *ptmp;                               // MAX_PERM_ROWS x n row-permutation scratch
     int32_t *qlist;                              // [n] skipped columns
     __half *dA, *dB;                             // digit planes
     __half *dA2;                                 // digit planes of the next panel's columns (lookahead)
@@ -265,17 +264,16 @@ struct Work {
 
 static size_t al(size_t x) { return (x + 255) & ~size_t(255); }
 
-static void layout_ws(int64_t m, int64_t n, int64_t lcols, size_t *total, size_t off[17], limb::Layout *gl) {
+static void layout_ws(int64_t m, int64_t n, int64_t lcols, size_t *total, size_t off[16], limb::Layout *gl) {
     const int64_t ldw = gffm::round_up(n > 0 ? n : 1, 32);
     // digit planes large enough for any trailing update / back substitution of
     // this problem: operands n x NB and NB x m (4 digits)
     *gl = limb::layout(std::max<int64_t>(n, 1), std::max<int64_t>(m, 1), NB, int64_t(1) << 25);
-    size_t sizes[17] = {
+    size_t sizes[16] = {
         (size_t)std::max<int64_t>(m, 1) * ldw * 4,      // W
         (size_t)2 * MAX_PANEL_CTAS * sizeof(Rec),       // rec
         (size_t)NB * NB * 4,                            // linv
         (size_t)2 * NB * 4,                             // old_row
-        (size_t)MAX_PERM_ROWS * std::max<int64_t>(n, 1) * 4,  // ptmp (row permutation scratch)
         NB * 4, NB * 4, NB * 4,                         // piv_row/val/inv
         64,                                             // result
         (size_t)std::max<int64_t>(n, 1) * 4,            // colpiv
@@ -286,7 +284,7 @@ static void layout_ws(int64_t m, int64_t n, int64_t lcols, size_t *total, size_t
         (size_t)NB * NB * 4 + (size_t)std::max<int64_t>(n, 1) * 4,  // coef, qlist
         limb::layout(NB, std::max<int64_t>(m, 1), NB, int64_t(1) << 25).a_bytes};  // dA2
     size_t o = 0;
-    for (int i = 0; i < 17; i++) {
+    for (int i = 0; i < 16; i++) {
         off[i] = o;
         o += al(sizes[i]);
     }
@@ -294,7 +292,7 @@ static void layout_ws(int64_t m, int64_t n, int64_t lcols, size_t *total, size_t
 }
 
 static void bind_ws(void *base, int64_t m, int64_t n, int64_t lcols, Work *w) {
-    size_t total, off[17];
+    size_t total, off[16];
     layout_ws(m, n, lcols, &total, off, &w->gl);
     uint8_t *b = static_cast<uint8_t *>(base);
     w->W = (int32_t *)(b + off[0]);
@@ -302,26 +300,25 @@ static void bind_ws(void *base, int64_t m, int64_t n, int64_t lcols, Work *w) {
     w->rec = (Rec *)(b + off[1]);
     w->linv = (int32_t *)(b + off[2]);
     w->old_row = (int32_t *)(b + off[3]);
-    w->ptmp = (int32_t *)(b + off[4]);
-    w->piv_row = (int32_t *)(b + off[5]);
-    w->piv_val = (int32_t *)(b + off[6]);
-    w->piv_inv = (int32_t *)(b + off[7]);
-    w->result = (int *)(b + off[8]);
-    w->colpiv = (int32_t *)(b + off[9]);
-    w->lsrc = (int32_t *)(b + off[10]);
+    w->piv_row = (int32_t *)(b + off[4]);
+    w->piv_val = (int32_t *)(b + off[5]);
+    w->piv_inv = (int32_t *)(b + off[6]);
+    w->result = (int *)(b + off[7]);
+    w->colpiv = (int32_t *)(b + off[8]);
+    w->lsrc = (int32_t *)(b + off[9]);
     w->lrow = w->lsrc + std::max<int64_t>(lcols, 1);
     w->lpv = w->lrow + std::max<int64_t>(lcols, 1);
-    w->pcol = (int32_t *)(b + off[11]);
-    w->gather = (int32_t *)(b + off[12]);
-    w->dA = (__half *)(b + off[13]);
-    w->dB = (__half *)(b + off[14]);
-    w->coef = (int32_t *)(b + off[15]);
+    w->pcol = (int32_t *)(b + off[10]);
+    w->gather = (int32_t *)(b + off[11]);
+    w->dA = (__half *)(b + off[12]);
+    w->dB = (__half *)(b + off[13]);
+    w->coef = (int32_t *)(b + off[14]);
     w->qlist = w->coef + NB * NB;
-    w->dA2 = (__half *)(b + off[16]);
+    w->dA2 = (__half *)(b + off[15]);
 }
 
 size_t workspace_bytes(int64_t m, int64_t n, int64_t lcols) {
-    size_t total, off[17];
+    size_t total, off[16];
     limb::Layout gl;
     layout_ws(m, n, lcols, &total, off, &gl);
     return total;
@@ -447,16 +444,13 @@ static int rowmajor_gemm(Work &w, int64_t N, int32_t *C, int64_t ldc, const int3
     return limb::gemm_digits(g, w.dA, w.dB, cols, rows, k, N, C, ldc, epi, 0, s);
 }
 
-// Apply a composed row permutation to columns [c_lo, c_hi) of W.
-static int permute_rows(Work &w, const PermArgs &perm, int c_lo, int c_hi, cudaStream_t s) {
-    const int ncols = c_hi - c_lo;
-    if (ncols <= 0 || perm.K == 0) return GFFM_OK;
-    const int64_t total = (int64_t)perm.K * ncols;
-    const unsigned blocks = (unsigned)((total + 255) / 256);
-    k_rows_gather<<<blocks, 256, 0, s>>>(w.W, w.ldw, c_lo, ncols, w.ptmp, perm);
-    GFFM_LAUNCH_CHECK("k_rows_gather");
-    k_rows_scatter<<<blocks, 256, 0, s>>>(w.W, w.ldw, c_lo, ncols, w.ptmp, perm);
-    GFFM_LAUNCH_CHECK("k_rows_scatter");
+// Apply a composed row permutation to columns [0, c_left) and [c_lo, c_hi) of W.
+static int permute_rows2(const Work &w, const PermArgs &perm, int c_left, int c_lo, int c_hi, cudaStream_t s) {
+    if (perm.K == 0) return GFFM_OK;
+    const int nb = (c_left + 31) / 32 + (c_hi > c_lo ? (c_hi - c_lo + 31) / 32 : 0);
+    if (nb == 0) return GFFM_OK;
+    k_rows_permute<<<nb, 256, (size_t)perm.K * 32 * 4, s>>>(w.W, w.ldw, c_left, c_lo, c_hi > c_lo ? c_hi : c_lo, perm);
+    GFFM_LAUNCH_CHECK("k_rows_permute");
     return GFFM_OK;
 }
 
@@ -641,11 +635,11 @@ static int forward(Work &w, int m, int n, int64_t N, int mode, int lcols, cudaSt
             // columns left of the panel: multipliers of earlier pivots and skipped columns
             // (W keeps every multiplier column permuted for the arithmetic; the reference's
             // narrower L swap width is restored when L is extracted)
+            // and the trailing columns: one launch
             const int left_hi = col;
-            if (left_hi > 0) {
-                st = permute_rows(w, perm, 0, left_hi, s);
-                if (st) return st;
-            }
+            const int cs = col + nbw;
+            st = permute_rows2(w, perm, left_hi, cs, n, s);
+            if (st) return st;
             if (!skipped.empty()) {
                 // skipped columns hold A values: row swaps at every width, then the
                 // pivot-row scaling (later swaps never touch a finished pivot row)
@@ -654,11 +648,8 @@ static int forward(Work &w, int m, int n, int64_t N, int mode, int lcols, cudaSt
                                                              w.piv_inv, M);
                 GFFM_LAUNCH_CHECK("k_skipped");
             }
-            // trailing columns: swaps, triangular solve, update of the rows below
-            const int cs = col + nbw;
+            // trailing columns (swapped above): triangular solve, update of the rows below
             if (cs < n) {
-                st = permute_rows(w, perm, cs, n, s);
-                if (st) return st;
                 // U12 = L11^{-1} P A12 (a single-CTA panel has written L11^{-1} already)
                 if (nbw > P1_NB || m - row > P1_MAX_ROWS) {
                     GFFM_CUDA(cudaFuncSetAttribute(k_linv, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)LINV_SMEM));
