@@ -1,4 +1,4 @@
-// elim_panel.cuh -- the elimination's panel factorization kernel and the
+// elim_panel.cuh -- the elimination's panel factorization kernels and the
 // row-permutation kernel that follows each panel.
 #pragma once
 
@@ -8,11 +8,19 @@
 namespace elim {
 
 constexpr int NB = 128;             // panel width (pivot columns per panel)
-constexpr int CPL = NB / 32;        // panel columns per lane in the elimination
 constexpr int PANEL_THREADS = 512;
 constexpr int PANEL_WARPS = PANEL_THREADS / 32;
 constexpr int MAX_PANEL_CTAS = 160;
 constexpr int MAX_PERM_ROWS = 2 * NB;
+constexpr int PANEL_MAX_R = 288;    // rows per CTA: threads 0..287 own one row each
+constexpr int PANEL_AUX0 = PANEL_MAX_R;              // threads 288..511: publication, polling
+constexpr int PANEL_NAUX = PANEL_THREADS - PANEL_AUX0;
+constexpr int LU_LD = NB + 1;
+// Dynamic shared memory of k_panel: the CTA's rows (NB columns x (R + 1) words,
+// column-major) and the Linv / pivot-row square (NB x LU_LD words).
+__host__ __device__ constexpr size_t panel_smem_bytes(int R) {
+    return ((size_t)NB * (size_t)(R + 1) + (size_t)NB * LU_LD) * 4;
+}
 
 enum PanelStatus { PS_DONE = 0, PS_ZERO_COL = 1, PS_TIMEOUT = 2, PS_BOUNDS = 3 };
 
@@ -24,13 +32,19 @@ __device__ __forceinline__ unsigned long long pkey(uint32_t v, int row) {
 __device__ __forceinline__ uint32_t pkey_val(unsigned long long k) { return (uint32_t)(k >> 38); }
 __device__ __forceinline__ int pkey_row(unsigned long long k) { return (int)(0x3FFFFFu - (uint32_t)((k >> 16) & 0x3FFFFFu)); }
 
-// One published candidate: the CTA's best row of the panel and the inverse of
-// its leading value (computed while the row is written).
+// One CTA's published candidate for a pivot step.  Every word carries the
+// step's tag (the key in its low 16 bits, the row words in their high 32 bits),
+// so a reader that sees the tag sees the value: no fence between writer and
+// reader, and each word is polled on its own.
 struct alignas(16) Rec {
-    unsigned long long key;   // written last
-    unsigned long long inv;
-    int32_t row[NB];
+    unsigned long long key;      // pkey | tag
+    unsigned long long row[NB];  // (tag << 32) | residue
 };
+// The exchange area: the displaced row's words (two parities), then the records.
+constexpr size_t OLD_ROW_WORDS = (size_t)2 * (NB + 1);
+__host__ __device__ constexpr size_t exchange_bytes(int G) {
+    return OLD_ROW_WORDS * 8 + (size_t)2 * G * sizeof(Rec);
+}
 
 struct PanelArgs {
     int32_t *W;
@@ -40,19 +54,32 @@ struct PanelArgs {
     int R;             // rows per CTA
     ModP M;
     int l_cols;        // L's padded width (PLUQ bound check), <= 0: no check
-    Mont mont;         // for the pivot inverses
-    Rec *rec;          // [2][G], keys zero at launch
-    int32_t *old_row;  // [2][NB]
+    Rec *rec;          // [2][G], zero at launch
+    unsigned long long *old_row;  // [2][NB + 1], zero at launch
     int32_t *piv_row, *piv_val, *piv_inv;  // [NB]
-    int32_t *linv;     // k_panel1: L11^{-1} of the panel's pivots, row-major, ld NB
+    int32_t *linv;     // L11^{-1} of the panel's pivots, row-major, ld NB
     int *result;       // [0] pivots, [1] status
     int *err;
 };
 
-__device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long long *p) {
+__device__ __forceinline__ void st_relaxed_u64(unsigned long long *p, unsigned long long v) {
+    asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ unsigned long long ld_relaxed_u64(const unsigned long long *p) {
     unsigned long long v;
-    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
     return v;
+}
+// The value of a row word once it carries `tag` (bounded wait; false when it gave up).
+__device__ __forceinline__ bool wait_row_word(const unsigned long long *p, uint32_t tag, uint32_t &val) {
+    unsigned long long w = ld_relaxed_u64(p);
+    if ((uint32_t)(w >> 32) != tag) {
+        const unsigned long long t0 = gffm_dev::globaltimer();
+        while ((uint32_t)((w = ld_relaxed_u64(p)) >> 32) != tag)
+            if (gffm_dev::globaltimer() - t0 > gffm_dev::kWaitLimitNs) return false;
+    }
+    val = (uint32_t)w;
+    return true;
 }
 
 __device__ __forceinline__ unsigned long long warp_max_u64(unsigned long long v) {
@@ -63,122 +90,194 @@ __device__ __forceinline__ unsigned long long warp_max_u64(unsigned long long v)
     return v;
 }
 
-// Cooperative panel factorization.  CTA b owns rows [R0 + b*R, R0 + (b+1)*R)
-// of columns [C0, C0 + nbw) in shared memory.  Per pivot step the CTAs
-// exchange one record each (their best candidate row with its inverse, tagged
-// with the step) through a parity-double-buffered global slot: polling the G
-// tags is the grid barrier, then every CTA loads the winning row.  The next
-// pivot column is eliminated first, so the next candidate's inverse (warp 0)
-// overlaps the elimination of the remaining columns (the other warps).
+__device__ __forceinline__ uint32_t p1_red(uint64_t x, const ModP &M) {
+    return (uint32_t)gffm_dev::barrett64(x, M.n, M.minv);
+}
+// sum_{s < n8} a[s * sa] * b[s * sb], n8 a multiple of 8, at most 128 products below 2^52
+__device__ __forceinline__ uint64_t p1_dot8(const uint32_t *a, int sa, const uint32_t *b, int sb, int n8) {
+    uint64_t x0 = 0, x1 = 0, x2 = 0, x3 = 0;
+    for (int q = 0; q < n8; q += 8) {
+        uint32_t va[8], vb[8];
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+            va[k] = a[(q + k) * sa];
+            vb[k] = b[(q + k) * sb];
+        }
+        x0 += (uint64_t)va[0] * vb[0] + (uint64_t)va[4] * vb[4];
+        x1 += (uint64_t)va[1] * vb[1] + (uint64_t)va[5] * vb[5];
+        x2 += (uint64_t)va[2] * vb[2] + (uint64_t)va[6] * vb[6];
+        x3 += (uint64_t)va[3] * vb[3] + (uint64_t)va[7] * vb[7];
+    }
+    return (x0 + x1) + (x2 + x3);
+}
+__device__ __forceinline__ void p1_named_sync(int id, int nthreads) {
+    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
+}
+
+// Linv[tp][s] = inv * sum_{s <= q < tp} Lneg_piv[q] Linv[q][s] for s = tid < tp, and
+// Linv[tp][tp] = inv: the new row of the inverse of the panel's lower-triangular
+// factor (pivot values on its diagonal, negated multipliers Lneg = N - l).
+__device__ __forceinline__ void linv_row(uint32_t *LU, const uint32_t *piv, int tp, uint32_t inv, int tid,
+                                         const ModP &M) {
+    if (tid < tp) {
+        uint64_t a0 = 0, a1 = 0;
+        int q = tid;
+        for (; q + 1 < tp; q += 2) {
+            a0 += (uint64_t)piv[q] * LU[q * LU_LD + tid];
+            a1 += (uint64_t)piv[q + 1] * LU[(q + 1) * LU_LD + tid];
+        }
+        if (q < tp) a0 += (uint64_t)piv[q] * LU[q * LU_LD + tid];
+        LU[tp * LU_LD + tid] = mulmod(p1_red(a0 + a1, M), inv, M);
+    } else if (tid == tp) {
+        LU[tp * LU_LD + tp] = inv;
+    }
+}
+// U[s][c] = sum_{q <= s} Linv[s][q] PR[q][c] for s = tid < np (PR: the pivot rows'
+// residues above the diagonal of LU)
+__device__ __forceinline__ void u_column(const uint32_t *LU, uint32_t *u, int np, int c, int tid, const ModP &M) {
+    if (tid < np) {
+        uint64_t a0 = 0, a1 = 0;
+        int q = 0;
+        for (; q + 1 <= tid; q += 2) {
+            a0 += (uint64_t)LU[tid * LU_LD + q] * LU[q * LU_LD + c];
+            a1 += (uint64_t)LU[tid * LU_LD + q + 1] * LU[(q + 1) * LU_LD + c];
+        }
+        if (q <= tid) a0 += (uint64_t)LU[tid * LU_LD + q] * LU[q * LU_LD + c];
+        u[tid] = p1_red(a0 + a1, M);
+    }
+}
+
+// Cooperative left-looking panel factorization.  CTA b keeps rows
+// [R0 + b*R, R0 + (b+1)*R) of columns [C0, C0 + nbw) in shared memory,
+// column-major, thread lr < R owning row lr.  Column t is brought up to date
+// only when the pivot search reaches it:
+//   U[0:t][t] = Linv W_piv[0:t][t],   v[r] = W[r][t] + sum_{s<t} Lneg[r][s] U[s][t],
+// Linv the inverse of the panel's lower-triangular factor, W_piv the pivot rows'
+// residues, Lneg = N - l the negated multipliers -- one exact 64-bit dot product
+// per row, reduced once.  Every CTA keeps the same Linv and pivot rows (LU).
+// Per pivot step t:
+//   A. each CTA publishes its candidate (largest residue of column t in its rows,
+//      lowest row on ties): the key and the row, tagged words; the owner of row
+//      r = R0 + t publishes that row too,
+//   B. while the auxiliary threads poll the G keys (bounded waits), the row
+//      threads form Linv's row t-1, U[0:t][t+1] and the partial values
+//      y[r] = W[r][t+1] + sum_{s<t} Lneg[r][s] U[s][t+1]; the owner of row r
+//      publishes y[r],
+//   C. every CTA picks the same winner, fetches its row (and, where the winner
+//      lands, the displaced row r with y[r]) while one warp computes the pivot's
+//      inverse by the reference's Euclid,
+//   D. the two rows move, U[t][t+1] = inv (W_piv[t][t+1] + sum_{s<t} Lneg_piv[s]
+//      U[s][t+1]) completes column t+1: v[r] = y[r] + Lneg[r][t] U[t][t+1], and
+//      the CTA's next candidate is its largest v.
+// The panel is written back with the pivot rows scaled (U), the multipliers
+// unscaled below the pivots and the columns after a stop brought up to date;
+// CTA 0 writes L11^{-1} for the product U12 = L11^{-1} P A12.
 __global__ void __launch_bounds__(PANEL_THREADS, 1) k_panel(PanelArgs a) {
-    extern __shared__ int32_t smem_dyn[];
-    int32_t *P = smem_dyn;  // R x NB
+    extern __shared__ __align__(16) uint32_t psm[];
+    const int R = a.R, rs = R + 1;
+    uint32_t *P = psm;                      // P[j * rs + lr]
+    uint32_t *LU = psm + (size_t)NB * rs;   // LU[s * LU_LD + c]: Linv (c <= s), pivot row s (c > s)
     __shared__ unsigned long long keys[MAX_PANEL_CTAS];
-    __shared__ uint32_t invs[MAX_PANEL_CTAS];
-    __shared__ __align__(16) int32_t piv[NB];
-    __shared__ __align__(16) int32_t oldr[NB];
-    __shared__ int32_t u[NB];
+    __shared__ uint32_t s_piv[NB];          // the pivot row: Lneg (c < t), residues (c > t)
+    __shared__ uint32_t s_old[NB + 1];      // the displaced row, and its partial value of column t+1
+    __shared__ __align__(16) uint32_t s_u[NB + 8];   // U[s][t+1] for s < t, zero from t on
     __shared__ unsigned long long red[PANEL_WARPS];
-    __shared__ unsigned long long s_best;
-    __shared__ int s_stop, s_status, s_prow, s_bw;
-    __shared__ uint32_t s_inv, s_cinv;
+    __shared__ int s_stop, s_status, s_prow;
+    __shared__ uint32_t s_pv, s_inv, s_g;
     const int b = blockIdx.x, G = gridDim.x, tid = threadIdx.x;
-    const int lane = tid & 31, wid = tid >> 5;
-    const int rbeg = a.R0 + b * a.R;
-    const int rend = min(rbeg + a.R, a.m);
+    const int lane = tid & 31, warp = tid >> 5;
+    const int rbeg = a.R0 + b * R;
+    const int rend = min(rbeg + R, a.m);
     const int nr = max(rend - rbeg, 0);
     const int nbw = a.nbw;
-    const uint32_t n = a.M.n;
+    const ModP M = a.M;
+    const uint32_t N = M.n;
+    const int lr = tid, grow = rbeg + tid;
+    const bool own = tid < nr;
 
-    for (int e = tid; e < nr * NB; e += blockDim.x) {
-        const int i = e / NB, j = e - (e / NB) * NB;
-        P[e] = (j < nbw) ? a.W[(int64_t)(rbeg + i) * a.ldw + a.C0 + j] : 0;
+    for (int e = tid; e < nr * nbw; e += PANEL_THREADS) {
+        const int i = e / nbw, j = e - i * nbw;
+        P[j * rs + i] = (uint32_t)a.W[(int64_t)(rbeg + i) * a.ldw + a.C0 + j];
     }
+    for (int i = tid; i < NB + 8; i += PANEL_THREADS) s_u[i] = 0;
     if (tid == 0) {
         s_stop = 0;
         s_status = PS_DONE;
     }
     __syncthreads();
-    // candidate for step 0: column 0 over all own rows, and its inverse
-    {
-        unsigned long long best = 0;
-        for (int i = tid; i < nr; i += blockDim.x) {
-            const unsigned long long k = pkey((uint32_t)P[i * NB], rbeg + i);
-            best = k > best ? k : best;
-        }
-        best = warp_max_u64(best);
-        if (lane == 0) red[wid] = best;
-        __syncthreads();
-        if (wid == 0) {
-            best = lane < PANEL_WARPS ? red[lane] : 0ull;
-            best = warp_max_u64(best);
-            if (lane == 0) {
-                s_best = best;
-                s_cinv = pkey_val(best) ? mod_inverse(pkey_val(best), a.mont) : 0u;
-            }
-        }
-        __syncthreads();
+    // column 0: negated multipliers and the first candidate
+    unsigned long long best = 0;
+    if (own) {
+        const uint32_t v = P[lr];
+        P[lr] = v ? N - v : 0u;
+        best = pkey(v, grow);
     }
+    best = warp_max_u64(best);
+    if (lane == 0) red[warp] = best;
+    __syncthreads();
+    best = warp_max_u64(lane < PANEL_WARPS ? red[lane] : 0ull);
 
     const int tmax = min(nbw, a.m - a.R0);
+    uint64_t y = 0;   // this row's partial value of column t+1
     int t = 0;
     for (; t < tmax; t++) {
         const int r = a.R0 + t;
         const int par = t & 1;
-        const unsigned long long tag = (unsigned long long)(t + 1);
-        Rec *mine = a.rec + par * G + b;
-        // 1. publish the candidate row (and the current row r from its owner), then
-        //    the inverse and the tagged key with release semantics
-        const unsigned long long best0 = s_best;
-        if (best0) {
-            const int li = pkey_row(best0) - rbeg;
-            for (int j = tid; j < NB; j += blockDim.x) mine->row[j] = P[li * NB + j];
-        }
-        if (r >= rbeg && r < rend)
-            for (int j = tid; j < NB; j += blockDim.x) a.old_row[par * NB + j] = P[(r - rbeg) * NB + j];
-        __syncthreads();
-        if (tid == 0) {
-            mine->inv = s_cinv;
-            asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(&mine->key), "l"(best0 | tag) : "memory");
-        }
-        // 2. poll the G tagged keys (the grid barrier)
-        for (int g = tid; g < G; g += blockDim.x) {
-            const unsigned long long *kp = &a.rec[par * G + g].key;
-            unsigned long long k = ld_acquire_u64(kp);
-            if ((k & 0xFFFFull) != tag) {
-                const unsigned long long t0 = gffm_dev::globaltimer();
-                while (((k = ld_acquire_u64(kp)) & 0xFFFFull) != tag) {
-                    if (gffm_dev::globaltimer() - t0 > gffm_dev::kWaitLimitNs) {
-                        atomicOr(a.err, 16);
-                        s_stop = 1;
-                        s_status = PS_TIMEOUT;
-                        k = 0;
-                        break;
+        const uint32_t tag = (uint32_t)(t + 1);
+        const bool owner_r = r >= rbeg && r < rend;
+        const bool next = t + 1 < nbw;
+        unsigned long long *oldw = a.old_row + par * (NB + 1);
+        // A. publication
+        if (tid >= PANEL_AUX0) {
+            const int x = tid - PANEL_AUX0;
+            if (x < NB) {
+                Rec *mine = a.rec + par * G + b;
+                if (best != 0 && x < nbw)
+                    st_relaxed_u64(&mine->row[x],
+                                   ((unsigned long long)tag << 32) | P[x * rs + (pkey_row(best) - rbeg)]);
+                if (x == 0) st_relaxed_u64(&mine->key, best | tag);
+            } else if (owner_r) {
+                for (int j = x - NB; j < nbw; j += PANEL_NAUX - NB)
+                    st_relaxed_u64(&oldw[j], ((unsigned long long)tag << 32) | P[j * rs + (r - rbeg)]);
+            }
+            // B (auxiliary threads): the G keys
+            for (int g = x; g < G; g += PANEL_NAUX) {
+                const unsigned long long *kp = &a.rec[par * G + g].key;
+                unsigned long long k = ld_relaxed_u64(kp);
+                if ((k & 0xFFFFull) != tag) {
+                    const unsigned long long t0 = gffm_dev::globaltimer();
+                    while (((k = ld_relaxed_u64(kp)) & 0xFFFFull) != tag) {
+                        if (gffm_dev::globaltimer() - t0 > gffm_dev::kWaitLimitNs) {
+                            atomicOr(a.err, 16);
+                            s_stop = 1;
+                            s_status = PS_TIMEOUT;
+                            k = 0;
+                            break;
+                        }
                     }
                 }
+                keys[g] = k & ~0xFFFFull;
             }
-            keys[g] = k & ~0xFFFFull;
-            invs[g] = (uint32_t)__ldcg(&a.rec[par * G + g].inv);
+        } else {
+            // B (row threads): Linv's row t-1, U[0:t][t+1], partial values of column t+1
+            if (t > 0) linv_row(LU, s_piv, t - 1, s_inv, tid, M);
+            p1_named_sync(1, PANEL_AUX0);
+            if (next) {
+                u_column(LU, s_u, t, t + 1, tid, M);
+                p1_named_sync(1, PANEL_AUX0);
+                if (own && grow >= r) {
+                    y = (uint64_t)P[(t + 1) * rs + lr] + p1_dot8(P + lr, rs, s_u, 1, (t + 7) & ~7);
+                    if (grow == r) st_relaxed_u64(&oldw[NB], ((unsigned long long)tag << 32) | p1_red(y, M));
+                }
+            }
         }
         __syncthreads();
         if (s_stop) break;
-        // 3. the global pivot (every CTA decides the same)
-        if (wid == 0) {
+        // C. the global pivot (every CTA decides the same)
+        if (warp == PANEL_WARPS - 1) {
             unsigned long long wk = 0;
-            int wg = 0;
-            for (int g = lane; g < G; g += 32)
-                if (keys[g] > wk) {
-                    wk = keys[g];
-                    wg = g;
-                }
-            for (int o = 16; o; o >>= 1) {
-                const unsigned long long x = __shfl_xor_sync(0xffffffffu, wk, o);
-                const int xg = __shfl_xor_sync(0xffffffffu, wg, o);
-                if (x > wk) {
-                    wk = x;
-                    wg = xg;
-                }
-            }
+            for (int g = lane; g < G; g += 32) wk = keys[g] > wk ? keys[g] : wk;
+            wk = warp_max_u64(wk);
             if (lane == 0) {
                 const uint32_t pv = pkey_val(wk);
                 if (pv == 0) {
@@ -189,117 +288,112 @@ __global__ void __launch_bounds__(PANEL_THREADS, 1) k_panel(PanelArgs a) {
                     s_status = PS_BOUNDS;
                 } else {
                     s_prow = pkey_row(wk);
-                    s_bw = wg;
-                    s_inv = invs[wg];
-                    if (b == 0) {
-                        a.piv_row[t] = s_prow;
-                        a.piv_val[t] = (int32_t)pv;
-                        a.piv_inv[t] = (int32_t)s_inv;
-                    }
+                    s_pv = pv;
                 }
             }
         }
         __syncthreads();
         if (s_stop) break;
-        // 4. the winning row and the current row r
-        {
-            const int owner = (r - a.R0) / a.R;
-            if (tid < NB / 4)
-                reinterpret_cast<int4 *>(piv)[tid] =
-                    __ldcg(reinterpret_cast<const int4 *>(a.rec[par * G + s_bw].row) + tid);
-            else if (tid < NB / 2 && owner != b)
-                reinterpret_cast<int4 *>(oldr)[tid - NB / 4] =
-                    __ldcg(reinterpret_cast<const int4 *>(a.old_row + par * NB) + (tid - NB / 4));
-            else if (tid < NB / 2)
-                for (int q = 0; q < 4; q++) oldr[(tid - NB / 4) * 4 + q] = P[(r - rbeg) * NB + (tid - NB / 4) * 4 + q];
-        }
-        __syncthreads();
         const int prow = s_prow;
-        const uint32_t inv = s_inv;
-        for (int j = tid; j < NB; j += blockDim.x) u[j] = (int32_t)mulmod((uint32_t)piv[j], inv, a.M);
-        __syncthreads();
-        // 5. swap_rows_and_mod restricted to the panel: row r <- pivot row (scaled from
-        //    column t on), row prow <- old row r; the multiplier columns swap unscaled
-        if (r >= rbeg && r < rend) {
-            int32_t *pr = P + (r - rbeg) * NB;
-            for (int j = tid; j < nbw; j += blockDim.x) pr[j] = j >= t ? u[j] : piv[j];
-        }
-        if (prow != r && prow >= rbeg && prow < rend) {
-            int32_t *pp = P + (prow - rbeg) * NB;
-            for (int j = tid; j < nbw; j += blockDim.x) pp[j] = oldr[j];
-        }
-        __syncthreads();
-        // 6. eliminate the rows below the pivot (the multiplier stays in column t).
-        //    a) the next pivot column, one thread per row, and the next candidate
-        const int i0 = max(r + 1 - rbeg, 0);
-        const int jb = t + 1;
-        {
-            unsigned long long best = 0;
-            if (jb < nbw) {
-                const uint32_t ub = (uint32_t)u[jb], sb = shoup_pre(ub, a.M);
-                for (int i = i0 + tid; i < nr; i += blockDim.x) {
-                    const uint32_t l = (uint32_t)P[i * NB + t];
-                    uint32_t x = (uint32_t)P[i * NB + jb];
-                    const uint32_t d = shoup_mul(l, ub, sb, n);
-                    x = x >= d ? x - d : x + n - d;
-                    P[i * NB + jb] = (int32_t)x;
-                    const unsigned long long k = pkey(x, rbeg + i);
-                    best = k > best ? k : best;
+        const int bw = (prow - a.R0) / R;
+        const bool lands = bw == b && prow != r;   // the displaced row r moves into this CTA
+        if (tid < nbw) {
+            uint32_t v = 0;
+            if (!wait_row_word(&a.rec[par * G + bw].row[tid], tag, v)) {
+                atomicOr(a.err, 16);
+                s_stop = 1;
+                s_status = PS_TIMEOUT;
+            }
+            s_piv[tid] = v;
+        } else if (tid >= NB && tid <= 2 * NB && lands) {
+            const int j = tid - NB;
+            if (j < nbw || (j == NB && next)) {
+                uint32_t v = 0;
+                if (!wait_row_word(&oldw[j], tag, v)) {
+                    atomicOr(a.err, 16);
+                    s_stop = 1;
+                    s_status = PS_TIMEOUT;
                 }
+                s_old[j] = v;
             }
-            best = warp_max_u64(best);
-            if (lane == 0) red[wid] = best;
-            __syncthreads();
-            if (wid == 0) {
-                best = lane < PANEL_WARPS ? red[lane] : 0ull;
-                best = warp_max_u64(best);
-                if (lane == 0) s_best = best;
-            }
-            __syncthreads();
-        }
-        //    b) warp 0: the inverse of the next candidate; warps 1..: columns jb+1..
-        if (wid == 0) {
-            if (lane == 0) {
-                const uint32_t v = pkey_val(s_best);
-                s_cinv = (jb < nbw && v) ? mod_inverse(v, a.mont) : 0u;
-            }
-        } else if (jb + 1 < nbw) {
-            uint32_t uc[CPL], us[CPL];
-#pragma unroll
-            for (int c = 0; c < CPL; c++) {
-                const int j = jb + 1 + lane + 32 * c;
-                uc[c] = j < nbw ? (uint32_t)u[j] : 0u;
-                us[c] = shoup_pre(uc[c], a.M);
-            }
-            for (int i = i0 + wid - 1; i < nr; i += PANEL_WARPS - 1) {
-                int32_t *pi = P + i * NB;
-                const uint32_t l = (uint32_t)pi[t];
-                uint32_t x[CPL];
-#pragma unroll
-                for (int c = 0; c < CPL; c++) {
-                    const int j = jb + 1 + lane + 32 * c;
-                    x[c] = j < nbw ? (uint32_t)pi[j] : 0u;
-                }
-#pragma unroll
-                for (int c = 0; c < CPL; c++) {
-                    const int j = jb + 1 + lane + 32 * c;
-                    if (j < nbw) {
-                        const uint32_t d = shoup_mul(l, uc[c], us[c], n);
-                        pi[j] = (int32_t)(x[c] >= d ? x[c] - d : x[c] + n - d);
-                    }
-                }
-            }
+        } else if (tid == PANEL_THREADS - 32) {
+            s_inv = mod_inv_euclid_alu(s_pv, N);
         }
         __syncthreads();
+        if (s_stop) break;
+        // D. row moves, the pivot row's residues, U[t][t+1]
+        const uint32_t inv = s_inv, pv = s_pv;
+        if (owner_r && tid <= t) P[tid * rs + (r - rbeg)] = tid < t ? s_piv[tid] : mulmod(pv, inv, M);
+        if (lands && tid < nbw) P[tid * rs + (prow - rbeg)] = s_old[tid];
+        if (lands && tid == prow - rbeg) y = s_old[NB];
+        if (tid > t && tid < nbw) LU[t * LU_LD + tid] = s_piv[tid];
+        if (warp == PANEL_WARPS - 2 && next) {
+            uint64_t acc = 0;
+            for (int s = lane; s < t; s += 32) acc += (uint64_t)s_piv[s] * s_u[s];
+            uint32_t p = p1_red(acc, M);   // 32 residues sum below 2^31
+            for (int o = 16; o; o >>= 1) p += __shfl_xor_sync(0xffffffffu, p, o);
+            if (lane == 0) s_g = mulmod(p1_red((uint64_t)p + s_piv[t + 1], M), inv, M);
+        }
+        if (b == 0 && tid == 0) {
+            a.piv_row[t] = prow;
+            a.piv_val[t] = (int32_t)pv;
+            a.piv_inv[t] = (int32_t)inv;
+        }
+        __syncthreads();
+        // column t+1: the rows below the pivot and the pivot rows' U values; next candidate
+        best = 0;
+        if (next && own) {
+            const uint32_t g = s_g;
+            if (grow > r) {
+                const uint32_t v = p1_red(y + (uint64_t)P[t * rs + lr] * g, M);
+                P[(t + 1) * rs + lr] = v ? N - v : 0u;
+                best = pkey(v, grow);
+            } else {
+                const int s = grow - a.R0;
+                P[(t + 1) * rs + lr] = s < t ? s_u[s] : g;
+            }
+        }
+        best = warp_max_u64(best);
+        if (lane == 0) red[warp] = best;
+        __syncthreads();
+        best = warp_max_u64(lane < PANEL_WARPS ? red[lane] : 0ull);
     }
     __syncthreads();
-    for (int e = tid; e < nr * NB; e += blockDim.x) {
-        const int i = e / NB, j = e - (e / NB) * NB;
-        if (j < nbw) a.W[(int64_t)(rbeg + i) * a.ldw + a.C0 + j] = P[e];
+    const int npiv = t, status = s_status;
+    if (status == PS_DONE || status == PS_ZERO_COL) {
+        // Linv's last row, then the columns after a stop (the column at a zero stop is
+        // final already): U by Linv, the rows below by the multipliers
+        if (npiv > 0) linv_row(LU, s_piv, npiv - 1, s_inv, tid, M);
+        __syncthreads();
+        for (int j = npiv + 1; npiv > 0 && j < nbw; j++) {
+            u_column(LU, s_u, npiv, j, tid, M);
+            __syncthreads();
+            if (own) {
+                if (grow >= a.R0 + npiv)
+                    P[j * rs + lr] = p1_red((uint64_t)P[j * rs + lr] + p1_dot8(P + lr, rs, s_u, 1, (npiv + 7) & ~7), M);
+                else
+                    P[j * rs + lr] = s_u[grow - a.R0];
+            }
+            __syncthreads();
+        }
     }
-    if (b == 0 && tid == 0) {
-        a.result[0] = t;
-        a.result[1] = s_status;
+    // back to W: pivot columns hold U on and above the diagonal and the unscaled
+    // multipliers below it; the other columns their current residues
+    for (int e = tid; e < nr * nbw; e += PANEL_THREADS) {
+        const int i = e / nbw, j = e - i * nbw;
+        uint32_t x = P[j * rs + i];
+        if (j < npiv && rbeg + i > a.R0 + j) x = x ? N - x : 0u;
+        a.W[(int64_t)(rbeg + i) * a.ldw + a.C0 + j] = (int32_t)x;
+    }
+    if (b == 0) {
+        for (int e = tid; e < npiv * npiv; e += PANEL_THREADS) {
+            const int i = e / npiv, j = e - i * npiv;
+            a.linv[i * NB + j] = j <= i ? (int32_t)LU[i * LU_LD + j] : 0;
+        }
+        if (tid == 0) {
+            a.result[0] = npiv;
+            a.result[1] = status;
+        }
     }
 }
 
@@ -321,30 +415,6 @@ constexpr int P1_THREADS = 256;
 constexpr int P1_INV_WARP = 7;
 constexpr int P1_MAX_ROWS = 1536;
 __host__ __device__ constexpr size_t p1_smem_bytes(int rows) { return (size_t)P1_NB * (size_t)(rows + 4) * 4; }
-
-__device__ __forceinline__ uint32_t p1_red(uint64_t x, const ModP &M) {
-    return (uint32_t)gffm_dev::barrett64(x, M.n, M.minv);
-}
-// sum_{s < n8} a[s * sa] * b[s * sb], n8 a multiple of 8, at most 32 products below 2^52
-__device__ __forceinline__ uint64_t p1_dot8(const uint32_t *a, int sa, const uint32_t *b, int sb, int n8) {
-    uint64_t x0 = 0, x1 = 0, x2 = 0, x3 = 0;
-    for (int q = 0; q < n8; q += 8) {
-        uint32_t va[8], vb[8];
-#pragma unroll
-        for (int k = 0; k < 8; k++) {
-            va[k] = a[(q + k) * sa];
-            vb[k] = b[(q + k) * sb];
-        }
-        x0 += (uint64_t)va[0] * vb[0] + (uint64_t)va[4] * vb[4];
-        x1 += (uint64_t)va[1] * vb[1] + (uint64_t)va[5] * vb[5];
-        x2 += (uint64_t)va[2] * vb[2] + (uint64_t)va[6] * vb[6];
-        x3 += (uint64_t)va[3] * vb[3] + (uint64_t)va[7] * vb[7];
-    }
-    return (x0 + x1) + (x2 + x3);
-}
-__device__ __forceinline__ void p1_named_sync(int id, int nthreads) {
-    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
-}
 
 __global__ void __launch_bounds__(P1_THREADS, 1) k_panel1(PanelArgs a) {
     extern __shared__ __align__(16) int32_t p1s[];
@@ -484,7 +554,7 @@ __global__ void __launch_bounds__(P1_THREADS, 1) k_panel1(PanelArgs a) {
         if (j < npiv && lr > j) x = x ? N - x : 0u;
         a.W[(int64_t)(r0 + lr) * a.ldw + c0 + j] = (int32_t)x;
     }
-    // L11^{-1} for the U12 product (what k_linv computes for the cooperative panel)
+    // L11^{-1} for the U12 product
     for (int idx = tid; idx < npiv * npiv; idx += blockDim.x) {
         const int i = idx / npiv, j = idx - i * npiv;
         a.linv[i * NB + j] = (int32_t)Lv[i * 33 + j];
@@ -492,55 +562,6 @@ __global__ void __launch_bounds__(P1_THREADS, 1) k_panel1(PanelArgs a) {
     if (tid == 0) {
         a.result[0] = npiv;
         a.result[1] = status;
-    }
-}
-
-// L11^{-1} of a panel with t pivots (rows R0.., pivot columns C0..; L11 has the
-// pivot values on the diagonal and the multipliers W[R0+i][C0+s] below), one
-// warp per column j by forward substitution:
-//   X[i][j] = inv_i * (delta_ij - sum_{j<=s<i} L11[i][s] X[s][j]).
-// Lanes hold X[s][j] for s = lane + 32c; each dot product is a warp sum.
-// Output row-major, ld NB, zero above the diagonal.  Dynamic shared memory:
-// NB x (NB + 1) words for L11.
-constexpr size_t LINV_SMEM = (size_t)NB * (NB + 1) * 4;
-__global__ void __launch_bounds__(1024) k_linv(const int32_t *W, int64_t ldw, int R0, int C0, int t,
-                                               const int32_t *inv, int32_t *linv, ModP M) {
-    extern __shared__ uint32_t L11s[];
-    auto L11 = [&](int i, int s) -> uint32_t & { return L11s[i * (NB + 1) + s]; };
-    for (int e = threadIdx.x; e < NB * NB; e += blockDim.x) {
-        const int i = e / NB, s = e % NB;
-        L11(i, s) = (s < i && i < t) ? (uint32_t)W[(int64_t)(R0 + i) * ldw + C0 + s] : 0;
-    }
-    __syncthreads();
-    const int lane = threadIdx.x & 31;
-    const int j = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-    if (j >= NB) return;
-    uint32_t x[CPL];  // X[lane + 32c][j]
-#pragma unroll
-    for (int c = 0; c < CPL; c++) x[c] = 0;
-    for (int i = 0; i < NB; i++) {
-        uint32_t xi = 0;
-        if (i < t && i >= j) {
-            if (i == j) {
-                xi = (uint32_t)inv[i];
-            } else {
-                uint64_t part = 0;
-#pragma unroll
-                for (int c = 0; c < CPL; c++) {
-                    const int s = lane + 32 * c;
-                    if (s >= j && s < i) part += (uint64_t)L11(i, s) * x[c];
-                }
-                // reduce each lane's part first: the warp sum of 32 residues fits 32 bits
-                uint32_t p32 = (uint32_t)gffm_dev::barrett64(part, M.n, M.minv);
-                for (int o = 16; o; o >>= 1) p32 += __shfl_xor_sync(0xffffffffu, p32, o);
-                const uint32_t a = (uint32_t)gffm_dev::barrett64(p32, M.n, M.minv);
-                xi = mulmod(a ? M.n - a : 0, (uint32_t)inv[i], M);
-            }
-        }
-#pragma unroll
-        for (int c = 0; c < CPL; c++)
-            if (lane + 32 * c == i) x[c] = xi;
-        if (lane == 0 && i < t) linv[i * NB + j] = (int32_t)xi;
     }
 }
 

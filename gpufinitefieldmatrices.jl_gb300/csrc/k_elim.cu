@@ -8,23 +8,28 @@
 //
 // One panel = up to NB consecutive pivot columns starting at (R0, C0).  The
 // panel kernel (elim_panel.cuh) is a cooperative grid: CTA b keeps rows
-// [R0 + b*R, R0 + (b+1)*R) of the panel in shared memory.  Per pivot step it
+// [R0 + b*R, R0 + (b+1)*R) of the panel in shared memory and factors
+// left-looking (column t is formed only when the pivot search reaches it, by
+// one exact dot product per row against U[0:t][t] = L11^{-1} W_piv[0:t][t]).
+// Per pivot step it
 //   1. publishes its candidate -- the largest residue of the pivot column in
-//      its rows (lowest row on ties), that row, and the value's inverse by the
-//      reference's extended Euclid -- in a parity-double-buffered global slot
-//      tagged with the step; its owner also publishes the current row r,
-//   2. polls the G tagged slots (the grid barrier, bounded wait) and loads
-//      every candidate row,
-//   3. picks the global winner, swaps / scales the two rows it owns, and
-//      eliminates its rows below the pivot: W[i][j] = (W[i][j] + (N - l_i) * u_j)
-//      mod N, finding its next candidate on the way.
+//      its rows (lowest row on ties) and that row -- as words tagged with the
+//      step in a parity-double-buffered global slot; the owner of the current
+//      row r publishes that row,
+//   2. polls the G keys (the grid barrier, bounded waits) while its row
+//      threads form the next column's partial sums,
+//   3. picks the global winner, fetches its row (and the displaced row r where
+//      that lands) while one warp inverts the pivot by the reference's extended
+//      Euclid, moves the two rows and completes the next column.
+// A single CTA factors 32-column panels once the rows fit it (k_panel1).
+// Both panels write L11^{-1} of their pivots.
 // Everything the reference does to columns outside the panel is deferred and
 // applied after the panel in the same order-independent form:
 //   - columns left of the panel: the panel's row swaps (earlier multipliers and
 //     skipped columns), then the pivot-row scaling of the skipped columns,
 //   - trailing columns: the row swaps, the triangular solve for the panel rows
 //     U12 = L11^{-1} P A12 (x_t = inv_t * (a_t - sum_{s<t} L[r_t, c_s] x_s):
-//     the reference's scaling and updates in closed form; k_linv builds
+//     the reference's scaling and updates in closed form, with the panel's
 //     L11^{-1}) and the update of the rows below, A22 -= L21 * U12 mod N, both
 //     on the limb tensor-core GEMM.
 // W keeps every multiplier column permuted for this arithmetic; the
@@ -247,7 +252,7 @@ struct Work {
     int32_t *W;
     int64_t ldw;
     Rec *rec;
-    int32_t *old_row;
+    unsigned long long *old_row;                 // the panel's displaced-row words (exchange area)
     int32_t *piv_row, *piv_val, *piv_inv;
     int *result;
     int32_t *colpiv, *lsrc, *lrow, *lpv, *pcol;  // [n], [lcols] x3, [min(m,n)]
@@ -264,16 +269,15 @@ struct Work {
 
 static size_t al(size_t x) { return (x + 255) & ~size_t(255); }
 
-static void layout_ws(int64_t m, int64_t n, int64_t lcols, size_t *total, size_t off[16], limb::Layout *gl) {
+static void layout_ws(int64_t m, int64_t n, int64_t lcols, size_t *total, size_t off[15], limb::Layout *gl) {
     const int64_t ldw = gffm::round_up(n > 0 ? n : 1, 32);
     // digit planes large enough for any trailing update / back substitution of
     // this problem: operands n x NB and NB x m (4 digits)
     *gl = limb::layout(std::max<int64_t>(n, 1), std::max<int64_t>(m, 1), NB, int64_t(1) << 25);
-    size_t sizes[16] = {
+    size_t sizes[15] = {
         (size_t)std::max<int64_t>(m, 1) * ldw * 4,      // W
-        (size_t)2 * MAX_PANEL_CTAS * sizeof(Rec),       // rec
+        exchange_bytes(MAX_PANEL_CTAS),                 // old_row words + rec
         (size_t)NB * NB * 4,                            // linv
-        (size_t)2 * NB * 4,                             // old_row
         NB * 4, NB * 4, NB * 4,                         // piv_row/val/inv
         64,                                             // result
         (size_t)std::max<int64_t>(n, 1) * 4,            // colpiv
@@ -284,7 +288,7 @@ static void layout_ws(int64_t m, int64_t n, int64_t lcols, size_t *total, size_t
         (size_t)NB * NB * 4 + (size_t)std::max<int64_t>(n, 1) * 4,  // coef, qlist
         limb::layout(NB, std::max<int64_t>(m, 1), NB, int64_t(1) << 25).a_bytes};  // dA2
     size_t o = 0;
-    for (int i = 0; i < 16; i++) {
+    for (int i = 0; i < 15; i++) {
         off[i] = o;
         o += al(sizes[i]);
     }
@@ -292,33 +296,33 @@ static void layout_ws(int64_t m, int64_t n, int64_t lcols, size_t *total, size_t
 }
 
 static void bind_ws(void *base, int64_t m, int64_t n, int64_t lcols, Work *w) {
-    size_t total, off[16];
+    size_t total, off[15];
     layout_ws(m, n, lcols, &total, off, &w->gl);
     uint8_t *b = static_cast<uint8_t *>(base);
     w->W = (int32_t *)(b + off[0]);
     w->ldw = gffm::round_up(n > 0 ? n : 1, 32);
-    w->rec = (Rec *)(b + off[1]);
+    w->old_row = (unsigned long long *)(b + off[1]);
+    w->rec = (Rec *)(b + off[1] + OLD_ROW_WORDS * 8);
     w->linv = (int32_t *)(b + off[2]);
-    w->old_row = (int32_t *)(b + off[3]);
-    w->piv_row = (int32_t *)(b + off[4]);
-    w->piv_val = (int32_t *)(b + off[5]);
-    w->piv_inv = (int32_t *)(b + off[6]);
-    w->result = (int *)(b + off[7]);
-    w->colpiv = (int32_t *)(b + off[8]);
-    w->lsrc = (int32_t *)(b + off[9]);
+    w->piv_row = (int32_t *)(b + off[3]);
+    w->piv_val = (int32_t *)(b + off[4]);
+    w->piv_inv = (int32_t *)(b + off[5]);
+    w->result = (int *)(b + off[6]);
+    w->colpiv = (int32_t *)(b + off[7]);
+    w->lsrc = (int32_t *)(b + off[8]);
     w->lrow = w->lsrc + std::max<int64_t>(lcols, 1);
     w->lpv = w->lrow + std::max<int64_t>(lcols, 1);
-    w->pcol = (int32_t *)(b + off[10]);
-    w->gather = (int32_t *)(b + off[11]);
-    w->dA = (__half *)(b + off[12]);
-    w->dB = (__half *)(b + off[13]);
-    w->coef = (int32_t *)(b + off[14]);
+    w->pcol = (int32_t *)(b + off[9]);
+    w->gather = (int32_t *)(b + off[10]);
+    w->dA = (__half *)(b + off[11]);
+    w->dB = (__half *)(b + off[12]);
+    w->coef = (int32_t *)(b + off[13]);
     w->qlist = w->coef + NB * NB;
-    w->dA2 = (__half *)(b + off[15]);
+    w->dA2 = (__half *)(b + off[14]);
 }
 
 size_t workspace_bytes(int64_t m, int64_t n, int64_t lcols) {
-    size_t total, off[16];
+    size_t total, off[15];
     limb::Layout gl;
     layout_ws(m, n, lcols, &total, off, &gl);
     return total;
@@ -460,22 +464,21 @@ static int run_panel(Work &w, int m, int n, int R0, int C0, int nbw, const ModP 
     using namespace gffm;
     const int rows = m - R0;
     const int sms = sm_count();
-    // rows per CTA: at least 64, and at most 128 CTAs while the rows fit (the per-step
-    // exchange moves G candidate rows into every CTA); at most max_g CTAs when the
-    // panel shares the GPU with a trailing update
+    // rows per CTA: at least 64, and at most 128 CTAs while the rows fit; at most
+    // max_g CTAs when the panel shares the GPU with a trailing update
     int R = 64;
     if (max_g > 0) {
-        while ((rows + R - 1) / R > max_g) R += 32;
+        while ((rows + R - 1) / R > max_g && R < PANEL_MAX_R) R += 32;
     } else {
-        while ((rows + R - 1) / R > std::min(sms, 128) && R < 640) R += 32;
-        while ((rows + R - 1) / R > std::min(sms, MAX_PANEL_CTAS)) R += 32;
+        while ((rows + R - 1) / R > std::min(sms, 128) && R < PANEL_MAX_R) R += 32;
     }
     const int G = std::max(1, (rows + R - 1) / R);
     const bool one = rows <= P1_MAX_ROWS && nbw <= P1_NB;   // the whole panel in one CTA
-    const size_t smem = one ? p1_smem_bytes(rows) : (size_t)R * NB * 4;
-    if (smem > 200 * 1024)
-        return set_error(GFFM_ERR_UNSUPPORTED, "elimination panel: %d rows exceed the panel kernel's capacity", rows);
-    if (!one) GFFM_CUDA(cudaMemsetAsync(w.rec, 0, (size_t)2 * G * sizeof(Rec), s));
+    if (!one && G > std::min(sms, MAX_PANEL_CTAS))
+        return set_error(GFFM_ERR_UNSUPPORTED, "elimination panel: %d rows exceed the panel kernel's capacity (%d)",
+                         rows, std::min(sms, MAX_PANEL_CTAS) * PANEL_MAX_R);
+    const size_t smem = one ? p1_smem_bytes(rows) : panel_smem_bytes(R);
+    if (!one) GFFM_CUDA(cudaMemsetAsync(w.old_row, 0, exchange_bytes(G), s));
     PanelArgs a;
     a.W = w.W;
     a.ldw = w.ldw;
@@ -487,7 +490,6 @@ static int run_panel(Work &w, int m, int n, int R0, int C0, int nbw, const ModP 
     a.R = R;
     a.M = M;
     a.l_cols = lcols_check;
-    a.mont = make_mont(M.n);
     a.rec = w.rec;
     a.old_row = w.old_row;
     a.piv_row = w.piv_row;
@@ -518,7 +520,7 @@ static int run_panel(Work &w, int m, int n, int R0, int C0, int nbw, const ModP 
 // columns past it runs beside it on the other SMs (a second stream).  The next
 // panel's own columns are updated first, on the whole GPU.
 static int look_ctas(int rows) {
-    const int gmin = (rows + 383) / 384;   // the panel keeps at most 384 rows per CTA
+    const int gmin = (rows + PANEL_MAX_R - 1) / PANEL_MAX_R;   // the panel's rows per CTA
     return std::max(gmin, std::min(32, (rows + 63) / 64));
 }
 
@@ -650,12 +652,7 @@ static int forward(Work &w, int m, int n, int64_t N, int mode, int lcols, cudaSt
             }
             // trailing columns (swapped above): triangular solve, update of the rows below
             if (cs < n) {
-                // U12 = L11^{-1} P A12 (a single-CTA panel has written L11^{-1} already)
-                if (nbw > P1_NB || m - row > P1_MAX_ROWS) {
-                    GFFM_CUDA(cudaFuncSetAttribute(k_linv, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)LINV_SMEM));
-                    k_linv<<<NB / 32, 1024, LINV_SMEM, s>>>(w.W, w.ldw, row, col, t, w.piv_inv, w.linv, M);
-                    GFFM_LAUNCH_CHECK("k_linv");
-                }
+                // U12 = L11^{-1} P A12 (the panel has written L11^{-1})
                 st = rowmajor_gemm(w, N, w.W + (int64_t)row * w.ldw + cs, w.ldw, w.linv, NB,
                                    w.W + (int64_t)row * w.ldw + cs, w.ldw, t, n - cs, t, limb::EPI_STORE_I32, s);
                 if (st) return st;

@@ -103,6 +103,29 @@ def test_pluq_lookahead_sizes_match_oracle(gffm, case):
     test_pluq_matches_oracle(gffm, case)
 
 
+# More than 1536 rows below the first pivot: the cooperative left-looking panel
+# (128 columns over several CTAs) -- zero-column stops inside a panel and at its
+# start, a rank drop mid-panel, ties across CTAs, a narrow last panel.
+MULTI_CTA = [("uniform", 1700, 1700, P26), ("rank200", 1800, 1800, P26), ("zero_cols", 1700, 1750, 13),
+             ("ties", 1700, 1700, 3), ("uniform", 2500, 300, 65521), ("uniform", 1600, 2600, P25),
+             ("lead_zero", 1700, 1720, 7), ("rank100", 2000, 400, 65521)]
+
+
+@pytest.mark.parametrize("case", MULTI_CTA, ids=lambda c: "%s-%dx%d-%d" % c)
+def test_pluq_multi_cta_panel_matches_oracle(gffm, case):
+    test_pluq_matches_oracle(gffm, case)
+
+
+def test_rref_multi_cta_panel_matches_oracle(gffm):
+    rng = np.random.default_rng(77)
+    A = make("rank1700", 1800, 1900, P26, rng)
+    R, rank, piv = gffm.rref_gpu_type(gffm.CuModMatrix(A, P26, elem_type=torch.float64), return_pivots=True)
+    R0, rank0, piv0 = oracle.rref(A, P26)
+    assert rank == rank0 == 1700 and piv == [c + 1 for c in piv0]
+    np.testing.assert_array_equal(as_int(R), R0)
+    status_ok(gffm)
+
+
 def test_rref_lookahead_size_matches_oracle(gffm):
     rng = np.random.default_rng(77)
     A = make("rank1100", 1300, 1400, P26, rng)
@@ -146,7 +169,8 @@ def test_pluq_float32_storage(gffm):
 
 
 @pytest.mark.parametrize("case", [("uniform", 50, 50, 7), ("rank20", 60, 70, 11), ("zero_cols", 40, 45, 13),
-                                  ("uniform", 150, 100, P26), ("lead_zero", 70, 70, 65521)],
+                                  ("uniform", 150, 100, P26), ("lead_zero", 70, 70, 65521),
+                                  ("zero_cols", 1700, 1650, 65521)],
                          ids=lambda c: "%s-%dx%d-%d" % c)
 def test_lu_matches_oracle(gffm, case):
     kind, m, n, N = case
