@@ -83,11 +83,9 @@ __device__ __forceinline__ bool wait_row_word(const unsigned long long *p, uint3
 }
 
 __device__ __forceinline__ unsigned long long warp_max_u64(unsigned long long v) {
-    for (int o = 16; o; o >>= 1) {
-        const unsigned long long x = __shfl_xor_sync(0xffffffffu, v, o);
-        v = x > v ? x : v;
-    }
-    return v;
+    const unsigned hi = __reduce_max_sync(0xffffffffu, (unsigned)(v >> 32));
+    const unsigned lo = __reduce_max_sync(0xffffffffu, (unsigned)(v >> 32) == hi ? (unsigned)v : 0u);
+    return ((unsigned long long)hi << 32) | lo;
 }
 
 __device__ __forceinline__ uint32_t p1_red(uint64_t x, const ModP &M) {
@@ -114,61 +112,65 @@ __device__ __forceinline__ void p1_named_sync(int id, int nthreads) {
     asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
 }
 
-// Linv[tp][s] = inv * sum_{s <= q < tp} Lneg_piv[q] Linv[q][s] for s = tid < tp, and
-// Linv[tp][tp] = inv: the new row of the inverse of the panel's lower-triangular
-// factor (pivot values on its diagonal, negated multipliers Lneg = N - l).
-__device__ __forceinline__ void linv_row(uint32_t *LU, const uint32_t *piv, int tp, uint32_t inv, int tid,
+// Row tp of the inverse of the panel's lower-triangular factor (pivot values on
+// the diagonal, negated multipliers Lneg = N - l below), thread s < tp:
+//   Linv[tp][s] = inv * sum_{s <= q < tp} Lneg_tp[q] Linv[q][s],   Linv[tp][tp] = inv.
+// lp: Lneg_tp, zero from tp on.  LU[q][s] for q < s holds U, hence the mask.
+__device__ __forceinline__ void linv_row(uint32_t *LU, const uint32_t *lp, int tp, uint32_t inv, int s,
                                          const ModP &M) {
-    if (tid < tp) {
-        uint64_t a0 = 0, a1 = 0;
-        int q = tid;
-        for (; q + 1 < tp; q += 2) {
-            a0 += (uint64_t)piv[q] * LU[q * LU_LD + tid];
-            a1 += (uint64_t)piv[q + 1] * LU[(q + 1) * LU_LD + tid];
+    if (s < tp) {
+        uint64_t x0 = 0, x1 = 0;
+        for (int q = s & ~7; q < tp; q += 8) {
+            uint32_t va[8], vb[8];
+#pragma unroll
+            for (int k = 0; k < 8; k++) {
+                va[k] = q + k >= s ? lp[q + k] : 0u;
+                vb[k] = LU[(q + k) * LU_LD + s];
+            }
+#pragma unroll
+            for (int k = 0; k < 8; k += 2) {
+                x0 += (uint64_t)va[k] * vb[k];
+                x1 += (uint64_t)va[k + 1] * vb[k + 1];
+            }
         }
-        if (q < tp) a0 += (uint64_t)piv[q] * LU[q * LU_LD + tid];
-        LU[tp * LU_LD + tid] = mulmod(p1_red(a0 + a1, M), inv, M);
-    } else if (tid == tp) {
+        LU[tp * LU_LD + s] = mulmod(p1_red(x0 + x1, M), inv, M);
+    } else if (s == tp) {
         LU[tp * LU_LD + tp] = inv;
     }
 }
-// U[s][c] = sum_{q <= s} Linv[s][q] PR[q][c] for s = tid < np (PR: the pivot rows'
-// residues above the diagonal of LU)
-__device__ __forceinline__ void u_column(const uint32_t *LU, uint32_t *u, int np, int c, int tid, const ModP &M) {
-    if (tid < np) {
-        uint64_t a0 = 0, a1 = 0;
-        int q = 0;
-        for (; q + 1 <= tid; q += 2) {
-            a0 += (uint64_t)LU[tid * LU_LD + q] * LU[q * LU_LD + c];
-            a1 += (uint64_t)LU[tid * LU_LD + q + 1] * LU[(q + 1) * LU_LD + c];
-        }
-        if (q <= tid) a0 += (uint64_t)LU[tid * LU_LD + q] * LU[q * LU_LD + c];
-        u[tid] = p1_red(a0 + a1, M);
-    }
+// Row tp of U for column c > tp + 1 (thread c):
+//   U[tp][c] = inv * (W_tp[c] + sum_{s < tp} Lneg_tp[s] U[s][c]),
+// W_tp the pivot row's residues, lp its negated multipliers (zero from tp on).
+__device__ __forceinline__ void u_row(uint32_t *LU, const uint32_t *piv, const uint32_t *lp, int tp, uint32_t inv,
+                                      int c, const ModP &M) {
+    const uint64_t acc = p1_dot8(lp, 1, LU + c, LU_LD, (tp + 7) & ~7);
+    LU[tp * LU_LD + c] = mulmod(p1_red(acc + piv[c], M), inv, M);
 }
 
 // Cooperative left-looking panel factorization.  CTA b keeps rows
 // [R0 + b*R, R0 + (b+1)*R) of columns [C0, C0 + nbw) in shared memory,
 // column-major, thread lr < R owning row lr.  Column t is brought up to date
 // only when the pivot search reaches it:
-//   U[0:t][t] = Linv W_piv[0:t][t],   v[r] = W[r][t] + sum_{s<t} Lneg[r][s] U[s][t],
-// Linv the inverse of the panel's lower-triangular factor, W_piv the pivot rows'
-// residues, Lneg = N - l the negated multipliers -- one exact 64-bit dot product
-// per row, reduced once.  Every CTA keeps the same Linv and pivot rows (LU).
-// Per pivot step t:
+//   v[r] = W[r][t] + sum_{s<t} Lneg[r][s] U[s][t],
+// Lneg = N - l the negated multipliers -- one exact 64-bit dot product per row,
+// reduced once.  Every CTA keeps the same U rows of the panel's pivots,
+//   U[s][c] = inv_s (W_s[c] + sum_{s'<s} Lneg_s[s'] U[s'][c]),
+// (the reference's row scaling and updates in closed form) and the inverse Linv
+// of the panel's lower-triangular factor, in one square (LU).  Per pivot step t:
 //   A. each CTA publishes its candidate (largest residue of column t in its rows,
-//      lowest row on ties): the key and the row, tagged words; the owner of row
-//      r = R0 + t publishes that row too,
-//   B. while the auxiliary threads poll the G keys (bounded waits), the row
-//      threads form Linv's row t-1, U[0:t][t+1] and the partial values
+//      lowest row on ties): the key and the row, as tagged words; the owner of
+//      row r = R0 + t publishes that row too,
+//   B. while two auxiliary warps poll the G keys (bounded waits) and four form
+//      Linv's row t-1, the row threads form U's row t-1 and the partial values
 //      y[r] = W[r][t+1] + sum_{s<t} Lneg[r][s] U[s][t+1]; the owner of row r
 //      publishes y[r],
-//   C. every CTA picks the same winner, fetches its row (and, where the winner
-//      lands, the displaced row r with y[r]) while one warp computes the pivot's
-//      inverse by the reference's Euclid,
-//   D. the two rows move, U[t][t+1] = inv (W_piv[t][t+1] + sum_{s<t} Lneg_piv[s]
-//      U[s][t+1]) completes column t+1: v[r] = y[r] + Lneg[r][t] U[t][t+1], and
-//      the CTA's next candidate is its largest v.
+//   C. every warp picks the same winner; the CTA fetches its row (and, where the
+//      winner lands, the displaced row r with y[r]) while one warp computes the
+//      pivot's inverse by the reference's Euclid,
+//   D. every warp forms U[t][t+1] = inv (W_t[t+1] + sum_{s<t} Lneg_t[s] U[s][t+1]);
+//      the row threads complete column t+1, v[r] = y[r] + Lneg[r][t] U[t][t+1],
+//      and the CTA's next candidate is its largest v while the auxiliary warps
+//      move the two rows.
 // The panel is written back with the pivot rows scaled (U), the multipliers
 // unscaled below the pivots and the columns after a stop brought up to date;
 // CTA 0 writes L11^{-1} for the product U12 = L11^{-1} P A12.
@@ -176,14 +178,15 @@ __global__ void __launch_bounds__(PANEL_THREADS, 1) k_panel(PanelArgs a) {
     extern __shared__ __align__(16) uint32_t psm[];
     const int R = a.R, rs = R + 1;
     uint32_t *P = psm;                      // P[j * rs + lr]
-    uint32_t *LU = psm + (size_t)NB * rs;   // LU[s * LU_LD + c]: Linv (c <= s), pivot row s (c > s)
+    uint32_t *LU = psm + (size_t)NB * rs;   // LU[s * LU_LD + c]: Linv (c <= s), U (c > s); zero until formed
     __shared__ unsigned long long keys[MAX_PANEL_CTAS];
-    __shared__ uint32_t s_piv[NB];          // the pivot row: Lneg (c < t), residues (c > t)
-    __shared__ uint32_t s_old[NB + 1];      // the displaced row, and its partial value of column t+1
-    __shared__ __align__(16) uint32_t s_u[NB + 8];   // U[s][t+1] for s < t, zero from t on
+    __shared__ __align__(16) uint32_t s_piv[NB];     // the pivot row: Lneg (c < t), residues (c > t)
+    __shared__ __align__(16) uint32_t s_lp[NB + 8];  // its negated multipliers, zero from t on
+    __shared__ uint32_t s_old[NB + 1];               // the displaced row, and its partial value of column t+1
     __shared__ unsigned long long red[PANEL_WARPS];
-    __shared__ int s_stop, s_status, s_prow;
-    __shared__ uint32_t s_pv, s_inv, s_g;
+    __shared__ int s_stop, s_status;
+    __shared__ uint32_t s_inv;
+    __shared__ int32_t s_rec[3][NB];                 // pivot rows, values, inverses (written out after the loop)
     const int b = blockIdx.x, G = gridDim.x, tid = threadIdx.x;
     const int lane = tid & 31, warp = tid >> 5;
     const int rbeg = a.R0 + b * R;
@@ -194,12 +197,14 @@ __global__ void __launch_bounds__(PANEL_THREADS, 1) k_panel(PanelArgs a) {
     const uint32_t N = M.n;
     const int lr = tid, grow = rbeg + tid;
     const bool own = tid < nr;
+    const int x = tid - PANEL_AUX0;         // auxiliary thread index (>= 0)
 
     for (int e = tid; e < nr * nbw; e += PANEL_THREADS) {
         const int i = e / nbw, j = e - i * nbw;
         P[j * rs + i] = (uint32_t)a.W[(int64_t)(rbeg + i) * a.ldw + a.C0 + j];
     }
-    for (int i = tid; i < NB + 8; i += PANEL_THREADS) s_u[i] = 0;
+    for (int i = tid; i < NB * LU_LD; i += PANEL_THREADS) LU[i] = 0;
+    for (int i = tid; i < NB + 8; i += PANEL_THREADS) s_lp[i] = 0;
     if (tid == 0) {
         s_stop = 0;
         s_status = PS_DONE;
@@ -227,74 +232,61 @@ __global__ void __launch_bounds__(PANEL_THREADS, 1) k_panel(PanelArgs a) {
         const bool owner_r = r >= rbeg && r < rend;
         const bool next = t + 1 < nbw;
         unsigned long long *oldw = a.old_row + par * (NB + 1);
-        // A. publication
-        if (tid >= PANEL_AUX0) {
-            const int x = tid - PANEL_AUX0;
+        Rec *recs = a.rec + par * G;
+        if (x >= 0) {
+            // A. publication
             if (x < NB) {
-                Rec *mine = a.rec + par * G + b;
                 if (best != 0 && x < nbw)
-                    st_relaxed_u64(&mine->row[x],
+                    st_relaxed_u64(&recs[b].row[x],
                                    ((unsigned long long)tag << 32) | P[x * rs + (pkey_row(best) - rbeg)]);
-                if (x == 0) st_relaxed_u64(&mine->key, best | tag);
+                if (x == 0) st_relaxed_u64(&recs[b].key, best | tag);
             } else if (owner_r) {
                 for (int j = x - NB; j < nbw; j += PANEL_NAUX - NB)
                     st_relaxed_u64(&oldw[j], ((unsigned long long)tag << 32) | P[j * rs + (r - rbeg)]);
             }
-            // B (auxiliary threads): the G keys
-            for (int g = x; g < G; g += PANEL_NAUX) {
-                const unsigned long long *kp = &a.rec[par * G + g].key;
-                unsigned long long k = ld_relaxed_u64(kp);
-                if ((k & 0xFFFFull) != tag) {
-                    const unsigned long long t0 = gffm_dev::globaltimer();
-                    while (((k = ld_relaxed_u64(kp)) & 0xFFFFull) != tag) {
-                        if (gffm_dev::globaltimer() - t0 > gffm_dev::kWaitLimitNs) {
-                            atomicOr(a.err, 16);
-                            s_stop = 1;
-                            s_status = PS_TIMEOUT;
-                            k = 0;
-                            break;
-                        }
+            // B. two warps poll the keys, four form Linv's row t-1
+            if (x < 64) {
+                const int g0 = x, g1 = x + 64, g2 = x + 128;
+                unsigned pend = (g0 < G ? 1u : 0u) | (g1 < G ? 2u : 0u) | (g2 < G ? 4u : 0u);
+                const unsigned long long t0 = gffm_dev::globaltimer();
+                while (pend) {
+                    const unsigned long long k0 = (pend & 1u) ? ld_relaxed_u64(&recs[g0].key) : 0ull;
+                    const unsigned long long k1 = (pend & 2u) ? ld_relaxed_u64(&recs[g1].key) : 0ull;
+                    const unsigned long long k2 = (pend & 4u) ? ld_relaxed_u64(&recs[g2].key) : 0ull;
+                    if ((pend & 1u) && (k0 & 0xFFFFull) == tag) { keys[g0] = k0 & ~0xFFFFull; pend &= ~1u; }
+                    if ((pend & 2u) && (k1 & 0xFFFFull) == tag) { keys[g1] = k1 & ~0xFFFFull; pend &= ~2u; }
+                    if ((pend & 4u) && (k2 & 0xFFFFull) == tag) { keys[g2] = k2 & ~0xFFFFull; pend &= ~4u; }
+                    if (pend && gffm_dev::globaltimer() - t0 > gffm_dev::kWaitLimitNs) {
+                        atomicOr(a.err, 16);
+                        s_stop = 1;
+                        s_status = PS_TIMEOUT;
+                        break;
                     }
                 }
-                keys[g] = k & ~0xFFFFull;
+            } else if (x < 64 + NB && t > 0) {
+                linv_row(LU, s_lp, t - 1, s_inv, x - 64, M);
             }
         } else {
-            // B (row threads): Linv's row t-1, U[0:t][t+1], partial values of column t+1
-            if (t > 0) linv_row(LU, s_piv, t - 1, s_inv, tid, M);
+            // B. the row threads: U's row t-1, then the partial values of column t+1
+            if (t > 0 && tid > t && tid < nbw) u_row(LU, s_piv, s_lp, t - 1, s_inv, tid, M);
             p1_named_sync(1, PANEL_AUX0);
-            if (next) {
-                u_column(LU, s_u, t, t + 1, tid, M);
-                p1_named_sync(1, PANEL_AUX0);
-                if (own && grow >= r) {
-                    y = (uint64_t)P[(t + 1) * rs + lr] + p1_dot8(P + lr, rs, s_u, 1, (t + 7) & ~7);
-                    if (grow == r) st_relaxed_u64(&oldw[NB], ((unsigned long long)tag << 32) | p1_red(y, M));
-                }
+            if (next && own && grow >= r) {
+                y = (uint64_t)P[(t + 1) * rs + lr] + p1_dot8(P + lr, rs, LU + t + 1, LU_LD, (t + 7) & ~7);
+                if (grow == r) st_relaxed_u64(&oldw[NB], ((unsigned long long)tag << 32) | p1_red(y, M));
             }
         }
         __syncthreads();
         if (s_stop) break;
-        // C. the global pivot (every CTA decides the same)
-        if (warp == PANEL_WARPS - 1) {
-            unsigned long long wk = 0;
-            for (int g = lane; g < G; g += 32) wk = keys[g] > wk ? keys[g] : wk;
-            wk = warp_max_u64(wk);
-            if (lane == 0) {
-                const uint32_t pv = pkey_val(wk);
-                if (pv == 0) {
-                    s_stop = 1;
-                    s_status = PS_ZERO_COL;
-                } else if (a.l_cols > 0 && a.C0 + t >= a.l_cols) {
-                    s_stop = 1;
-                    s_status = PS_BOUNDS;
-                } else {
-                    s_prow = pkey_row(wk);
-                    s_pv = pv;
-                }
-            }
+        // C. the global pivot (every warp decides the same)
+        unsigned long long wk = 0;
+        for (int g = lane; g < G; g += 32) wk = keys[g] > wk ? keys[g] : wk;
+        wk = warp_max_u64(wk);
+        const uint32_t pv = pkey_val(wk);
+        if (pv == 0 || (a.l_cols > 0 && a.C0 + t >= a.l_cols)) {
+            if (tid == 0) s_status = pv == 0 ? PS_ZERO_COL : PS_BOUNDS;
+            break;
         }
-        __syncthreads();
-        if (s_stop) break;
-        const int prow = s_prow;
+        const int prow = pkey_row(wk);
         const int bw = (prow - a.R0) / R;
         const bool lands = bw == b && prow != r;   // the displaced row r moves into this CTA
         if (tid < nbw) {
@@ -305,6 +297,7 @@ __global__ void __launch_bounds__(PANEL_THREADS, 1) k_panel(PanelArgs a) {
                 s_status = PS_TIMEOUT;
             }
             s_piv[tid] = v;
+            s_lp[tid] = tid < t ? v : 0u;
         } else if (tid >= NB && tid <= 2 * NB && lands) {
             const int j = tid - NB;
             if (j < nbw || (j == NB && next)) {
@@ -317,40 +310,46 @@ __global__ void __launch_bounds__(PANEL_THREADS, 1) k_panel(PanelArgs a) {
                 s_old[j] = v;
             }
         } else if (tid == PANEL_THREADS - 32) {
-            s_inv = mod_inv_euclid_alu(s_pv, N);
+            s_inv = mod_inv_euclid_alu(pv, N);
         }
         __syncthreads();
         if (s_stop) break;
-        // D. row moves, the pivot row's residues, U[t][t+1]
-        const uint32_t inv = s_inv, pv = s_pv;
-        if (owner_r && tid <= t) P[tid * rs + (r - rbeg)] = tid < t ? s_piv[tid] : mulmod(pv, inv, M);
-        if (lands && tid < nbw) P[tid * rs + (prow - rbeg)] = s_old[tid];
-        if (lands && tid == prow - rbeg) y = s_old[NB];
-        if (tid > t && tid < nbw) LU[t * LU_LD + tid] = s_piv[tid];
-        if (warp == PANEL_WARPS - 2 && next) {
+        // D. U[t][t+1] (every warp), column t+1 and the next candidate (row threads),
+        //    the row moves (auxiliary threads)
+        const uint32_t inv = s_inv;
+        uint32_t g = 0;
+        if (next) {
             uint64_t acc = 0;
-            for (int s = lane; s < t; s += 32) acc += (uint64_t)s_piv[s] * s_u[s];
-            uint32_t p = p1_red(acc, M);   // 32 residues sum below 2^31
-            for (int o = 16; o; o >>= 1) p += __shfl_xor_sync(0xffffffffu, p, o);
-            if (lane == 0) s_g = mulmod(p1_red((uint64_t)p + s_piv[t + 1], M), inv, M);
+            for (int s = lane; s < t; s += 32) acc += (uint64_t)s_lp[s] * LU[s * LU_LD + t + 1];
+            const uint32_t part = __reduce_add_sync(0xffffffffu, p1_red(acc, M));   // 32 residues: below 2^31
+            g = mulmod(p1_red((uint64_t)part + s_piv[t + 1], M), inv, M);
         }
-        if (b == 0 && tid == 0) {
-            a.piv_row[t] = prow;
-            a.piv_val[t] = (int32_t)pv;
-            a.piv_inv[t] = (int32_t)inv;
-        }
-        __syncthreads();
-        // column t+1: the rows below the pivot and the pivot rows' U values; next candidate
         best = 0;
-        if (next && own) {
-            const uint32_t g = s_g;
-            if (grow > r) {
-                const uint32_t v = p1_red(y + (uint64_t)P[t * rs + lr] * g, M);
-                P[(t + 1) * rs + lr] = v ? N - v : 0u;
-                best = pkey(v, grow);
-            } else {
-                const int s = grow - a.R0;
-                P[(t + 1) * rs + lr] = s < t ? s_u[s] : g;
+        if (x < 0) {
+            if (next && own) {
+                if (grow > r) {
+                    const bool moved = lands && grow == prow;
+                    const uint32_t lt = moved ? s_old[t] : P[t * rs + lr];
+                    const uint64_t yy = moved ? (uint64_t)s_old[NB] : y;
+                    const uint32_t v = p1_red(yy + (uint64_t)lt * g, M);
+                    P[(t + 1) * rs + lr] = v ? N - v : 0u;
+                    best = pkey(v, grow);
+                } else {
+                    const int s = grow - a.R0;
+                    P[(t + 1) * rs + lr] = s < t ? LU[s * LU_LD + t + 1] : g;
+                }
+            }
+        } else {
+            if (owner_r)
+                for (int j = x; j <= t; j += PANEL_NAUX) P[j * rs + (r - rbeg)] = j < t ? s_piv[j] : mulmod(pv, inv, M);
+            if (lands)
+                for (int j = x; j < nbw; j += PANEL_NAUX)
+                    if (j != t + 1) P[j * rs + (prow - rbeg)] = s_old[j];
+            if (x == 0) {
+                if (next) LU[t * LU_LD + t + 1] = g;
+                s_rec[0][t] = prow;
+                s_rec[1][t] = (int32_t)pv;
+                s_rec[2][t] = (int32_t)inv;
             }
         }
         best = warp_max_u64(best);
@@ -360,32 +359,35 @@ __global__ void __launch_bounds__(PANEL_THREADS, 1) k_panel(PanelArgs a) {
     }
     __syncthreads();
     const int npiv = t, status = s_status;
-    if (status == PS_DONE || status == PS_ZERO_COL) {
-        // Linv's last row, then the columns after a stop (the column at a zero stop is
-        // final already): U by Linv, the rows below by the multipliers
-        if (npiv > 0) linv_row(LU, s_piv, npiv - 1, s_inv, tid, M);
+    if (npiv > 0 && (status == PS_DONE || status == PS_ZERO_COL)) {
+        // the last pivot's rows of Linv and U, then the columns after a stop (the
+        // column at a zero stop is final already): U above, the multipliers below
+        if (x >= 0 && x < NB) linv_row(LU, s_lp, npiv - 1, s_inv, x, M);
+        if (x < 0 && tid > npiv && tid < nbw) u_row(LU, s_piv, s_lp, npiv - 1, s_inv, tid, M);
         __syncthreads();
-        for (int j = npiv + 1; npiv > 0 && j < nbw; j++) {
-            u_column(LU, s_u, npiv, j, tid, M);
-            __syncthreads();
-            if (own) {
+        if (own)
+            for (int j = npiv + 1; j < nbw; j++) {
                 if (grow >= a.R0 + npiv)
-                    P[j * rs + lr] = p1_red((uint64_t)P[j * rs + lr] + p1_dot8(P + lr, rs, s_u, 1, (npiv + 7) & ~7), M);
+                    P[j * rs + lr] = p1_red((uint64_t)P[j * rs + lr] + p1_dot8(P + lr, rs, LU + j, LU_LD, (npiv + 7) & ~7), M);
                 else
-                    P[j * rs + lr] = s_u[grow - a.R0];
+                    P[j * rs + lr] = LU[(grow - a.R0) * LU_LD + j];
             }
-            __syncthreads();
-        }
+        __syncthreads();
     }
     // back to W: pivot columns hold U on and above the diagonal and the unscaled
     // multipliers below it; the other columns their current residues
     for (int e = tid; e < nr * nbw; e += PANEL_THREADS) {
         const int i = e / nbw, j = e - i * nbw;
-        uint32_t x = P[j * rs + i];
-        if (j < npiv && rbeg + i > a.R0 + j) x = x ? N - x : 0u;
-        a.W[(int64_t)(rbeg + i) * a.ldw + a.C0 + j] = (int32_t)x;
+        uint32_t v = P[j * rs + i];
+        if (j < npiv && rbeg + i > a.R0 + j) v = v ? N - v : 0u;
+        a.W[(int64_t)(rbeg + i) * a.ldw + a.C0 + j] = (int32_t)v;
     }
     if (b == 0) {
+        for (int e = tid; e < npiv; e += PANEL_THREADS) {
+            a.piv_row[e] = s_rec[0][e];
+            a.piv_val[e] = s_rec[1][e];
+            a.piv_inv[e] = s_rec[2][e];
+        }
         for (int e = tid; e < npiv * npiv; e += PANEL_THREADS) {
             const int i = e / npiv, j = e - i * npiv;
             a.linv[i * NB + j] = j <= i ? (int32_t)LU[i * LU_LD + j] : 0;
