@@ -26,9 +26,12 @@
 // sum_s C_s * (2^(7s) mod N) into int64 registers; the final value is reduced
 // mod N with Barrett's method and stored.
 //
-// Warp roles (320 threads): warp 0 issues TMA loads, warp 1 allocates TMEM
-// and one lane issues the mma's, warps 2..9 are the epilogue (two warps per
-// 32-lane TMEM quadrant, each owning 32 of the 64 output columns).  Every
+// Warp roles: warp 0 issues TMA loads, warp 1 allocates TMEM and one lane
+// issues the mma's, the other warps are the epilogue -- 8 (two per 32-lane
+// TMEM quadrant, each owning 32 of the 64 output columns), or 16 of 16
+// columns for the read-modify-write epilogue, whose tiles are short (the
+// elimination's K = 128 updates) and whose per-tile chain (drain, reduction,
+// C read and write) then paces the mma's.  Every
 // wait is bounded; on timeout a kernel records the failure in the library's
 // error word and returns without storing.
 #pragma once
@@ -43,15 +46,18 @@ constexpr int BN = 64;             // output columns per tile
 constexpr int BK = 64;             // k per pipeline stage (one 128-byte swizzle row of fp16)
 constexpr int A_TILE = BM * BK * 2;
 constexpr int B_TILE = BN * BK * 2;
-constexpr int NUM_EPI_WARPS = 8;
+constexpr int NUM_EPI_WARPS = 8;                      // the batched grouped GEMM's epilogue warps
 constexpr int NUM_THREADS = 64 + 32 * NUM_EPI_WARPS;
+// epilogue warps and threads per CTA for an epilogue kind
+__host__ __device__ constexpr int epi_warps(int epi) { return epi == 2 /* EPI_SUB_I32 */ ? 16 : 8; }
+__host__ __device__ constexpr int gemm_threads(int epi) { return 64 + 32 * epi_warps(epi); }
 constexpr int MAX_SHIFTS = 7;
 constexpr int TILE_GROUP = 16;     // output-tile rows per raster group (L2 reuse)
 
-// Tile width BNV: 64 (one accumulator set, 8 epilogue warps on 2 x 32 columns) or 32
-// (two accumulator sets in TMEM, 4 epilogue warps per set: the drain of one tile
-// overlaps the mma's of the next -- for short K, where a tile is one or two
-// exact chunks and the drain is as long as the products).
+// Tile width BNV: 64 (one accumulator set) or 32 (two accumulator sets in TMEM,
+// half the epilogue warps per set: the drain of one tile overlaps the mma's of
+// the next -- for short K, where a tile is one or two exact chunks and the
+// drain is as long as the products).
 template <int L, int BNV = 64>
 struct Cfg {
     static constexpr int B_T = BNV * BK * 2;
@@ -61,7 +67,6 @@ struct Cfg {
     static constexpr int NSHIFT = 2 * L - 1;
     static constexpr int ACC_BUFS = BNV == 32 ? 2 : 1;
     static constexpr int BUF_COLS = BNV == 32 ? 256 : 0;   // column offset of the second accumulator set
-    static constexpr int EPI_PER_BUF = NUM_EPI_WARPS / ACC_BUFS;
     static constexpr int TMEM_COLS = BNV == 32 ? 512
                                                : ((64 * NSHIFT <= 64) ? 64 : (64 * NSHIFT <= 128 ? 128 : (64 * NSHIFT <= 256 ? 256 : 512)));
     static constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024;
@@ -99,10 +104,13 @@ __device__ __forceinline__ int64_t reduce_signed(int64_t acc, const Params &p) {
 }
 
 template <int L, int EPI, int BNV = 64>
-__global__ void __launch_bounds__(NUM_THREADS, 1)
+__global__ void __launch_bounds__(gemm_threads(EPI), 1)
     k_gemm_limb(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, Params p) {
     using C_ = Cfg<L, BNV>;
     constexpr int AB = C_::ACC_BUFS;
+    constexpr int EW = epi_warps(EPI);
+    constexpr int EPB = EW / AB;         // epilogue warps per accumulator set
+    constexpr int CW = BNV / (EPB / 4);  // output columns per epilogue warp (32 or 16)
     extern __shared__ uint8_t dsmem_raw[];
     __shared__ uint64_t full_bar[C_::STAGES];
     __shared__ uint64_t empty_bar[C_::STAGES];
@@ -124,7 +132,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
         }
         for (int b = 0; b < AB; b++) {
             gffm_dev::mbar_init(&acc_full_bar[b], 1);
-            gffm_dev::mbar_init(&acc_empty_bar[b], C_::EPI_PER_BUF);
+            gffm_dev::mbar_init(&acc_empty_bar[b], EPB);
         }
         gffm_dev::mbar_init(&drain_bar, 1);
         abort_s = 0;
@@ -253,19 +261,30 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
         // ---------------- epilogue ----------------
         const int ew = warp - 2;
         const int quad = warp & 3;       // TMEM lane quadrant this warp may access
-        // BNV = 64: `half` picks which 32 of the 64 tile columns; BNV = 32: which accumulator set
-        const int half = ew >> 2;
+        // each group of four consecutive warps covers the four quadrants; a group
+        // owns one accumulator set (BNV = 32) and CW of its columns
+        const int grp = ew >> 2;
+        const int buf = AB == 2 ? grp / (EPB / 4) : 0;
+        const int part = grp % (EPB / 4);
         uint32_t acc_phase = 0;
         int local = 0;
         for (int t = blockIdx.x; t < ntiles_total; t += gridDim.x, local++) {
-            if (AB == 2 && (local & 1) != half) continue;      // the other warp group's tile
-            const int buf = AB == 2 ? half : 0;
-            const uint32_t accb = tmem + (uint32_t)(buf * C_::BUF_COLS) + (AB == 2 ? 0u : (uint32_t)(32 * half));
+            if (AB == 2 && (local & 1) != buf) continue;      // the other warp group's tile
+            const uint32_t accb = tmem + (uint32_t)(buf * C_::BUF_COLS) + (uint32_t)(CW * part);
             int tm, tn;
             tile_coords(t, p.mtiles, p.ntiles, tm, tn);
-            int64_t acc[32];
+            const int64_t row = (int64_t)tm * BM + quad * 32 + lane;
+            const int64_t col0 = (int64_t)tn * BNV + CW * part;
+            // read-modify-write: C's values are loaded before the accumulators are ready
+            int32_t cv[EPI == EPI_SUB_I32 ? CW : 1];
+            if (EPI == EPI_SUB_I32) {
+                const int32_t *cbase = (const int32_t *)p.C + row + col0 * p.ldc;
 #pragma unroll
-            for (int j = 0; j < 32; j++) acc[j] = 0;
+                for (int j = 0; j < CW; j++) cv[j] = (row < p.m && col0 + j < p.n) ? __ldcg(cbase + j * p.ldc) : 0;
+            }
+            int64_t acc[CW];
+#pragma unroll
+            for (int j = 0; j < CW; j++) acc[j] = 0;
             bool ok = true;
             int chunk = 0;
             for (int kb0 = 0; kb0 < p.kblocks; kb0 += p.chunk_kb, chunk++) {
@@ -278,20 +297,20 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
                 gffm_dev::tc_fence_after();
 #pragma unroll
                 for (int s = 0; s < C_::NSHIFT; s++) {
-                    uint32_t v[32];
-                    gffm_dev::tmem_ld_32x32b_x32(accb + ((uint32_t)(quad * 32) << 16) + BNV * s, v);
+                    uint32_t v[CW];
+                    gffm_dev::tmem_ld_32x32b<CW>(accb + ((uint32_t)(quad * 32) << 16) + BNV * s, v);
                     gffm_dev::tmem_ld_wait();
                     if (EPI == EPI_EXACT_I64) {
                         // exact chunk value sum_s C_s 2^(7s), in [0, 2^62) for raw digits: wrapping
                         // 64-bit sums are exact once every shift has been added
 #pragma unroll
-                        for (int j = 0; j < 32; j++)
+                        for (int j = 0; j < CW; j++)
                             acc[j] = (int64_t)((uint64_t)acc[j] +
                                                ((uint64_t)(int64_t)__float2int_rz(__uint_as_float(v[j])) << (7 * s)));
                     } else {
                         const int w = p.W[s];
 #pragma unroll
-                        for (int j = 0; j < 32; j++) acc[j] += (int64_t)__float2int_rz(__uint_as_float(v[j])) * w;
+                        for (int j = 0; j < CW; j++) acc[j] += (int64_t)__float2int_rz(__uint_as_float(v[j])) * w;
                     }
                 }
                 gffm_dev::tc_fence_before();
@@ -301,25 +320,19 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
                 if (EPI == EPI_EXACT_I64) {
                     // acc < N < 2^52 before the chunk, so acc + chunk < 2^63: one Barrett step
 #pragma unroll
-                    for (int j = 0; j < 32; j++)
+                    for (int j = 0; j < CW; j++)
                         acc[j] = (int64_t)gffm_dev::barrett64((uint64_t)acc[j], (uint64_t)p.N, p.minv);
                 } else if ((chunk & 63) == 63) {
 #pragma unroll
-                    for (int j = 0; j < 32; j++) acc[j] = reduce_signed(acc[j], p);
+                    for (int j = 0; j < CW; j++) acc[j] = reduce_signed(acc[j], p);
                 }
             }
             if (!ok || abort_s) break;
-            const int64_t row = (int64_t)tm * BM + quad * 32 + lane;
-            const int64_t col0 = (int64_t)tn * BNV + (AB == 2 ? 0 : half * 32);
             if (row < p.m) {
                 if (EPI == EPI_SUB_I32) {
-                    // read-modify-write: issue all 32 loads before any store
                     int32_t *cbase = (int32_t *)p.C + row + col0 * p.ldc;
-                    int32_t cv[32];
 #pragma unroll
-                    for (int j = 0; j < 32; j++) cv[j] = (col0 + j < p.n) ? __ldcg(cbase + j * p.ldc) : 0;
-#pragma unroll
-                    for (int j = 0; j < 32; j++) {
+                    for (int j = 0; j < CW; j++) {
                         if (col0 + j < p.n) {
                             const int64_t v = (int64_t)cv[j] - reduce_signed(acc[j], p);
                             cbase[j * p.ldc] = (int32_t)(v < 0 ? v + p.N : v);
@@ -328,17 +341,17 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
                 } else if (EPI == EPI_EXACT_I64) {
                     int64_t *cbase = (int64_t *)p.C + row + col0 * p.ldc;
 #pragma unroll
-                    for (int j = 0; j < 32; j++)
+                    for (int j = 0; j < CW; j++)
                         if (col0 + j < p.n) cbase[j * p.ldc] = acc[j];
                 } else if (EPI == EPI_KSUB_F64) {
                     // C = (AB - X - Y) mod N: all subtrahend loads before any store
                     const int64_t base = row + col0 * p.ldc;
-                    double xv[32];
+                    double xv[CW];
 #pragma unroll
-                    for (int j = 0; j < 32; j++)
+                    for (int j = 0; j < CW; j++)
                         xv[j] = (col0 + j < p.n) ? __ldcg(p.X + base + j * p.ldc) + __ldcg(p.Y + base + j * p.ldc) : 0.0;
 #pragma unroll
-                    for (int j = 0; j < 32; j++) {
+                    for (int j = 0; j < CW; j++) {
                         if (col0 + j < p.n) {
                             int64_t v = reduce_signed(acc[j], p) - (int64_t)xv[j];   // X + Y < 2N, exact in double
                             v += (v < 0) ? p.N : 0;
@@ -348,7 +361,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
                     }
                 } else {
 #pragma unroll
-                    for (int j = 0; j < 32; j++) {
+                    for (int j = 0; j < CW; j++) {
                         const int64_t col = col0 + j;
                         if (col < p.n) {
                             const int64_t r = reduce_signed(acc[j], p);

@@ -13,7 +13,7 @@ static int launch_gemm_L(const CUtensorMap &ta, const CUtensorMap &tb, const Par
     constexpr int smem = Cfg<L, BNV>::SMEM_BYTES;
     GFFM_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
     gffm::profile_hook().before(s);
-    kern<<<grid, NUM_THREADS, smem, s>>>(ta, tb, p);
+    kern<<<grid, gemm_threads(EPI), smem, s>>>(ta, tb, p);
     gffm::profile_hook().after(s);
     GFFM_LAUNCH_CHECK("k_gemm_limb");
     return GFFM_OK;
