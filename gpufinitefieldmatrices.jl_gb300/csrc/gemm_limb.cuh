@@ -49,7 +49,7 @@ constexpr int B_TILE = BN * BK * 2;
 constexpr int NUM_EPI_WARPS = 8;                      // the batched grouped GEMM's epilogue warps
 constexpr int NUM_THREADS = 64 + 32 * NUM_EPI_WARPS;
 // epilogue warps and threads per CTA for an epilogue kind
-__host__ __device__ constexpr int epi_warps(int epi) { return epi == 2 /* EPI_SUB_I32 */ ? 16 : 8; }
+__host__ __device__ constexpr int epi_warps(int epi) { return epi == EPI_SUB_I32 || epi == EPI_SUB_I32M ? 16 : 8; }
 __host__ __device__ constexpr int gemm_threads(int epi) { return 64 + 32 * epi_warps(epi); }
 constexpr int MAX_SHIFTS = 7;
 constexpr int TILE_GROUP = 16;     // output-tile rows per raster group (L2 reuse)
@@ -87,6 +87,12 @@ struct Params {
     int64_t ldc;
     const double *X, *Y;   // EPI_KSUB_F64 subtrahends
     int *err;
+    // EPI_SUB_I32M (EPI_SUB_I32 with odd N, one exact chunk whose shift sums stay below 2^22):
+    // the chunk values are read by adding 1.5 * 2^23 in fp32 (the integer lands in the
+    // mantissa) and reduced by a 32-bit Montgomery step, the weights carrying 2^32.
+    uint32_t ninv;             // -N^-1 mod 2^32
+    int32_t Wm[MAX_SHIFTS];    // 2^(bits*s) * 2^32 mod N
+    int64_t fbias;             // N * 2^25 - 0x4B400000 * sum_s Wm[s]
 };
 
 __device__ __forceinline__ void tile_coords(int t, int mtiles, int ntiles, int &tm, int &tn) {
@@ -111,6 +117,8 @@ __global__ void __launch_bounds__(gemm_threads(EPI), 1)
     constexpr int EW = epi_warps(EPI);
     constexpr int EPB = EW / AB;         // epilogue warps per accumulator set
     constexpr int CW = BNV / (EPB / 4);  // output columns per epilogue warp (32 or 16)
+    constexpr bool SUB = EPI == EPI_SUB_I32 || EPI == EPI_SUB_I32M;   // read-modify-write of int32 C
+    constexpr bool FAST = EPI == EPI_SUB_I32M;
     extern __shared__ uint8_t dsmem_raw[];
     __shared__ uint64_t full_bar[C_::STAGES];
     __shared__ uint64_t empty_bar[C_::STAGES];
@@ -276,15 +284,15 @@ __global__ void __launch_bounds__(gemm_threads(EPI), 1)
             const int64_t row = (int64_t)tm * BM + quad * 32 + lane;
             const int64_t col0 = (int64_t)tn * BNV + CW * part;
             // read-modify-write: C's values are loaded before the accumulators are ready
-            int32_t cv[EPI == EPI_SUB_I32 ? CW : 1];
-            if (EPI == EPI_SUB_I32) {
+            int32_t cv[SUB ? CW : 1];
+            if (SUB) {
                 const int32_t *cbase = (const int32_t *)p.C + row + col0 * p.ldc;
 #pragma unroll
                 for (int j = 0; j < CW; j++) cv[j] = (row < p.m && col0 + j < p.n) ? __ldcg(cbase + j * p.ldc) : 0;
             }
             int64_t acc[CW];
 #pragma unroll
-            for (int j = 0; j < CW; j++) acc[j] = 0;
+            for (int j = 0; j < CW; j++) acc[j] = FAST ? p.fbias : 0;
             bool ok = true;
             int chunk = 0;
             for (int kb0 = 0; kb0 < p.kblocks; kb0 += p.chunk_kb, chunk++) {
@@ -307,6 +315,13 @@ __global__ void __launch_bounds__(gemm_threads(EPI), 1)
                         for (int j = 0; j < CW; j++)
                             acc[j] = (int64_t)((uint64_t)acc[j] +
                                                ((uint64_t)(int64_t)__float2int_rz(__uint_as_float(v[j])) << (7 * s)));
+                    } else if (FAST) {
+                        // bits(C + 1.5 * 2^23) = 0x4B400000 + C for |C| < 2^22; the constant
+                        // is taken out through the initial value (fbias)
+                        const int w = p.Wm[s];
+#pragma unroll
+                        for (int j = 0; j < CW; j++)
+                            acc[j] += (int64_t)(int32_t)__float_as_uint(__fadd_rn(__uint_as_float(v[j]), 12582912.0f)) * w;
                     } else {
                         const int w = p.W[s];
 #pragma unroll
@@ -329,13 +344,27 @@ __global__ void __launch_bounds__(gemm_threads(EPI), 1)
             }
             if (!ok || abort_s) break;
             if (row < p.m) {
-                if (EPI == EPI_SUB_I32) {
+                if (SUB) {
                     int32_t *cbase = (int32_t *)p.C + row + col0 * p.ldc;
+                    if (FAST) {
+                        // x in [0, 2^26 N): t = (x + m N) / 2^32 < 2N, t = x 2^-32 mod N
+                        const uint32_t n32 = (uint32_t)p.N;
 #pragma unroll
-                    for (int j = 0; j < CW; j++) {
-                        if (col0 + j < p.n) {
-                            const int64_t v = (int64_t)cv[j] - reduce_signed(acc[j], p);
-                            cbase[j * p.ldc] = (int32_t)(v < 0 ? v + p.N : v);
+                        for (int j = 0; j < CW; j++) {
+                            const uint64_t x = (uint64_t)acc[j];
+                            const uint32_t m = (uint32_t)x * p.ninv;
+                            uint32_t r = (uint32_t)((x + (uint64_t)m * n32) >> 32);
+                            r = r >= n32 ? r - n32 : r;
+                            const int32_t v = cv[j] - (int32_t)r;
+                            if (col0 + CW <= p.n || col0 + j < p.n) cbase[j * p.ldc] = v < 0 ? v + (int32_t)n32 : v;
+                        }
+                    } else {
+#pragma unroll
+                        for (int j = 0; j < CW; j++) {
+                            if (col0 + j < p.n) {
+                                const int64_t v = (int64_t)cv[j] - reduce_signed(acc[j], p);
+                                cbase[j * p.ldc] = (int32_t)(v < 0 ? v + p.N : v);
+                            }
                         }
                     }
                 } else if (EPI == EPI_EXACT_I64) {

@@ -232,6 +232,20 @@ int gemm_digits(const Layout &g, const __half *Ad, const __half *Bd, int64_t m, 
         p.W[sft] = (int32_t)w;      // unused by EPI_EXACT_I64, whose N may exceed 32 bits
         w = (int64_t)(((__int128)w * (g.bits == 8 ? 256 : 128)) % N);
     }
+    // the read-modify-write fast path: odd N, one exact chunk, shift sums below 2^22
+    if (epi == EPI_SUB_I32 && (N & 1) && p.kblocks <= p.chunk_kb &&
+        (int64_t)p.kblocks * BK * g.L * (int64_t(1) << (2 * g.bits - 2)) <= (int64_t(1) << 22)) {
+        uint32_t inv = 1;                         // N^-1 mod 2^32 by Newton's iteration
+        for (int it = 0; it < 5; it++) inv *= 2u - (uint32_t)N * inv;
+        p.ninv = 0u - inv;
+        int64_t wsum = 0;
+        for (int sft = 0; sft < MAX_SHIFTS; sft++) {
+            p.Wm[sft] = (int32_t)(((__int128)p.W[sft] << 32) % N);
+            if (sft < 2 * g.L - 1) wsum += p.Wm[sft];
+        }
+        p.fbias = N * (int64_t(1) << 25) - (int64_t)0x4B400000 * wsum;
+        epi = EPI_SUB_I32M;
+    }
     p.C = C;
     p.ldc = ldc;
     p.X = X;
@@ -250,6 +264,7 @@ int gemm_digits(const Layout &g, const __half *Ad, const __half *Bd, int64_t m, 
         case EPI_STORE_I32: return launch_gemm<EPI_STORE_I32>(g.L, ta, tb, p, grid, s);
         case EPI_EXACT_I64: return launch_gemm<EPI_EXACT_I64>(g.L, ta, tb, p, grid, s);
         case EPI_KSUB_F64: return launch_gemm<EPI_KSUB_F64>(g.L, ta, tb, p, grid, s);
+        case EPI_SUB_I32M: return launch_gemm<EPI_SUB_I32M>(g.L, ta, tb, p, grid, s);
         default: return launch_gemm<EPI_SUB_I32>(g.L, ta, tb, p, grid, s);
     }
 }

@@ -26,6 +26,7 @@ int launch_gemm_short(int epi, int L, const CUtensorMap &ta, const CUtensorMap &
         case EPI_STORE_I32: return launch_short_L<EPI_STORE_I32>(L, ta, tb, p, grid, s);
         case EPI_EXACT_I64: return launch_short_L<EPI_EXACT_I64>(L, ta, tb, p, grid, s);
         case EPI_KSUB_F64: return launch_short_L<EPI_KSUB_F64>(L, ta, tb, p, grid, s);
+        case EPI_SUB_I32M: return launch_short_L<EPI_SUB_I32M>(L, ta, tb, p, grid, s);
         default: return launch_short_L<EPI_SUB_I32>(L, ta, tb, p, grid, s);
     }
 }

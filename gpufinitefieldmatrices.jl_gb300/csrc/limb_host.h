@@ -15,7 +15,9 @@ namespace limb {
 //   EPI_EXACT_I64              C = AB mod N on int64 for 2 <= N < 2^52, from NON-centred digits
 //                              (SPLIT_RAW): every exact chunk value is folded in modulo N
 //   EPI_KSUB_F64               C = (AB - X - Y) mod N on Float64, X and Y Float64 residues with C's ldc
-enum Epi { EPI_STORE_F64 = 0, EPI_STORE_F32 = 1, EPI_SUB_I32 = 2, EPI_STORE_I32 = 3, EPI_EXACT_I64 = 4, EPI_KSUB_F64 = 5 };
+//   EPI_SUB_I32M               EPI_SUB_I32 with odd N and one exact chunk (selected inside gemm_digits)
+enum Epi { EPI_STORE_F64 = 0, EPI_STORE_F32 = 1, EPI_SUB_I32 = 2, EPI_STORE_I32 = 3, EPI_EXACT_I64 = 4, EPI_KSUB_F64 = 5,
+           EPI_SUB_I32M = 6 };
 
 // digit split of an operand:
 //   SPLIT_CENTRED  x mod N centred into (-N/2, N/2]
