@@ -21,13 +21,18 @@ namespace batched {
 using namespace limb;
 
 struct MMInst {
-    int m, n, L, kblocks, mtiles, ntiles, chunk_kb, Mpad, Npad, pad_;
-    int32_t W[MAX_SHIFTS];       // 2^(7s) mod N
+    int m, n, L, kblocks, mtiles, ntiles, chunk_kb, Mpad, Npad, fast;
+    int32_t W[MAX_SHIFTS];       // 2^(bits s) mod N
     int64_t N;
     uint64_t minv;
     int64_t bias;
     double *C;
     int64_t ldc;
+    // fast epilogue (odd N, one exact chunk whose shift sums stay within 2^22): the sums
+    // are read by adding 1.5 * 2^23 in fp32 and reduced by one 32-bit Montgomery step
+    uint32_t ninv;               // -N^-1 mod 2^32
+    int32_t Wm[MAX_SHIFTS];      // 2^(bits s) * 2^32 mod N
+    int64_t fbias;               // N * 2^25 - 0x4B400000 * sum_s Wm[s]
 };
 
 struct WorkItem {
@@ -143,7 +148,75 @@ __device__ __forceinline__ int64_t reduce_inst(int64_t acc, const MMInst &I) {
     return (int64_t)gffm_dev::barrett64((uint64_t)(acc + I.bias), (uint64_t)I.N, I.minv);
 }
 
-__global__ void __launch_bounds__(NUM_THREADS, 1)
+// epilogue warps of the grouped GEMM: four per TMEM lane quadrant, 16 columns each
+constexpr int G_EPI_WARPS = 16;
+constexpr int G_THREADS = 64 + 32 * G_EPI_WARPS;
+
+// one tile's drain and store by one epilogue warp (32 rows x 16 columns)
+template <bool FAST>
+__device__ __forceinline__ bool grouped_tile(const MMInst &I, const WorkItem &it, uint32_t tq, int quad, int part,
+                                             int lane, uint64_t *acc_full_bar, uint64_t *acc_empty_bar,
+                                             uint32_t &acc_phase, int *err, volatile int &abort_s) {
+    const int nshift = 2 * I.L - 1;
+    int64_t acc[16];
+#pragma unroll
+    for (int j = 0; j < 16; j++) acc[j] = FAST ? I.fbias : 0;
+    int chunk = 0;
+    for (int kb0 = 0; kb0 < I.kblocks; kb0 += I.chunk_kb, chunk++) {
+        if (!gffm_dev::mbar_wait(acc_full_bar, acc_phase)) {
+            atomicOr(err, 8);
+            abort_s = 1;
+            return false;
+        }
+        gffm_dev::tc_fence_after();
+        for (int s = 0; s < nshift; s++) {
+            uint32_t v[16];
+            gffm_dev::tmem_ld_32x32b_x16(tq + 64 * s, v);
+            gffm_dev::tmem_ld_wait();
+            if (FAST) {
+                const int w = I.Wm[s];
+#pragma unroll
+                for (int j = 0; j < 16; j++)
+                    acc[j] += (int64_t)(int32_t)__float_as_uint(__fadd_rn(__uint_as_float(v[j]), 12582912.0f)) * w;
+            } else {
+                const int w = I.W[s];
+#pragma unroll
+                for (int j = 0; j < 16; j++) acc[j] += (int64_t)__float2int_rz(__uint_as_float(v[j])) * w;
+            }
+        }
+        gffm_dev::tc_fence_before();
+        __syncwarp();
+        if (lane == 0) gffm_dev::mbar_arrive(acc_empty_bar);
+        acc_phase ^= 1;
+        if (!FAST && (chunk & 63) == 63) {
+#pragma unroll
+            for (int j = 0; j < 16; j++) acc[j] = reduce_inst(acc[j], I);
+        }
+    }
+    const int64_t row = (int64_t)it.tm * BM + quad * 32 + lane;
+    const int64_t col0 = (int64_t)it.tn * BN + part * 16;
+    if (row < I.m) {
+        double *cb = I.C + row + col0 * I.ldc;
+        const uint32_t n32 = (uint32_t)I.N;
+#pragma unroll
+        for (int j = 0; j < 16; j++) {
+            if (col0 + j < I.n) {
+                if (FAST) {
+                    // x in [0, 2^26 N): t = (x + m N) / 2^32 < 2N, t = x 2^-32 mod N
+                    const uint64_t x = (uint64_t)acc[j];
+                    const uint32_t mq = (uint32_t)x * I.ninv;
+                    uint32_t r = (uint32_t)((x + (uint64_t)mq * n32) >> 32);
+                    cb[j * I.ldc] = (double)(r >= n32 ? r - n32 : r);
+                } else {
+                    cb[j * I.ldc] = (double)reduce_inst(acc[j], I);
+                }
+            }
+        }
+    }
+    return true;
+}
+
+__global__ void __launch_bounds__(G_THREADS, 1)
     k_gemm_grouped(const MMInst *__restrict__ insts, const WorkItem *__restrict__ items, int nitems,
                    const CUtensorMap *__restrict__ tmaps, int *err) {
     extern __shared__ uint8_t dsmem_raw[];
@@ -164,7 +237,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
             gffm_dev::mbar_init(&empty_bar[s], 1);
         }
         gffm_dev::mbar_init(&acc_full_bar, 1);
-        gffm_dev::mbar_init(&acc_empty_bar, NUM_EPI_WARPS);
+        gffm_dev::mbar_init(&acc_empty_bar, G_EPI_WARPS);
         gffm_dev::mbar_init(&drain_bar, 1);
         abort_s = 0;
         gffm_dev::fence_mbar_init();
@@ -289,50 +362,17 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
     } else {
         // ---------------- epilogue ----------------
         const int quad = warp & 3;
-        const int half = (warp - 2) >> 2;
+        const int part = (warp - 2) >> 2;   // which 16 of the tile's 64 columns
+        const uint32_t tq = tmem + ((uint32_t)(quad * 32) << 16) + 16 * part;
         uint32_t acc_phase = 0;
         for (int t = blockIdx.x; t < nitems; t += gridDim.x) {
             const WorkItem it = items[t];
             const MMInst I = insts[it.inst];
-            const int nshift = 2 * I.L - 1;
-            int64_t acc[32];
-#pragma unroll
-            for (int j = 0; j < 32; j++) acc[j] = 0;
-            bool ok = true;
-            int chunk = 0;
-            for (int kb0 = 0; kb0 < I.kblocks; kb0 += I.chunk_kb, chunk++) {
-                if (!gffm_dev::mbar_wait(&acc_full_bar, acc_phase)) {
-                    atomicOr(err, 8);
-                    abort_s = 1;
-                    ok = false;
-                    break;
-                }
-                gffm_dev::tc_fence_after();
-                for (int s = 0; s < nshift; s++) {
-                    uint32_t v[32];
-                    gffm_dev::tmem_ld_32x32b_x32(tmem + ((uint32_t)(quad * 32) << 16) + 64 * s + 32 * half, v);
-                    gffm_dev::tmem_ld_wait();
-                    const int w = I.W[s];
-#pragma unroll
-                    for (int j = 0; j < 32; j++) acc[j] += (int64_t)__float2int_rz(__uint_as_float(v[j])) * w;
-                }
-                gffm_dev::tc_fence_before();
-                __syncwarp();
-                if (lane == 0) gffm_dev::mbar_arrive(&acc_empty_bar);
-                acc_phase ^= 1;
-                if ((chunk & 63) == 63) {
-#pragma unroll
-                    for (int j = 0; j < 32; j++) acc[j] = reduce_inst(acc[j], I);
-                }
-            }
+            const bool ok = I.fast ? grouped_tile<true>(I, it, tq, quad, part, lane, &acc_full_bar, &acc_empty_bar,
+                                                        acc_phase, err, abort_s)
+                                   : grouped_tile<false>(I, it, tq, quad, part, lane, &acc_full_bar, &acc_empty_bar,
+                                                         acc_phase, err, abort_s);
             if (!ok || abort_s) break;
-            const int64_t row = (int64_t)it.tm * BM + quad * 32 + lane;
-            const int64_t col0 = (int64_t)it.tn * BN + half * 32;
-            if (row < I.m) {
-#pragma unroll
-                for (int j = 0; j < 32; j++)
-                    if (col0 + j < I.n) I.C[row + (col0 + j) * I.ldc] = (double)reduce_inst(acc[j], I);
-            }
         }
     }
 
@@ -464,7 +504,7 @@ int build_graph(gffm_batch_plan p, bool overlap) {
         if (p->n_mm > 0 && p->nitems > 0) {
             k_split_batched<<<(unsigned)p->nchunks, 256, 0, s0>>>(p->d_jobs, p->d_chunks);
             fail(cudaGetLastError(), "k_split_batched");
-            k_gemm_grouped<<<p->gemm_grid, NUM_THREADS, G_SMEM_BYTES, s0>>>(p->d_mm, p->d_items, p->nitems, p->d_tmaps,
+            k_gemm_grouped<<<p->gemm_grid, G_THREADS, G_SMEM_BYTES, s0>>>(p->d_mm, p->d_items, p->nitems, p->d_tmaps,
                                                                           gffm::device_error_flag());
             fail(cudaGetLastError(), "k_gemm_grouped");
         }
@@ -554,7 +594,6 @@ int create(const gffm_batch_desc *descs, int64_t count, const gffm_batch_tuning 
         I.chunk_kb = limb::chunk_kblocks(g);
         I.Mpad = (int)g.Mpad;
         I.Npad = (int)g.Npad;
-        I.pad_ = 0;
         I.N = d.N;
         I.minv = ~uint64_t(0) / (uint64_t)d.N;
         I.bias = d.N * (((int64_t(1) << 60) + d.N - 1) / d.N);
@@ -562,6 +601,25 @@ int create(const gffm_batch_desc *descs, int64_t count, const gffm_batch_tuning 
         for (int sft = 0; sft < MAX_SHIFTS; sft++) {
             I.W[sft] = (int32_t)w;
             w = (w * (g.bits == 8 ? 256 : 128)) % d.N;
+        }
+        // the fast epilogue: odd N, one exact chunk, shift sums within 2^22
+        I.fast = 0;
+        I.ninv = 0;
+        I.fbias = 0;
+        if ((d.N & 1) && I.kblocks <= I.chunk_kb &&
+            (int64_t)I.kblocks * BK * g.L * (int64_t(1) << (2 * g.bits - 2)) <= (int64_t(1) << 22)) {
+            uint32_t inv = 1;                         // N^-1 mod 2^32 by Newton's iteration
+            for (int it = 0; it < 5; it++) inv *= 2u - (uint32_t)d.N * inv;
+            I.ninv = 0u - inv;
+            int64_t wsum = 0;
+            for (int sft = 0; sft < MAX_SHIFTS; sft++) {
+                I.Wm[sft] = (int32_t)(((__int128)I.W[sft] << 32) % d.N);
+                if (sft < 2 * g.L - 1) wsum += I.Wm[sft];
+            }
+            I.fbias = d.N * (int64_t(1) << 25) - (int64_t)0x4B400000 * wsum;
+            I.fast = 1;
+        } else {
+            for (int sft = 0; sft < MAX_SHIFTS; sft++) I.Wm[sft] = 0;
         }
         I.C = d.C;
         I.ldc = d.ldc;
