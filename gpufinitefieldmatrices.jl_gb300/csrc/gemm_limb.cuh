@@ -26,12 +26,13 @@
 // sum_s C_s * (2^(7s) mod N) into int64 registers; the final value is reduced
 // mod N with Barrett's method and stored.
 //
-// Warp roles: warp 0 issues TMA loads, warp 1 allocates TMEM and one lane
-// issues the mma's, the other warps are the epilogue -- 8 (two per 32-lane
-// TMEM quadrant, each owning 32 of the 64 output columns), or 16 of 16
-// columns for the read-modify-write epilogue, whose tiles are short (the
-// elimination's K = 128 updates) and whose per-tile chain (drain, reduction,
-// C read and write) then paces the mma's.  Every
+// Warp roles (576 threads): warp 0 issues TMA loads, warp 1 allocates TMEM
+// and one lane issues the mma's, warps 2..17 are the epilogue (four per 32-lane
+// TMEM quadrant, each owning 16 of the 64 output columns).  With one
+// accumulator set the mma's of a tile wait for the drain of the previous one,
+// and for short K (the elimination's K = 128 updates) the epilogue's per-tile
+// chain paces the mma's; twice the epilogue warps of 8 x 32 columns halve
+// both.  Every
 // wait is bounded; on timeout a kernel records the failure in the library's
 // error word and returns without storing.
 #pragma once
@@ -46,10 +47,8 @@ constexpr int BN = 64;             // output columns per tile
 constexpr int BK = 64;             // k per pipeline stage (one 128-byte swizzle row of fp16)
 constexpr int A_TILE = BM * BK * 2;
 constexpr int B_TILE = BN * BK * 2;
-constexpr int NUM_EPI_WARPS = 8;                      // the batched grouped GEMM's epilogue warps
-constexpr int NUM_THREADS = 64 + 32 * NUM_EPI_WARPS;
-// epilogue warps and threads per CTA for an epilogue kind
-__host__ __device__ constexpr int epi_warps(int epi) { return epi == EPI_SUB_I32 || epi == EPI_SUB_I32M ? 16 : 8; }
+// epilogue warps and threads per CTA for an epilogue kind (the same for all)
+__host__ __device__ constexpr int epi_warps(int) { return 16; }
 __host__ __device__ constexpr int gemm_threads(int epi) { return 64 + 32 * epi_warps(epi); }
 constexpr int MAX_SHIFTS = 7;
 constexpr int TILE_GROUP = 16;     // output-tile rows per raster group (L2 reuse)
