@@ -415,7 +415,7 @@ __global__ void __launch_bounds__(PANEL_THREADS, 1) k_panel(PanelArgs a) {
 constexpr int P1_NB = 32;
 constexpr int P1_THREADS = 256;
 constexpr int P1_INV_WARP = 7;
-constexpr int P1_MAX_ROWS = 1536;
+constexpr int P1_MAX_ROWS = 512;
 __host__ __device__ constexpr size_t p1_smem_bytes(int rows) { return (size_t)P1_NB * (size_t)(rows + 4) * 4; }
 
 __global__ void __launch_bounds__(P1_THREADS, 1) k_panel1(PanelArgs a) {

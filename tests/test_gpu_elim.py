@@ -103,7 +103,7 @@ def test_pluq_lookahead_sizes_match_oracle(gffm, case):
     test_pluq_matches_oracle(gffm, case)
 
 
-# More than 1536 rows below the first pivot: the cooperative left-looking panel
+# Well over 512 rows below the first pivot: the cooperative left-looking panel
 # (128 columns over several CTAs) -- zero-column stops inside a panel and at its
 # start, a rank drop mid-panel, ties across CTAs, a narrow last panel.
 MULTI_CTA = [("uniform", 1700, 1700, P26), ("rank200", 1800, 1800, P26), ("zero_cols", 1700, 1750, 13),
