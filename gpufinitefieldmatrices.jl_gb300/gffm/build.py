@@ -2,7 +2,7 @@
 
 Every CUDA translation unit under ``csrc/`` is compiled in parallel and linked
 into ``lib/libgffm.so``.  The library links the CUDA runtime statically, so it
-only needs the driver at run time.
+only needs the NVIDIA driver (libcuda) at run time.
 """
 import concurrent.futures
 import os
