@@ -341,3 +341,21 @@ def test_rref_and_inverse_need_a_prime(gffm):
     with pytest.raises(gffm.CuModMatrixModulusNotPrimeException):
         gffm.inverse(A)
     status_ok(gffm)
+
+
+def test_panel_row_capacity(gffm):
+    """The cooperative panel keeps at most 288 rows per CTA, one CTA per SM: a
+    matrix one row taller fails with GFFM_ERR_UNSUPPORTED before its first panel,
+    and the device stays usable."""
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    rows = min(sms, 160) * 288 + 1
+    A = gffm.CuModMatrix(np.ones((rows, 33), dtype=np.int64), 65521, elem_type=torch.float64)
+    with pytest.raises(gffm.GFFMError) as ei:
+        gffm.pluq_gpu_kernel(A)
+    assert "capacity" in str(ei.value)
+    status_ok(gffm)
+    # one row fewer factors
+    B = gffm.CuModMatrix(np.eye(rows - 1, 33, dtype=np.int64), 65521, elem_type=torch.float64)
+    U, L, rs, cs = gffm.pluq_gpu_kernel(B)
+    assert rs == [] and cs == []
+    status_ok(gffm)
