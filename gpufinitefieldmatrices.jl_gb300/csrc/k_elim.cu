@@ -45,6 +45,8 @@
 #include "limb_host.h"
 
 #include <algorithm>
+#include <cstring>
+#include <unordered_map>
 #include <vector>
 
 namespace elim {
@@ -459,7 +461,7 @@ static int permute_rows2(const Work &w, const PermArgs &perm, int c_left, int c_
 }
 
 static int run_panel(Work &w, int m, int n, int R0, int C0, int nbw, const ModP &M, int lcols_check,
-                     cudaStream_t s, int h_res[2], std::vector<int32_t> &h_prow, std::vector<int32_t> &h_pv,
+                     cudaStream_t s, void *stage, int h_res[2], std::vector<int32_t> &h_prow, std::vector<int32_t> &h_pv,
                      int max_g = 0) {
     using namespace gffm;
     const int rows = m - R0;
@@ -507,10 +509,16 @@ static int run_panel(Work &w, int m, int n, int R0, int C0, int nbw, const ModP 
         void *args[] = {&a};
         GFFM_CUDA(cudaLaunchCooperativeKernel((void *)k_panel, dim3(G), dim3(PANEL_THREADS), args, smem, s));
     }
-    GFFM_CUDA(cudaMemcpyAsync(h_res, w.result, 2 * sizeof(int), cudaMemcpyDeviceToHost, s));
-    GFFM_CUDA(cudaMemcpyAsync(h_prow.data(), w.piv_row, NB * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
-    GFFM_CUDA(cudaMemcpyAsync(h_pv.data(), w.piv_val, NB * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+    // pivot rows, values and the status: consecutive workspace regions, one copy into
+    // pinned memory
+    const char *b0 = reinterpret_cast<const char *>(w.piv_row);
+    const size_t span = (size_t)(reinterpret_cast<const char *>(w.result + 2) - b0);
+    GFFM_CUDA(cudaMemcpyAsync(stage, b0, span, cudaMemcpyDeviceToHost, s));
     GFFM_CUDA(cudaStreamSynchronize(s));
+    const char *sb = static_cast<const char *>(stage);
+    std::memcpy(h_prow.data(), sb, NB * sizeof(int32_t));
+    std::memcpy(h_pv.data(), sb + (reinterpret_cast<const char *>(w.piv_val) - b0), NB * sizeof(int32_t));
+    std::memcpy(h_res, sb + (reinterpret_cast<const char *>(w.result) - b0), 2 * sizeof(int));
     return GFFM_OK;
 }
 
@@ -579,6 +587,18 @@ static int forward(Work &w, int m, int n, int64_t N, int mode, int lcols, cudaSt
     std::vector<int> skipped;  // PLUQ: columns holding a swapped-in column that is never eliminated
     std::vector<int32_t> h_prow(NB), h_pv(NB);
     int h_res[2];
+    // pinned staging for the panel results (pivot rows, values, inverses, status)
+    struct Stage {
+        void *p = nullptr;
+        ~Stage() {
+            if (p) cudaFreeHost(p);
+        }
+    } stage;
+    if ((size_t)(reinterpret_cast<const char *>(w.result + 2) - reinterpret_cast<const char *>(w.piv_row)) > 4096 ||
+        reinterpret_cast<const char *>(w.piv_val) < reinterpret_cast<const char *>(w.piv_row) ||
+        reinterpret_cast<const char *>(w.result) < reinterpret_cast<const char *>(w.piv_val))
+        return set_error(GFFM_ERR_WORKSPACE, "elimination: panel result regions are not consecutive");
+    GFFM_CUDA(cudaMallocHost(&stage.p, 4096));
     int row = 0, col = 0;
     res.perm.resize(m);
     for (int i = 0; i < m; i++) res.perm[i] = i;
@@ -593,7 +613,7 @@ static int forward(Work &w, int m, int n, int64_t N, int mode, int lcols, cudaSt
     while (row < m && col < n) {
         // panels of 32 in one CTA once the rows fit it, of NB across CTAs before
         const int nbw = std::min(m - row <= P1_MAX_ROWS ? P1_NB : NB, n - col);
-        int st = run_panel(w, m, n, row, col, nbw, M, mode == MODE_PLUQ ? lcols : 0, s, h_res, h_prow, h_pv,
+        int st = run_panel(w, m, n, row, col, nbw, M, mode == MODE_PLUQ ? lcols : 0, s, stage.p, h_res, h_prow, h_pv,
                            la.pending ? la.next_g : 0);
         if (st) return st;
         // everything after the panel may touch the columns the side update writes
@@ -617,16 +637,17 @@ static int forward(Work &w, int m, int n, int64_t N, int mode, int lcols, cudaSt
             // the panel's row swaps composed into one permutation of the rows involved
             PermArgs perm;
             {
+                // rows row .. row+t-1 sit at positions 0 .. t-1; the (at most t) rows
+                // below them that a swap touches follow, found through a small map
                 std::vector<int32_t> rows_inv;
+                std::unordered_map<int32_t, int> extra;
                 for (int q = 0; q < t; q++) rows_inv.push_back(row + q);
                 for (int q = 0; q < t; q++)
-                    if (h_prow[q] >= row + t && std::find(rows_inv.begin(), rows_inv.end(), h_prow[q]) == rows_inv.end())
+                    if (h_prow[q] >= row + t && extra.emplace(h_prow[q], (int)rows_inv.size()).second)
                         rows_inv.push_back(h_prow[q]);
                 std::vector<int32_t> content(rows_inv.size());
                 for (size_t k = 0; k < rows_inv.size(); k++) content[k] = (int32_t)k;
-                auto pos = [&](int32_t rr) {
-                    return (int)(std::find(rows_inv.begin(), rows_inv.end(), rr) - rows_inv.begin());
-                };
+                auto pos = [&](int32_t rr) { return rr < row + t ? (int)(rr - row) : extra.at(rr); };
                 for (int q = 0; q < t; q++) std::swap(content[pos(row + q)], content[pos(h_prow[q])]);
                 perm.K = (int)rows_inv.size();
                 for (int k = 0; k < perm.K; k++) {
