@@ -587,18 +587,20 @@ static int forward(Work &w, int m, int n, int64_t N, int mode, int lcols, cudaSt
     std::vector<int> skipped;  // PLUQ: columns holding a swapped-in column that is never eliminated
     std::vector<int32_t> h_prow(NB), h_pv(NB);
     int h_res[2];
-    // pinned staging for the panel results (pivot rows, values, inverses, status)
+    // pinned staging for the panel results (pivot rows, values, inverses, status),
+    // allocated once per host thread
     struct Stage {
         void *p = nullptr;
         ~Stage() {
             if (p) cudaFreeHost(p);
         }
-    } stage;
+    };
+    static thread_local Stage stage;
     if ((size_t)(reinterpret_cast<const char *>(w.result + 2) - reinterpret_cast<const char *>(w.piv_row)) > 4096 ||
         reinterpret_cast<const char *>(w.piv_val) < reinterpret_cast<const char *>(w.piv_row) ||
         reinterpret_cast<const char *>(w.result) < reinterpret_cast<const char *>(w.piv_val))
         return set_error(GFFM_ERR_WORKSPACE, "elimination: panel result regions are not consecutive");
-    GFFM_CUDA(cudaMallocHost(&stage.p, 4096));
+    if (!stage.p) GFFM_CUDA(cudaMallocHost(&stage.p, 4096));
     int row = 0, col = 0;
     res.perm.resize(m);
     for (int i = 0; i < m; i++) res.perm[i] = i;
