@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 #include <cuda.h>
 #include <cuda_fp16.h>
+#include <atomic>
 #include <cstdint>
 #include <cstdio>
 #include <cstdarg>
@@ -43,6 +44,26 @@ struct Scratch {
 };
 
 static inline int64_t round_up(int64_t x, int64_t m) { return (x + m - 1) / m * m; }
+
+// cudaFuncSetAttribute(KERN, MaxDynamicSharedMemorySize, bytes) once per kernel and
+// device for the largest size asked so far (the call costs microseconds of host
+// time, and small factorizations launch a kernel or two per pivot block).
+template <auto KERN>
+cudaError_t ensure_dynamic_smem(int bytes) {
+    static std::atomic<int> set[64];
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= 64) return cudaFuncSetAttribute(KERN, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (set[dev].load(std::memory_order_relaxed) >= bytes) return cudaSuccess;
+    e = cudaFuncSetAttribute(KERN, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (e == cudaSuccess) {
+        int cur = set[dev].load(std::memory_order_relaxed);
+        while (cur < bytes && !set[dev].compare_exchange_weak(cur, bytes, std::memory_order_relaxed)) {
+        }
+    }
+    return e;
+}
 
 }  // namespace gffm
 

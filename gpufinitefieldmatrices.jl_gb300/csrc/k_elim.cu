@@ -501,11 +501,11 @@ static int run_panel(Work &w, int m, int n, int R0, int C0, int nbw, const ModP 
     a.result = w.result;
     a.err = device_error_flag();
     if (one) {
-        GFFM_CUDA(cudaFuncSetAttribute(k_panel1, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        GFFM_CUDA(ensure_dynamic_smem<k_panel1>((int)smem));
         k_panel1<<<1, P1_THREADS, smem, s>>>(a);
         GFFM_LAUNCH_CHECK("k_panel1");
     } else {
-        GFFM_CUDA(cudaFuncSetAttribute(k_panel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        GFFM_CUDA(ensure_dynamic_smem<k_panel>((int)smem));
         void *args[] = {&a};
         GFFM_CUDA(cudaLaunchCooperativeKernel((void *)k_panel, dim3(G), dim3(PANEL_THREADS), args, smem, s));
     }
@@ -569,6 +569,11 @@ static int update_lookahead(Work &w, int64_t N, int row, int t, int col, int cs,
     if (st) return st;
     st = limb::gemm_digits(ga, w.dA2, w.dB, look, rows_b, t, N, C, w.ldw, limb::EPI_SUB_I32, 0, la.s);
     if (st) return st;
+    if (!la.s2) {
+        GFFM_CUDA(cudaStreamCreateWithFlags(&la.s2, cudaStreamNonBlocking));
+        GFFM_CUDA(cudaEventCreateWithFlags(&la.ea, cudaEventDisableTiming));
+        GFFM_CUDA(cudaEventCreateWithFlags(&la.eb, cudaEventDisableTiming));
+    }
     GFFM_CUDA(cudaEventRecord(la.ea, la.s));
     GFFM_CUDA(cudaStreamWaitEvent(la.s2, la.ea, 0));
     la.next_g = rows_b <= P1_MAX_ROWS ? 1 : look_ctas(rows_b);   // the next panel's CTAs
@@ -604,14 +609,9 @@ static int forward(Work &w, int m, int n, int64_t N, int mode, int lcols, cudaSt
     int row = 0, col = 0;
     res.perm.resize(m);
     for (int i = 0; i < m; i++) res.perm[i] = i;
-    Lookahead la;
+    Lookahead la;   // its stream and events are created on first use
     la.s = s;
     const bool use_look = !w.plain;
-    if (use_look) {
-        GFFM_CUDA(cudaStreamCreateWithFlags(&la.s2, cudaStreamNonBlocking));
-        GFFM_CUDA(cudaEventCreateWithFlags(&la.ea, cudaEventDisableTiming));
-        GFFM_CUDA(cudaEventCreateWithFlags(&la.eb, cudaEventDisableTiming));
-    }
     while (row < m && col < n) {
         // panels of 32 in one CTA once the rows fit it, of NB across CTAs before
         const int nbw = std::min(m - row <= P1_MAX_ROWS ? P1_NB : NB, n - col);

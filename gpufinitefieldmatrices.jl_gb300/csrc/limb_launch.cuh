@@ -11,7 +11,7 @@ template <int L, int EPI, int BNV>
 static int launch_gemm_L(const CUtensorMap &ta, const CUtensorMap &tb, const Params &p, int grid, cudaStream_t s) {
     auto kern = k_gemm_limb<L, EPI, BNV>;
     constexpr int smem = Cfg<L, BNV>::SMEM_BYTES;
-    GFFM_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    GFFM_CUDA((gffm::ensure_dynamic_smem<k_gemm_limb<L, EPI, BNV>>(smem)));
     gffm::profile_hook().before(s);
     kern<<<grid, gemm_threads(EPI), smem, s>>>(ta, tb, p);
     gffm::profile_hook().after(s);
