@@ -13,11 +13,11 @@ constexpr int PANEL_WARPS = PANEL_THREADS / 32;
 constexpr int MAX_PANEL_CTAS = 160;
 constexpr int MAX_PERM_ROWS = 2 * NB;
 constexpr int PANEL_MAX_R = 288;    // rows per CTA: threads 0..287 own one row each
-constexpr int PANEL_AUX0 = PANEL_MAX_R;              // threads 288..511: publication, polling
+constexpr int PANEL_AUX0 = PANEL_MAX_R;              // threads 288..511: publication, polling, Linv rows
 constexpr int PANEL_NAUX = PANEL_THREADS - PANEL_AUX0;
 constexpr int LU_LD = NB + 1;
 // Dynamic shared memory of k_panel: the CTA's rows (NB columns x (R + 1) words,
-// column-major) and the Linv / pivot-row square (NB x LU_LD words).
+// column-major) and the square of the panel's U rows and Linv (NB x LU_LD words).
 __host__ __device__ constexpr size_t panel_smem_bytes(int R) {
     return ((size_t)NB * (size_t)(R + 1) + (size_t)NB * LU_LD) * 4;
 }
