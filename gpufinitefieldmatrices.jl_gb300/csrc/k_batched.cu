@@ -60,49 +60,6 @@ constexpr int G_TMEM_COLS = 512;
 // ---------------------------------------------------------------------------
 // digit split of every product operand
 // ---------------------------------------------------------------------------
-template <int L>
-__device__ __forceinline__ void split_a_tile(const SplitJob &J, int64_t local, int32_t (*tile)[33]) {
-    const int kt = J.kpad / 32;
-    const int64_t r0 = (local / kt) * 32, k0 = (local % kt) * 32;
-    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
-    const ModN M{J.N, J.minv};
-#pragma unroll
-    for (int i = 0; i < 4; i++) {
-        const int64_t kk = k0 + ty + 8 * i, r = r0 + tx;
-        tile[ty + 8 * i][tx] = (r < J.rows && kk < J.cols) ? split_value<SPLIT_CENTRED>(J.src[r + kk * J.ld], 0.0, M) : 0;
-    }
-    __syncthreads();
-    const size_t plane = (size_t)J.prow * J.kpad;
-#pragma unroll
-    for (int i = 0; i < 4; i++) {
-        const int64_t r = r0 + ty + 8 * i, kk = k0 + tx;
-        __half d[L];
-        digits<L>(tile[tx][ty + 8 * i], d, J.bits);
-#pragma unroll
-        for (int l = 0; l < L; l++) J.dst[l * plane + (size_t)r * J.kpad + kk] = d[l];
-    }
-}
-
-template <int L>
-__device__ __forceinline__ void split_b_pairs(const SplitJob &J, int64_t local) {
-    const int64_t idx = local * 256 + threadIdx.x;
-    const int64_t ppc = J.kpad / 2;
-    if (idx >= ppc * J.prow) return;
-    const int64_t c = idx / ppc;
-    const int64_t kk = (idx - c * ppc) * 2;
-    const ModN M{J.N, J.minv};
-    const int k = J.rows, n = J.cols;
-    const int32_t v0 = (c < n && kk < k) ? split_value<SPLIT_CENTRED>(J.src[kk + c * J.ld], 0.0, M) : 0;
-    const int32_t v1 = (c < n && kk + 1 < k) ? split_value<SPLIT_CENTRED>(J.src[kk + 1 + c * J.ld], 0.0, M) : 0;
-    __half d0[L], d1[L];
-    digits<L>(v0, d0, J.bits);
-    digits<L>(v1, d1, J.bits);
-    const size_t plane = (size_t)J.prow * J.kpad;
-#pragma unroll
-    for (int l = 0; l < L; l++)
-        *reinterpret_cast<__half2 *>(J.dst + l * plane + (size_t)c * J.kpad + kk) = __halves2half2(d0[l], d1[l]);
-}
-
 // A block takes one chunk: up to SPLIT_CHUNK consecutive work units (32 x 32 tiles
 // of A, or 256 digit pairs of B) of one operand, found with a single table load.
 constexpr int SPLIT_CHUNK = 8;
@@ -111,28 +68,111 @@ struct SplitChunk {
     int job, local0, count, pad_;
 };
 
+// A operand: 32 x 32 tiles transposed through shared memory.  The next unit's
+// values are loaded before the current one is converted and stored, so a
+// thread keeps loads in flight across the units of its chunk.
+template <int L>
+__device__ __forceinline__ void split_a_chunk(const SplitJob &J, const SplitChunk &ch, int32_t (*tile)[33]) {
+    const int kt = J.kpad / 32;
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    const ModN M{J.N, J.minv};
+    const size_t plane = (size_t)J.prow * J.kpad;
+    double cur[4], nxt[4];
+    bool okc[4], okn[4];
+    auto load = [&](int64_t local, double (&v)[4], bool (&ok)[4]) {
+        const int64_t r0 = (local / kt) * 32, k0 = (local % kt) * 32;
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            const int64_t kk = k0 + ty + 8 * i, r = r0 + tx;
+            ok[i] = r < J.rows && kk < J.cols;
+            v[i] = ok[i] ? J.src[r + kk * J.ld] : 0.0;
+        }
+    };
+    load(ch.local0, cur, okc);
+    for (int u = 0; u < ch.count; u++) {
+        const int64_t local = (int64_t)ch.local0 + u;
+        if (u + 1 < ch.count) load(local + 1, nxt, okn);
+        const int64_t r0 = (local / kt) * 32, k0 = (local % kt) * 32;
+#pragma unroll
+        for (int i = 0; i < 4; i++) tile[ty + 8 * i][tx] = okc[i] ? split_value<SPLIT_CENTRED>(cur[i], 0.0, M) : 0;
+        __syncthreads();
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            const int64_t r = r0 + ty + 8 * i, kk = k0 + tx;
+            __half d[L];
+            digits<L>(tile[tx][ty + 8 * i], d, J.bits);
+#pragma unroll
+            for (int l = 0; l < L; l++) J.dst[l * plane + (size_t)r * J.kpad + kk] = d[l];
+        }
+        __syncthreads();   // the tile is reused by the next unit
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            cur[i] = nxt[i];
+            okc[i] = okn[i];
+        }
+    }
+}
+
+// B operand: 256 digit pairs per unit, the next unit's pair loaded ahead.
+template <int L>
+__device__ __forceinline__ void split_b_chunk(const SplitJob &J, const SplitChunk &ch) {
+    const int64_t ppc = J.kpad / 2;
+    const int64_t total = ppc * J.prow;
+    const ModN M{J.N, J.minv};
+    const int k = J.rows, n = J.cols;
+    const size_t plane = (size_t)J.prow * J.kpad;
+    double c0 = 0.0, c1 = 0.0, n0 = 0.0, n1 = 0.0;
+    bool k0c = false, k1c = false, k0n = false, k1n = false;
+    auto load = [&](int64_t local, double &v0, double &v1, bool &ok0, bool &ok1) {
+        const int64_t idx = local * 256 + threadIdx.x;
+        const int64_t c = idx / ppc;
+        const int64_t kk = (idx - c * ppc) * 2;
+        ok0 = idx < total && c < n && kk < k;
+        ok1 = idx < total && c < n && kk + 1 < k;
+        v0 = ok0 ? J.src[kk + c * J.ld] : 0.0;
+        v1 = ok1 ? J.src[kk + 1 + c * J.ld] : 0.0;
+    };
+    load(ch.local0, c0, c1, k0c, k1c);
+    for (int u = 0; u < ch.count; u++) {
+        const int64_t local = (int64_t)ch.local0 + u;
+        const int64_t idx = local * 256 + threadIdx.x;
+        if (idx >= total) return;
+        if (u + 1 < ch.count) load(local + 1, n0, n1, k0n, k1n);
+        const int64_t c = idx / ppc;
+        const int64_t kk = (idx - c * ppc) * 2;
+        const int32_t v0 = k0c ? split_value<SPLIT_CENTRED>(c0, 0.0, M) : 0;
+        const int32_t v1 = k1c ? split_value<SPLIT_CENTRED>(c1, 0.0, M) : 0;
+        __half d0[L], d1[L];
+        digits<L>(v0, d0, J.bits);
+        digits<L>(v1, d1, J.bits);
+#pragma unroll
+        for (int l = 0; l < L; l++)
+            *reinterpret_cast<__half2 *>(J.dst + l * plane + (size_t)c * J.kpad + kk) = __halves2half2(d0[l], d1[l]);
+        c0 = n0;
+        c1 = n1;
+        k0c = k0n;
+        k1c = k1n;
+    }
+}
+
 __global__ void __launch_bounds__(256) k_split_batched(const SplitJob *__restrict__ jobs,
                                                        const SplitChunk *__restrict__ chunks) {
     __shared__ int32_t tile[32][33];
     const SplitChunk ch = chunks[blockIdx.x];
     const SplitJob J = jobs[ch.job];
-    for (int u = 0; u < ch.count; u++) {
-        const int64_t local = (int64_t)ch.local0 + u;
-        if (J.is_b) {
-            switch (J.L) {
-                case 1: split_b_pairs<1>(J, local); break;
-                case 2: split_b_pairs<2>(J, local); break;
-                case 3: split_b_pairs<3>(J, local); break;
-                default: split_b_pairs<4>(J, local); break;
-            }
-        } else {
-            switch (J.L) {
-                case 1: split_a_tile<1>(J, local, tile); break;
-                case 2: split_a_tile<2>(J, local, tile); break;
-                case 3: split_a_tile<3>(J, local, tile); break;
-                default: split_a_tile<4>(J, local, tile); break;
-            }
-            __syncthreads();   // the tile is reused by the next unit
+    if (J.is_b) {
+        switch (J.L) {
+            case 1: split_b_chunk<1>(J, ch); break;
+            case 2: split_b_chunk<2>(J, ch); break;
+            case 3: split_b_chunk<3>(J, ch); break;
+            default: split_b_chunk<4>(J, ch); break;
+        }
+    } else {
+        switch (J.L) {
+            case 1: split_a_chunk<1>(J, ch, tile); break;
+            case 2: split_a_chunk<2>(J, ch, tile); break;
+            case 3: split_a_chunk<3>(J, ch, tile); break;
+            default: split_a_chunk<4>(J, ch, tile); break;
         }
     }
 }
