@@ -11,7 +11,9 @@ Printed JSON line (one, from rank 0):
   e2e          the same metric through the C ABI with host buffers: every step
                copies A and B from pinned host memory and C back
   roofline     the tcgen05 GEMM kernel's tensor FLOP/s (digit products) vs the
-               measured dense bf16/fp16 peak; traffic from the committed ncu summary
+               measured dense bf16/fp16 peak; traffic from an ncu capture (its
+               source is named in the line: no run reads DRAM counters itself)
+  config1_512  the 512 x 512 mod 65521 product on both paths, in microseconds
   plain_fp64   the plain path (the reference's Float64 method) on the same GPU
   pluq         PLUQ timings when the elimination is built (see --pluq)
   cpu_baseline the oracle (exact C restatement) on the host cores, bounded sample
@@ -22,7 +24,6 @@ import argparse
 import ctypes
 import json
 import os
-import re
 import statistics
 import subprocess
 import sys
@@ -124,15 +125,12 @@ def measured_peaks():
         return 1900.0, 6800.0, "fallback"
 
 
-def profiled_traffic():
-    """dram bytes per launch of the limb GEMM kernel, from the committed ncu summary."""
-    path = os.path.join(ROOT, "profiles", "limb_gemm_8192_mod_p26.md")
-    try:
-        txt = open(path).read()
-    except OSError:
-        return None
-    m = re.search(r"dram_bytes_per_launch:\s*([0-9.eE+]+)", txt)
-    return float(m.group(1)) if m else None
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per launch of the headline
+# GEMM kernel, from an ncu capture of the same kernel (one pass, -c 1,
+# --clock-control none); a benchmark run cannot read DRAM counters itself, so the
+# figure is reported with its source and is not measured in the run.
+GEMM_TRAFFIC = {"bytes": 1.1336e10, "source": "ncu dram__bytes_{read,write}.sum of a 4096^3 capture, scaled x8 "
+                                              "to 8192^3 (not measured in this run)"}
 
 
 # ---------------------------------------------------------------------------
@@ -297,7 +295,8 @@ def run_ours(args):
     achieved = tflop / (kavg / 1e3)
     roofline = {"bound": "tensor", "kernel": "limb::k_gemm_limb<4, EPI_STORE_F64>", "achieved": round(achieved, 1),
                 "peak": peak, "unit": "TFLOP/s", "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
-                "traffic": profiled_traffic(), "kernel_ms": round(kavg, 4),
+                "traffic": GEMM_TRAFFIC["bytes"], "traffic_source": GEMM_TRAFFIC["source"],
+                "kernel_ms": round(kavg, 4),
                 "algorithmic": "16 fp16 digit-pair products per modular MAC: 2*16*8192^3 FLOP per launch"}
 
     out = {
@@ -318,6 +317,7 @@ def run_ours(args):
     if not args.no_plain:
         out["plain_fp64"] = plain_run(L, sp, dev)
         out["plain_fp64"]["limb_speedup"] = round(value / world / out["plain_fp64"]["value"], 1)
+    out["config1_512"] = config1_run(L, sp, dev)
     if args.pluq != 0:
         out["pluq"] = pluq_run(args, L, sp, dev)
     if not args.no_karatsuba:
@@ -464,7 +464,12 @@ def pluq_run(args, L, sp, dev):
     import gffm
     import oracle
     from gffm import elimination
-    out = {"limb": elimination.bench_pluq(args.pluq, sp, dev, reps=2)}
+    out = {}
+    out["limb"], fact = elimination.bench_pluq(args.pluq, sp, dev, reps=2, outputs=True)
+    # the factorization just timed, checked outside the timed runs
+    out["check"] = check_pluq(*fact)
+    out["check_ok"] = all(out["check"].values())
+    del fact
     if not args.no_pluq_plain and args.only != "pluq":
         out["plain"] = elimination.bench_pluq(args.pluq, sp, dev, reps=1, method="plain", warmup=0)
         out["limb_speedup"] = round(out["plain"]["seconds"] / out["limb"]["seconds"], 1)
@@ -505,6 +510,70 @@ def pluq_run(args, L, sp, dev):
         gffm.inverse(B)
         torch.cuda.synchronize()
         out["inverse_%d_ms" % n] = round((time.perf_counter() - t0) * 1e3, 2)
+    return out
+
+
+def dev_int64(M):
+    """The true-size contents of a CuModArray as an int64 (rows x cols) Fortran-ordered host array."""
+    import torch
+    r, c = M.size
+    return M.data[:c, :r].to(torch.int64).cpu().numpy().T
+
+
+def check_pluq(A, U, L, rs, cs, width=256):
+    """Exact host checks of a full-rank factorization P A = L U mod p26: Freivalds on two
+    vectors, U unit upper / L lower with pivots on the diagonal (sampled rows), no column
+    swaps, and the first `width` pivot steps equal to the oracle's factorization of the
+    leading column block."""
+    import numpy as np
+    from oracle import checks
+    n = A.size[0]
+    Ah, Uh, Lh = dev_int64(A), dev_int64(U), dev_int64(L)
+    rng = np.random.default_rng(16384)
+    rows = rng.integers(0, n, size=64)
+    out = {"no_col_swaps": cs == [],
+           "freivalds_LU_eq_PA": checks.freivalds_pluq(Ah, Uh, Lh, rs, P26, rng),
+           "unit_upper_U": bool((np.diag(Uh) == 1).all()) and all((Uh[i, :i] == 0).all() for i in rows),
+           "lower_L": bool((np.diag(Lh) != 0).all()) and all((Lh[i, i + 1:] == 0).all() for i in rows)}
+    w = min(width, n)
+    blk = checks.pluq_leading_block(Ah[:, :w], Uh[:w, :w], Lh[:, :w], rs, P26)
+    out.update({"first_%d_steps_%s" % (w, k): v for k, v in blk.items()})
+    return out
+
+
+def config1_run(L, sp, dev):
+    """The reference's single-stripe product at its own size: 512 x 512 mod 65521, Float64
+    CuModMatrix operands, on both paths; microseconds per product, exact against the oracle."""
+    import numpy as np
+    import torch
+    import gffm
+    import oracle
+    n, p = 512, 65521
+    rng = np.random.default_rng(512)
+    Ah = rng.integers(0, p, size=(n, n))
+    Bh = rng.integers(0, p, size=(n, n))
+    A = gffm.CuModMatrix(Ah, p, elem_type=torch.float64)
+    B = gffm.CuModMatrix(Bh, p, elem_type=torch.float64)
+    want = oracle.matmul(Ah, Bh, p)
+    out = {"size": n, "modulus": p, "ops": 2 * n ** 3}
+    for method in ("limb", "plain"):
+        C = gffm.zeros(torch.float64, n, n, p)
+        fn = lambda: gffm.mat_mul_type_inplace_(C, A, B, method=method)
+        for _ in range(5):
+            fn()
+        torch.cuda.synchronize()
+        reps = 200
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        us = e0.elapsed_time(e1) * 1e3 / reps
+        out[method + "_us"] = round(us, 2)
+        out[method + "_gops"] = round(2 * n ** 3 / us / 1e3, 1)
+        out[method + "_exact"] = bool(np.array_equal(dev_int64(C), want))
     return out
 
 
@@ -563,6 +632,32 @@ def karatsuba_run(L, sp, dev):
             "schoolbook4_ms": round(ts, 3), "karatsuba_speedup_vs_schoolbook": round(ts / tp, 2)}
 
 
+def check_batch(specs, inst, results):
+    """Freivalds (exact, on the host) for every product C = A B and every PLUQ L U = P A of
+    a batch; PLUQs must be full rank (no column swaps, unit diagonal of U)."""
+    import numpy as np
+    from oracle import checks
+    rng = np.random.default_rng(4096)
+    failed, products, pluqs = [], 0, 0
+    for i, ((op, n, p), spec, got) in enumerate(zip(specs, inst, results)):
+        if op == "matmul":
+            products += 1
+            ok = checks.freivalds_product(dev_int64(spec[1]), dev_int64(spec[2]), dev_int64(got), p, rng)
+        else:
+            pluqs += 1
+            if not isinstance(got, tuple):
+                ok = False
+            else:
+                U, L, rs, cs = got
+                Uh = dev_int64(U)
+                ok = (cs == [] and bool((np.diag(Uh) == 1).all())
+                      and checks.freivalds_pluq(dev_int64(spec[1]), Uh, dev_int64(L), rs, p, rng))
+        if not ok:
+            failed.append(i)
+    return {"products_checked": products, "pluqs_checked": pluqs, "failed": len(failed),
+            "first_failed": failed[:8], "method": "Freivalds, 2 vectors per instance, exact mod p on the host"}
+
+
 def batched_run(args, dev, large_gemm_gops):
     """The batched uneven-instance workload: 4096 instances, n uniform over the multiples
     of 32 in [32, 512], p over the 32 fixed primes, half products half PLUQs, one graph."""
@@ -596,6 +691,9 @@ def batched_run(args, dev, large_gemm_gops):
     out = {"instances": len(specs), "ops": ops, "ms": round(ms, 3), "gops": round(ops / ms / 1e6, 1),
            "frac_of_large_gemm": round(ops / ms / 1e6 / large_gemm_gops, 3), "plan": plan.info(),
            "pluq_full_rank": "%d/%d" % (full_rank, len(info))}
+    # every instance of the batch just timed, checked outside the timed runs
+    out["check"] = check_batch(specs, inst, plan.results())
+    out["check_ok"] = out["check"]["failed"] == 0
     if args.only == "batched":
         return out
     best = (ms, None)

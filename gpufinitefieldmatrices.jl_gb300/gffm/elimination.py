@@ -201,10 +201,11 @@ def perm_array_to_matrix(perm, N, new_size, perm_stack=False, elem_type=torch.fl
 
 
 # -- benchmark helper used by bench.py -----------------------------------------
-def bench_pluq(size, stream_ptr, dev, reps=2, method="limb", warmup=1):
+def bench_pluq(size, stream_ptr, dev, reps=2, method="limb", warmup=1, outputs=False):
     """Time pluq on a full-rank size x size matrix mod 67108859 (seeded uniform residues)
     through the C ABI; returns a dict for the benchmark line.  method "plain" times the
-    plain Float64 trailing products."""
+    plain Float64 trailing products.  With outputs=True also returns the last run's
+    (A, U, L, Perm_rows, Perm_cols) for checking."""
     import time
     p = 67108859
     if size is None or size < 0:
@@ -240,5 +241,10 @@ def bench_pluq(size, stream_ptr, dev, reps=2, method="limb", warmup=1):
         times.append(time.perf_counter() - t0)
     best = min(times)
     ops = 2.0 / 3.0 * size ** 3
-    return {"size": size, "modulus": p, "method": method, "seconds": round(best, 4), "rank": rk.value,
-            "gops": round(ops / best / 1e9, 1), "ops": "2/3 n^3 modular multiply-adds"}
+    out = {"size": size, "modulus": p, "method": method, "seconds": round(best, 4), "rank": rk.value,
+           "gops": round(ops / best / 1e9, 1), "ops": "2/3 n^3 modular multiply-adds"}
+    if not outputs:
+        return out
+    Prows = [tuple(int(v) for v in rs[i]) for i in range(nr.value)]
+    Pcols = [tuple(int(v) for v in cs[i]) for i in range(nc.value)]
+    return out, (A, U, L, Prows, Pcols)
