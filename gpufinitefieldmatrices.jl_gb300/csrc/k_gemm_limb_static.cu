@@ -19,6 +19,7 @@
 #include "gffm_common.cuh"
 #include "limb_host.h"
 
+#include <cudaTypedefs.h>
 #include <mutex>
 
 namespace {
@@ -27,24 +28,62 @@ constexpr size_t kLimbStaticScratchBytes = size_t(32) << 20;
 
 static __device__ __align__(256) uint8_t g_limb_static_scratch[kLimbStaticScratchBytes];
 
-// Device address of the array, looked up once per device with that device
-// current (in host code the array's name is only a host-side stand-in).
+// Device address of the array, looked up with the device current (in host code
+// the array's name is only a host-side stand-in) once per device and context:
+// the address belongs to the context that loaded the module, so after
+// cudaDeviceReset (a new primary context) it is looked up again.  Contexts are
+// told apart by the driver's process-unique context ID.
 constexpr int kMaxDev = 64;
-void *g_scratch_addr[kMaxDev];
+struct ScratchAddr {
+    unsigned long long ctx_id = 0;
+    void *addr = nullptr;
+};
+ScratchAddr g_scratch_addr[kMaxDev];
 std::mutex g_scratch_mu;
+
+PFN_cuCtxGetCurrent_v4000 g_ctx_current = nullptr;
+PFN_cuCtxGetId_v12000 g_ctx_id = nullptr;
+std::once_flag g_ctx_once;
+
+// the process-unique ID of the current context, or 0 when none is current (or it was destroyed)
+unsigned long long current_context_id() {
+    std::call_once(g_ctx_once, [] {
+        void *fn = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &fn, 4000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            g_ctx_current = reinterpret_cast<PFN_cuCtxGetCurrent_v4000>(fn);
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &fn, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            g_ctx_id = reinterpret_cast<PFN_cuCtxGetId_v12000>(fn);
+    });
+    CUcontext ctx = nullptr;
+    unsigned long long id = 0;
+    if (!g_ctx_current || !g_ctx_id || g_ctx_current(&ctx) != CUDA_SUCCESS || !ctx ||
+        g_ctx_id(ctx, &id) != CUDA_SUCCESS)
+        return 0;
+    return id;
+}
 
 int scratch_address(void **out) {
     int dev = 0;
     GFFM_CUDA(cudaGetDevice(&dev));
     if (dev < 0 || dev >= kMaxDev) return gffm::set_error(GFFM_ERR_UNSUPPORTED, "device ordinal %d out of range", dev);
     std::lock_guard<std::mutex> lk(g_scratch_mu);
-    if (!g_scratch_addr[dev]) {
-        void *p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&p, g_limb_static_scratch);
-        if (e != cudaSuccess) return gffm::cuda_error(e, "cudaGetSymbolAddress(limb static scratch)");
-        g_scratch_addr[dev] = p;
+    ScratchAddr &a = g_scratch_addr[dev];
+    const unsigned long long id = current_context_id();
+    if (a.addr && id != 0 && id == a.ctx_id) {
+        *out = a.addr;
+        return GFFM_OK;
     }
-    *out = g_scratch_addr[dev];
+    // first call on this device, or a new context: look the address up (this also makes
+    // the device's primary context current), then remember which context it belongs to
+    void *p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_limb_static_scratch);
+    if (e != cudaSuccess) return gffm::cuda_error(e, "cudaGetSymbolAddress(limb static scratch)");
+    a.addr = p;
+    a.ctx_id = current_context_id();
+    *out = p;
     return GFFM_OK;
 }
 
@@ -55,6 +94,16 @@ extern "C" {
 int gffm_matmul_limb_static_max_bytes(size_t *bytes) {
     if (!bytes) return gffm::set_error(GFFM_ERR_ARG, "bytes is NULL");
     *bytes = kLimbStaticScratchBytes;
+    return GFFM_OK;
+}
+
+int gffm_matmul_limb_static_scratch_size(int64_t m, int64_t n, int64_t k, int64_t N, size_t *bytes) {
+    if (!bytes) return gffm::set_error(GFFM_ERR_ARG, "bytes is NULL");
+    int st = limb::check_args(m, n, k, m > 1 ? m : 1, k > 1 ? k : 1, m > 1 ? m : 1, N);
+    if (st) return st;
+    // the static path always uses the untuned layout: 7-bit schoolbook digits, 128 x 64 tiles
+    const limb::Layout g = limb::layout(m, n, k, N);
+    *bytes = (m == 0 || n == 0 || k == 0) ? 0 : g.a_bytes + g.b_bytes;
     return GFFM_OK;
 }
 

@@ -46,6 +46,7 @@ SIGNATURES = {
     "gffm_apply_col_swaps_f64": (_INT, [_P, _I64, _I64, _I64, _P, _I64, _INT, _P]),
     "gffm_apply_col_swaps_f32": (_INT, [_P, _I64, _I64, _I64, _P, _I64, _INT, _P]),
     "gffm_matmul_limb_static_max_bytes": (_INT, [_PSZ]),
+    "gffm_matmul_limb_static_scratch_size": (_INT, [_I64, _I64, _I64, _I64, _PSZ]),
     "gffm_matmul_limb_static_f64": (_INT, [_I64, _I64, _I64, _P, _I64, _P, _I64, _P, _I64, _I64, _P]),
     "gffm_matmul_host_workspace_size": (_INT, [_I64, _I64, _I64, _I64, _PSZ]),
     "gffm_div_scalar_f64": (_INT, [_P, _P, _I64, _I64, _I64, _P]),

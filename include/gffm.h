@@ -392,14 +392,19 @@ GFFM_API int gffm_batched_plan_destroy(gffm_batch_plan plan);
  * outputs only; its digit-plane scratch is a fixed array of
  * gffm_matmul_limb_static_max_bytes() bytes (32 MiB) that the library keeps
  * on every GPU that loads it until the process exits.  It calls no
- * allocator.  A product whose digit planes need more scratch than that
- * (gffm_matmul_limb_workspace_size) is rejected with GFFM_ERR_WORKSPACE.
- * The first call on a device looks up the array's device address; make that
- * first call before any stream capture on that device.  All calls share the
- * array: calls that run concurrently on the GPU (e.g. on two streams) race on
- * it, calls on one stream are safe.  Every call rewrites the scratch it uses,
- * so nothing in it needs to start at zero. */
+ * allocator.  It always forms the products the untuned way (7-bit schoolbook
+ * digits, whatever the tune table says), so its scratch need is
+ * gffm_matmul_limb_static_scratch_size, which can differ from
+ * gffm_matmul_limb_workspace_size; a product needing more than the array
+ * holds is rejected with GFFM_ERR_WORKSPACE.  The results equal
+ * gffm_matmul_limb_f64's bit for bit.  The first call on a device (and the
+ * first after cudaDeviceReset, which replaces the device's context) looks up
+ * the array's device address; make that call before any stream capture on
+ * that device.  All calls share the array: calls that run concurrently on the
+ * GPU (e.g. on two streams) race on it, calls on one stream are safe.  Every
+ * call rewrites the scratch it uses, so nothing in it needs to start at zero. */
 GFFM_API int gffm_matmul_limb_static_max_bytes(size_t *bytes);
+GFFM_API int gffm_matmul_limb_static_scratch_size(int64_t m, int64_t n, int64_t k, int64_t N, size_t *bytes);
 GFFM_API int gffm_matmul_limb_static_f64(int64_t m, int64_t n, int64_t k, const double *A, int64_t lda,
                                          const double *B, int64_t ldb, double *C, int64_t ldc, int64_t N,
                                          gffm_stream_t stream);

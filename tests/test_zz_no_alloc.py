@@ -68,7 +68,13 @@ def test_no_alloc_rejects_products_beyond_its_scratch(gffm):
     cap = ctypes.c_size_t(0)
     assert L.gffm_matmul_limb_static_max_bytes(ctypes.byref(cap)) == 0
     assert cap.value == 32 << 20
+    # its scratch need is its own query's, whatever the tuned workspace path would take
+    need = ctypes.c_size_t(0)
+    assert L.gffm_matmul_limb_static_scratch_size(1000, 900, 1100, P26, ctypes.byref(need)) == 0
+    assert need.value == 4 * (1024 + 960) * 1152 * 2          # 4 digit planes, 128 / 64 / 64 padding
     m = n = k = 2048             # 4 digits: 4 * (2048 + 2048) * 2048 * 2 bytes = 64 MiB > 32 MiB
+    assert L.gffm_matmul_limb_static_scratch_size(m, n, k, P26, ctypes.byref(need)) == 0
+    assert need.value > cap.value
     A = torch.zeros((k, m + 32), dtype=torch.float64, device="cuda")
     B = torch.zeros((n, k + 32), dtype=torch.float64, device="cuda")
     C = torch.zeros((n, m + 32), dtype=torch.float64, device="cuda")
