@@ -13,6 +13,7 @@
 // copy back stay exposed.  The host buffers should be page-locked for the
 // copies to run asynchronously.
 #include "gffm_common.cuh"
+#include "kara_host.h"
 #include "limb_host.h"
 
 #include <algorithm>
@@ -68,10 +69,10 @@ struct Blocks {
     std::vector<int64_t> ra, cb;   // row cuts of A, column cuts of B (first 0, last m / n)
     int na, nb;
 };
-Blocks blocks_for(int64_t m, int64_t n) {
+Blocks blocks_for(int64_t m, int64_t n, int64_t col_quantum) {
     Blocks b;
     b.ra = cuts(m, 128);
-    b.cb = cuts(n, 64);
+    b.cb = cuts(n, col_quantum);
     b.na = (int)b.ra.size() - 1;
     b.nb = (int)b.cb.size() - 1;
     return b;
@@ -81,7 +82,7 @@ Blocks blocks_for(int64_t m, int64_t n) {
 // to 32) and the digit planes of every block of A and of B
 struct HostLayout {
     Blocks b;
-    int bits, tile_n;
+    int bits, tile_n, form;
     int64_t lda_d, ldb_d, ldc_d;
     size_t off_a, off_b, off_c;
     std::vector<size_t> off_da, off_db;
@@ -90,9 +91,12 @@ struct HostLayout {
 
 HostLayout host_layout(int64_t m, int64_t n, int64_t k, int64_t N) {
     HostLayout h;
-    h.b = blocks_for(m, n);
     int ctas = 0;
-    limb::tuned_for(m, n, k, N, &h.bits, &ctas, &h.tile_n);
+    limb::tuned_for(m, n, k, N, &h.bits, &ctas, &h.tile_n, &h.form);
+    if (h.form == limb::FORM_KARATSUBA && !kara::applies(N)) h.form = limb::FORM_SCHOOLBOOK;
+    h.form = limb::resolve_form(h.form, h.bits, h.tile_n, N, k);
+    const bool kf = h.form == limb::FORM_KARATSUBA;
+    h.b = blocks_for(m, n, kf ? 128 : 64);
     h.lda_d = gffm::round_up(std::max<int64_t>(m, 1), 32);
     h.ldb_d = gffm::round_up(std::max<int64_t>(k, 1), 32);
     h.ldc_d = h.lda_d;
@@ -106,10 +110,16 @@ HostLayout host_layout(int64_t m, int64_t n, int64_t k, int64_t N) {
     h.off_b = take((size_t)h.ldb_d * (size_t)std::max<int64_t>(n, 1) * 8);
     h.off_c = take((size_t)h.ldc_d * (size_t)std::max<int64_t>(n, 1) * 8);
     if (k > 0) {
-        for (int i = 0; i < h.b.na; i++)
-            h.off_da.push_back(take(limb::layout_bits(h.b.ra[i + 1] - h.b.ra[i], 1, k, N, h.bits).a_bytes));
-        for (int j = 0; j < h.b.nb; j++)
-            h.off_db.push_back(take(limb::layout_bits(1, h.b.cb[j + 1] - h.b.cb[j], k, N, h.bits).b_bytes));
+        for (int i = 0; i < h.b.na; i++) {
+            const int64_t rows = h.b.ra[i + 1] - h.b.ra[i];
+            h.off_da.push_back(take(kf ? kara::layout(rows, 1, k).a_bytes
+                                       : limb::layout_bits(rows, 1, k, N, h.bits).a_bytes));
+        }
+        for (int j = 0; j < h.b.nb; j++) {
+            const int64_t cols = h.b.cb[j + 1] - h.b.cb[j];
+            h.off_db.push_back(take(kf ? kara::layout(1, cols, k).b_bytes
+                                       : limb::layout_bits(1, cols, k, N, h.bits).b_bytes));
+        }
     }
     h.total = off;
     return h;
@@ -185,13 +195,16 @@ int enqueue(const HostLayout &h, const HostStreams &hs, uint8_t *base, int64_t m
         const int i = ij.first, j = ij.second;
         const int64_t rows = rows_of(i), cols = cols_of(j);
         cudaStream_t c = hs.c[which];
+        const bool kf = h.form == limb::FORM_KARATSUBA;
         limb::Layout g = limb::layout_bits(rows, cols, k, N, h.bits);
         g.bn = h.tile_n;
+        const kara::Layout kg = kara::layout(rows, cols, k);
         __half *Ad = reinterpret_cast<__half *>(base + h.off_da[i]);
         __half *Bd = reinterpret_cast<__half *>(base + h.off_db[j]);
         if (a_on[i] < 0) {
             GFFM_CUDA(cudaStreamWaitEvent(c, a_in[i], 0));
-            st = limb::split_a<double>(dA + b.ra[i], h.lda_d, rows, k, Ad, g, N, c);
+            st = kf ? kara::split_a<double>(dA + b.ra[i], h.lda_d, rows, k, Ad, kg, N, c)
+                    : limb::split_a<double>(dA + b.ra[i], h.lda_d, rows, k, Ad, g, N, c);
             if (st) return st;
             GFFM_CUDA(cudaEventRecord(a_sp[i], c));
             a_on[i] = which;
@@ -200,7 +213,8 @@ int enqueue(const HostLayout &h, const HostStreams &hs, uint8_t *base, int64_t m
         }
         if (b_on[j] < 0) {
             GFFM_CUDA(cudaStreamWaitEvent(c, b_in[j], 0));
-            st = limb::split_b<double>(dB + b.cb[j] * h.ldb_d, h.ldb_d, k, cols, Bd, g, N, c);
+            st = kf ? kara::split_b<double>(dB + b.cb[j] * h.ldb_d, h.ldb_d, k, cols, Bd, kg, N, c)
+                    : limb::split_b<double>(dB + b.cb[j] * h.ldb_d, h.ldb_d, k, cols, Bd, g, N, c);
             if (st) return st;
             GFFM_CUDA(cudaEventRecord(b_sp[j], c));
             b_on[j] = which;
@@ -208,7 +222,8 @@ int enqueue(const HostLayout &h, const HostStreams &hs, uint8_t *base, int64_t m
             GFFM_CUDA(cudaStreamWaitEvent(c, b_sp[j], 0));
         }
         double *Cij = dC + b.ra[i] + b.cb[j] * h.ldc_d;
-        st = limb::gemm_digits(g, Ad, Bd, rows, cols, k, N, Cij, h.ldc_d, limb::EPI_STORE_F64, 0, c);
+        st = kf ? kara::gemm_digits(kg, Ad, Bd, rows, cols, k, N, Cij, h.ldc_d, limb::EPI_STORE_F64, 0, c)
+                : limb::gemm_digits(g, Ad, Bd, rows, cols, k, N, Cij, h.ldc_d, limb::EPI_STORE_F64, 0, c);
         if (st) return st;
         cudaEvent_t e_c;
         if ((st = evs.make(&e_c))) return st;

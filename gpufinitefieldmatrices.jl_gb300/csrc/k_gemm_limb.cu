@@ -1,6 +1,7 @@
 // k_gemm_limb.cu -- host side of the limb tensor-core GEMM (gemm_limb.cuh):
 // argument checks, workspace layout, TMA descriptors and launches.
 #include "gemm_limb.cuh"
+#include "kara_host.h"
 #include "limb_host.h"
 #include "limb_launch.cuh"
 
@@ -291,10 +292,11 @@ namespace limb {
 static std::vector<gffm_tune_entry> g_tune;
 static std::mutex g_tune_mu;
 
-void tuned_for(int64_t m, int64_t n, int64_t k, int64_t N, int *bits, int *max_ctas, int *tile_n) {
+void tuned_for(int64_t m, int64_t n, int64_t k, int64_t N, int *bits, int *max_ctas, int *tile_n, int *form) {
     *bits = 7;
     *max_ctas = 0;
     *tile_n = 64;
+    *form = FORM_DEFAULT;
     const double work = (double)m * (double)n * (double)k;
     std::lock_guard<std::mutex> lk(g_tune_mu);
     for (const gffm_tune_entry &e : g_tune) {
@@ -302,8 +304,17 @@ void tuned_for(int64_t m, int64_t n, int64_t k, int64_t N, int *bits, int *max_c
         *bits = e.tuning.digit_bits == 8 ? 8 : 7;
         *max_ctas = e.tuning.max_ctas > 0 ? e.tuning.max_ctas : 0;
         *tile_n = e.tuning.tile_n == 32 ? 32 : 64;
+        *form = e.tuning.form;
         return;
     }
+}
+
+int resolve_form(int form, int bits, int tile_n, int64_t N, int64_t k) {
+    if (form == FORM_SCHOOLBOOK || form == FORM_KARATSUBA) return form;
+    // the default: Karatsuba for four 7-bit digits once the products are long enough to
+    // amortise its three per-product accumulator drains, unless the schoolbook's 8-bit
+    // digits or 32-column tiles were asked for
+    return (bits == 7 && tile_n != 32 && kara::applies(N) && k >= KARA_MIN_K) ? FORM_KARATSUBA : FORM_SCHOOLBOOK;
 }
 
 }  // namespace limb
@@ -312,6 +323,7 @@ namespace {
 
 int check_tuning(const gffm_limb_tuning *t) {
     if (!t) return GFFM_OK;
+    if (t->form < 0 || t->form > 2) return gffm::set_error(GFFM_ERR_ARG, "form must be 0, 1 or 2");
     if (t->digit_bits != 0 && t->digit_bits != 7 && t->digit_bits != 8)
         return gffm::set_error(GFFM_ERR_ARG, "digit_bits must be 0, 7 or 8");
     if (t->max_ctas < 0) return gffm::set_error(GFFM_ERR_ARG, "max_ctas must be >= 0");
@@ -320,14 +332,33 @@ int check_tuning(const gffm_limb_tuning *t) {
     return GFFM_OK;
 }
 
-// the digit width, grid and tile width of a product: an explicit tuning, else the tune table
-void pick(const gffm_limb_tuning *t, int64_t m, int64_t n, int64_t k, int64_t N, int *bits, int *ctas, int *tile_n) {
-    limb::tuned_for(m, n, k, N, bits, ctas, tile_n);
+// the digit width, grid, tile width and product form of a product: an explicit tuning, else
+// the tune table; an explicit Karatsuba form must fit the modulus
+int pick(const gffm_limb_tuning *t, int64_t m, int64_t n, int64_t k, int64_t N, int *bits, int *ctas, int *tile_n,
+         int *form) {
+    limb::tuned_for(m, n, k, N, bits, ctas, tile_n, form);
     if (t) {
         if (t->digit_bits) *bits = t->digit_bits;
         *ctas = t->max_ctas;
         if (t->tile_n) *tile_n = t->tile_n;
+        if (t->form) *form = t->form;
+        if (t->form == limb::FORM_KARATSUBA && !kara::applies(N))
+            return gffm::set_error(GFFM_ERR_UNSUPPORTED, "the Karatsuba form needs 2080639 < N < 2^26 (got %lld)",
+                                   (long long)N);
     }
+    if (*form == limb::FORM_KARATSUBA && !kara::applies(N)) *form = limb::FORM_SCHOOLBOOK;   // a table range
+    *form = limb::resolve_form(*form, *bits, *tile_n, N, k);
+    return GFFM_OK;
+}
+
+// scratch bytes of a product in the chosen form
+size_t scratch_bytes(int64_t m, int64_t n, int64_t k, int64_t N, int bits, int form) {
+    if (form == limb::FORM_KARATSUBA) {
+        kara::Layout g = kara::layout(m, n, k);
+        return g.a_bytes + g.b_bytes;
+    }
+    limb::Layout g = limb::layout_bits(m, n, k, N, bits);
+    return g.a_bytes + g.b_bytes;
 }
 
 template <typename T>
@@ -348,11 +379,25 @@ int matmul_limb(int64_t m, int64_t n, int64_t k, const T *A, int64_t lda, const 
         GFFM_CUDA(cudaMemset2DAsync(C, (size_t)ldc * sizeof(T), 0, (size_t)m * sizeof(T), (size_t)n, s));
         return GFFM_OK;
     }
-    int bits, ctas, tile_n;
-    pick(tune, m, n, k, N, &bits, &ctas, &tile_n);
+    int bits, ctas, tile_n, form;
+    st = pick(tune, m, n, k, N, &bits, &ctas, &tile_n, &form);
+    if (st) return st;
+    const int epi = sizeof(T) == 8 ? limb::EPI_STORE_F64 : limb::EPI_STORE_F32;
+    Scratch scr;
+    if (form == limb::FORM_KARATSUBA) {
+        kara::Layout kg = kara::layout(m, n, k);
+        st = scr.acquire(ws, ws_bytes, kg.a_bytes + kg.b_bytes, s);
+        if (st) return st;
+        __half *Ad = static_cast<__half *>(scr.ptr);
+        __half *Bd = reinterpret_cast<__half *>(static_cast<uint8_t *>(scr.ptr) + kg.a_bytes);
+        st = kara::split_a<T>(A, lda, m, k, Ad, kg, N, s);
+        if (st) return st;
+        st = kara::split_b<T>(B, ldb, k, n, Bd, kg, N, s);
+        if (st) return st;
+        return kara::gemm_digits(kg, Ad, Bd, m, n, k, N, C, ldc, epi, ctas, s);
+    }
     limb::Layout g = limb::layout_bits(m, n, k, N, bits);
     g.bn = tile_n;
-    Scratch scr;
     st = scr.acquire(ws, ws_bytes, g.a_bytes + g.b_bytes, s);
     if (st) return st;
     __half *Ad = static_cast<__half *>(scr.ptr);
@@ -361,8 +406,7 @@ int matmul_limb(int64_t m, int64_t n, int64_t k, const T *A, int64_t lda, const 
     if (st) return st;
     st = limb::split_b<T>(B, ldb, k, n, Bd, g, N, s);
     if (st) return st;
-    return limb::gemm_digits(g, Ad, Bd, m, n, k, N, C, ldc,
-                             sizeof(T) == 8 ? limb::EPI_STORE_F64 : limb::EPI_STORE_F32, ctas, s);
+    return limb::gemm_digits(g, Ad, Bd, m, n, k, N, C, ldc, epi, ctas, s);
 }
 
 }  // namespace
@@ -376,10 +420,10 @@ int gffm_matmul_limb_tuned_workspace_size(int64_t m, int64_t n, int64_t k, int64
     if (st) return st;
     st = limb::check_args(m, n, k, m > 1 ? m : 1, k > 1 ? k : 1, m > 1 ? m : 1, N);
     if (st) return st;
-    int bits, ctas, tile_n;
-    pick(tuning, m, n, k, N, &bits, &ctas, &tile_n);
-    limb::Layout g = limb::layout_bits(m, n, k, N, bits);
-    *bytes = (m == 0 || n == 0 || k == 0) ? 0 : g.a_bytes + g.b_bytes;
+    int bits, ctas, tile_n, form;
+    st = pick(tuning, m, n, k, N, &bits, &ctas, &tile_n, &form);
+    if (st) return st;
+    *bytes = (m == 0 || n == 0 || k == 0) ? 0 : scratch_bytes(m, n, k, N, bits, form);
     return GFFM_OK;
 }
 

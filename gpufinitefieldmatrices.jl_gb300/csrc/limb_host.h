@@ -39,8 +39,15 @@ int raw_limbs_for(int64_t N);
 Layout layout(int64_t m, int64_t n, int64_t k, int64_t N);
 Layout layout_bits(int64_t m, int64_t n, int64_t k, int64_t N, int bits);
 int chunk_kblocks(const Layout &g);        // k-blocks of 64 per exact accumulation chunk
-// the process-wide tune table's choice for a product (digit width, grid, tile width); defaults 7 / 0 / 64
-void tuned_for(int64_t m, int64_t n, int64_t k, int64_t N, int *bits, int *max_ctas, int *tile_n);
+// how the digit products of a limb GEMM are formed (gffm_limb_tuning.form)
+enum Form { FORM_DEFAULT = 0, FORM_SCHOOLBOOK = 1, FORM_KARATSUBA = 2 };
+// the default form is Karatsuba (kara_host.h) for four 7-bit digits from this inner dimension on
+constexpr int64_t KARA_MIN_K = 1024;
+// the process-wide tune table's choice for a product (digit width, grid, tile width, form);
+// defaults 7 / 0 / 64 / FORM_DEFAULT
+void tuned_for(int64_t m, int64_t n, int64_t k, int64_t N, int *bits, int *max_ctas, int *tile_n, int *form);
+// FORM_SCHOOLBOOK or FORM_KARATSUBA for a tuned form, digit width, tile width, modulus and inner dimension
+int resolve_form(int form, int bits, int tile_n, int64_t N, int64_t k);
 Layout layout_L(int64_t m, int64_t n, int64_t k, int L);
 int check_args(int64_t m, int64_t n, int64_t k, int64_t lda, int64_t ldb, int64_t ldc, int64_t N);
 

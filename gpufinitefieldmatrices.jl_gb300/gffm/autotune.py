@@ -34,7 +34,7 @@ BITS8_RANGES = [(16256, 65279), (2080640, 16711423)]
 
 class _LimbTuning(ctypes.Structure):
     _fields_ = [("digit_bits", ctypes.c_int32), ("max_ctas", ctypes.c_int32), ("tile_n", ctypes.c_int32),
-                ("reserved", ctypes.c_int32)]
+                ("form", ctypes.c_int32)]
 
 
 class _Entry(ctypes.Structure):
@@ -62,7 +62,8 @@ def apply(table=None):
     arr = (_Entry * max(1, len(ents)))()
     for i, e in enumerate(ents):
         arr[i] = _Entry(int(e["N_lo"]), int(e["N_hi"]), float(e["work_lo"]), float(e["work_hi"]),
-                        _LimbTuning(int(e["digit_bits"]), int(e.get("max_ctas", 0)), int(e.get("tile_n", 0)), 0))
+                        _LimbTuning(int(e["digit_bits"]), int(e.get("max_ctas", 0)), int(e.get("tile_n", 0)),
+                                    int(e.get("form", 0))))
     call("gffm_tune_table_set", ctypes.cast(arr, ctypes.c_void_p), len(ents))
     return len(ents)
 

@@ -392,7 +392,7 @@ def limbs_for(N, bits=7):
 class LimbTuning(ctypes.Structure):
     """gffm_limb_tuning: digit width (0 = the tune table's choice, 7 or 8) and grid (0 = one CTA per SM)."""
     _fields_ = [("digit_bits", ctypes.c_int32), ("max_ctas", ctypes.c_int32), ("tile_n", ctypes.c_int32),
-                ("reserved", ctypes.c_int32)]
+                ("form", ctypes.c_int32)]
 
 
 def _gemm(C, A, B, N, method, stripe=0, tuning=None):

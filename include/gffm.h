@@ -164,7 +164,13 @@ GFFM_API int gffm_matmul_limb_f32(int64_t m, int64_t n, int64_t k, const float *
  * digit_bits: 7 (balanced base-2^7 digits, the default) or 8 (base-2^8: one
  * digit fewer for 16255 < N <= 65279 and 2080639 < N <= 16711423, with 4x more
  * frequent exact-accumulation drains); 0 keeps the table's / default choice.
- * max_ctas: persistent grid size (0 = one CTA per SM); tile_n: 0/64 or 32.  The process-wide tune
+ * max_ctas: persistent grid size (0 = one CTA per SM); tile_n: 0/64 or 32.
+ * form: how the digit products are formed: 1 = schoolbook (L^2 digit products,
+ * 16 for four digits), 2 = one level of Karatsuba over 13-bit halves (12 digit
+ * products; moduli 2080639 < N < 2^26 only, its own 7/6-bit digits, 128 x 128
+ * tiles; digit_bits and tile_n do not apply), 0 = the default: Karatsuba where
+ * it applies, k >= 1024 and neither 8-bit digits nor 32-column tiles were
+ * asked for, else schoolbook.  The process-wide tune
  * table (written by the autotuner, gffm/autotune.py) maps a modulus range and a
  * work range (m*n*k) to a tuning; gffm_matmul_limb_* and its workspace size
  * consult it, first matching entry wins.  It is the library's only global
@@ -173,7 +179,7 @@ typedef struct gffm_limb_tuning {
     int32_t digit_bits;
     int32_t max_ctas;
     int32_t tile_n;           /* output tile width: 64 (default) or 32 with two TMEM accumulator sets */
-    int32_t reserved;         /* 0 */
+    int32_t form;             /* 0 default, 1 schoolbook, 2 Karatsuba (12 digit products) */
 } gffm_limb_tuning;
 typedef struct gffm_tune_entry {
     int64_t N_lo, N_hi;       /* inclusive modulus range */

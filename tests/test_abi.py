@@ -60,7 +60,20 @@ def test_host_side_argument_errors(lib):
     assert st == 1
     ws = ctypes.c_size_t(0)
     assert lib.gffm_matmul_limb_workspace_size(8192, 8192, 8192, 67108859, ctypes.byref(ws)) == 0
+    # default form at 8192^3 mod p26: Karatsuba, six digit planes per operand
+    assert ws.value == 6 * (8192 + 8192) * 8192 * 2
+    # the schoolbook form asked for explicitly: four digit planes per operand
+    class Tuning(ctypes.Structure):
+        _fields_ = [(f, ctypes.c_int32) for f in ("digit_bits", "max_ctas", "tile_n", "form")]
+    assert lib.gffm_matmul_limb_tuned_workspace_size(8192, 8192, 8192, 67108859, ctypes.byref(Tuning(0, 0, 0, 1)),
+                                                     ctypes.byref(ws)) == 0
     assert ws.value == 4 * (8192 + 8192) * 8192 * 2
+    # below 1024 of k the default is the schoolbook
+    assert lib.gffm_matmul_limb_workspace_size(1000, 1000, 1000, 67108859, ctypes.byref(ws)) == 0
+    assert ws.value == 4 * (1024 + 1024) * 1024 * 2
+    # an explicit Karatsuba form for a modulus it does not cover is refused
+    assert lib.gffm_matmul_limb_tuned_workspace_size(64, 64, 64, 65521, ctypes.byref(Tuning(0, 0, 0, 2)),
+                                                     ctypes.byref(ws)) == 10
 
 
 def test_host_gemm_workspace_and_argument_errors(lib):
@@ -69,7 +82,7 @@ def test_host_gemm_workspace_and_argument_errors(lib):
     ws = ctypes.c_size_t(0)
     assert lib.gffm_matmul_host_workspace_size(8192, 8192, 8192, 67108859, ctypes.byref(ws)) == 0
     staging = 3 * 8192 * 8192 * 8
-    digits = 2 * 4 * 8192 * 8192 * 2          # 4 fp16 digits per residue at this modulus
+    digits = 2 * 6 * 8192 * 8192 * 2          # 6 fp16 planes per residue (the Karatsuba form) at this modulus
     assert staging + digits <= ws.value <= staging + digits + 64 * 1024
     assert lib.gffm_matmul_host_workspace_size(0, 5, 5, 7, ctypes.byref(ws)) == 0 and ws.value == 0
     assert lib.gffm_matmul_host_f64(-1, 4, 4, None, 4, None, 4, None, 4, 7, None, 0, None) == 1

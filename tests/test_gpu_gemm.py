@@ -328,3 +328,100 @@ def test_limb_gemm_32_column_tiles(gffm, N, bits, shape):
         want = oracle.matmul(A, B, N)
         assert np.array_equal(got, want), "%s: %d mismatches" % (name, int((got != want).sum()))
     status_ok(gffm)
+
+
+# ---- the two product forms: schoolbook (16 digit products) and one-level Karatsuba (12) ----
+KARA_MODULI = [2080640, 8388593, P25, P26, 2 ** 26 - 1]
+KARA_SHAPES = [(1, 1, 1), (130, 200, 1024), (129, 257, 1025), (64, 130, 2112), (200, 64, 4096), (70, 300, 4161),
+               (256, 256, 8256)]
+
+
+def kara_extreme(N, rng, shape):
+    """Residues whose Karatsuba digits sit at their extremes: a0, a2 in {-64, 63}, a1 in
+    {-32, 31, 32} and a3 at the largest magnitude the modulus allows
+    (c = a0 + 2^7 a1 + 2^13 (a2 + 2^7 a3)), kept within the centred range."""
+    half = (N - 1) // 2
+    top = max(1, min(32, (half // 8192 + 63) // 128))
+    size = int(np.prod(shape))
+    got = np.zeros(0, dtype=np.int64)
+    for _ in range(100):
+        if got.size >= size:
+            break
+        a0 = rng.choice(np.array([-64, 63]), size=2 * size)
+        a2 = rng.choice(np.array([-64, 63]), size=2 * size)
+        a1 = rng.choice(np.array([-32, 31, 32]), size=2 * size)
+        a3 = rng.choice(np.array([-top, top - 1, top]), size=2 * size)
+        lo = a0 + 128 * a1
+        c = lo + 8192 * (a2 + 128 * a3)
+        ok = (lo >= -4096) & (lo <= 4095) & (np.abs(c) <= half)
+        got = np.concatenate([got, c[ok] % N])
+    assert got.size >= size
+    return got[:size].reshape(shape)
+
+
+def kara_worst(N):
+    """One residue with digits (-64, 32, -64, 32) or the largest that fits N: the Karatsuba
+    middle product's sums s0 = -128, s1 = 64 reach the exactness bound 16384 per k."""
+    for a3 in (32, 16, 8, 0):
+        c = (-64 + 128 * 32) + 8192 * (-64 + 128 * a3)
+        if abs(c) <= (N - 1) // 2:
+            return c % N
+    return 1
+
+
+@pytest.mark.parametrize("N", KARA_MODULI)
+@pytest.mark.parametrize("shape", KARA_SHAPES, ids=lambda s: "x".join(map(str, s)))
+@pytest.mark.parametrize("form", [1, 2], ids=["schoolbook", "karatsuba"])
+def test_limb_gemm_forms_match_oracle(gffm, N, shape, form):
+    rng = np.random.default_rng(N % 1000 + shape[2] + form)
+    m, n, k = shape
+    tu = gffm.LimbTuning(0, 0, 0, form)
+    cases = list(patterns(rng, N, m, n, k))
+    cases.append(("kara_extreme", kara_extreme(N, rng, (m, k)), kara_extreme(N, rng, (k, n))))
+    w = kara_worst(N)
+    cases.append(("kara_worst", np.full((m, k), w), np.full((k, n), w)))
+    cases.append(("kara_worst_neg", np.full((m, k), w), np.full((k, n), (N - w) % N)))
+    for name, A, B in cases:
+        got = as_int(gffm.mat_mul_gpu_type(gffm.CuModMatrix(A, N, elem_type=torch.float64),
+                                           gffm.CuModMatrix(B, N, elem_type=torch.float64), method="limb", tuning=tu))
+        want = oracle.matmul(A, B, N)
+        assert np.array_equal(got, want), "%s: %d mismatches" % (name, int((got != want).sum()))
+    status_ok(gffm)
+
+
+@pytest.mark.parametrize("N", [8388593, P26])
+def test_karatsuba_form_f32_storage_and_workspace(gffm, N):
+    """The Karatsuba form through the Float32 entry point (N < 2^24 only) and with a caller
+    workspace of exactly the queried size."""
+    import ctypes
+    rng = np.random.default_rng(N)
+    m, n, k = 190, 250, 3000
+    A, B = rng.integers(0, N, size=(m, k)), rng.integers(0, N, size=(k, n))
+    L = gffm.load_library()
+    ws = ctypes.c_size_t(0)
+    assert L.gffm_matmul_limb_workspace_size(m, n, k, N, ctypes.byref(ws)) == 0
+    # six planes of 128-row padded A and B digits
+    assert ws.value == 6 * 2 * (256 + 256) * 3008
+    buf = torch.empty(ws.value, dtype=torch.uint8, device="cuda")
+    for dt, sfx in ((torch.float64, "f64"), (torch.float32, "f32")):
+        if dt == torch.float32 and N >= 2 ** 24:
+            continue
+        Ag = gffm.CuModMatrix(A, N, elem_type=dt)
+        Bg = gffm.CuModMatrix(B, N, elem_type=dt)
+        C = gffm.zeros(dt, m, n, N)
+        st = getattr(L, "gffm_matmul_limb_" + sfx)(m, n, k, Ag.data.data_ptr(), Ag.ld, Bg.data.data_ptr(), Bg.ld,
+                                                  C.data.data_ptr(), C.ld, N, buf.data_ptr(), ws.value, None)
+        assert st == 0
+        assert np.array_equal(as_int(C), oracle.matmul(A, B, N))
+    status_ok(gffm)
+
+
+def test_karatsuba_form_errors(gffm):
+    A = gffm.CuModMatrix([[1, 2], [3, 4]], 65521, elem_type=torch.float64)
+    with pytest.raises(gffm.GFFMError) as ei:            # the form needs four 7-bit digits
+        gffm.mat_mul_gpu_type(A, A, method="limb", tuning=gffm.LimbTuning(0, 0, 0, 2))
+    assert ei.value.status == 10
+    with pytest.raises(gffm.GFFMError) as ei:
+        gffm.mat_mul_gpu_type(A, A, method="limb", tuning=gffm.LimbTuning(0, 0, 0, 3))
+    assert ei.value.status == 1
+    status_ok(gffm)
