@@ -596,4 +596,149 @@ __global__ void __launch_bounds__(256) k_rows_permute(int32_t *__restrict__ W, i
     }
 }
 
+// ---------------------------------------------------------------------------
+// Tall panels: more rows below the panel than the cooperative kernel holds in
+// shared memory (MAX_PANEL_CTAS x PANEL_MAX_R, fewer on a GPU with fewer SMs).
+// A tall panel is at most TALL_NB columns wide and factors right-looking in
+// global memory, three launches per pivot step t:
+//   k_tall_search  the pivot: largest residue of column t below row R0 + t,
+//                  lowest row on ties (one 64-bit atomic max of
+//                  value << 32 | (2^32 - 1 - row)),
+//   k_tall_pivot   one warp: a zero column (or L's bound) stops the panel;
+//                  otherwise the pivot's inverse (the reference's Euclid), the
+//                  swap of rows R0 + t and the pivot row in the panel's
+//                  columns, the new pivot row scaled from column t on,
+//   k_tall_update  the rows below: W[r][c] -= l_r U[t][c] for the panel's
+//                  columns c > t, l_r = W[r][t] (kept unscaled: the multiplier).
+// k_tall_finish then writes the pivot count, the status and L11^{-1}.  The
+// panel ends as k_panel leaves it: U on and above the diagonal, the unscaled
+// multipliers below it, the columns after a stop up to date, the pivot records
+// and L11^{-1}; the blocked algorithm around it is unchanged.  No waits.
+constexpr int TALL_NB = 32;
+
+struct TallArgs {
+    int32_t *W;
+    int64_t ldw;
+    int m, R0, C0, nbw;
+    ModP M;
+    int l_cols;                  // L's padded width (PLUQ bound check), <= 0: no check
+    unsigned long long *key;     // the step's pivot key, zero before each search
+    int *state;                  // [0] stopped, [1] pivots at the stop, [2] status of the stop
+    uint32_t *urow;              // [TALL_NB] the step's scaled pivot row
+    int32_t *piv_row, *piv_val, *piv_inv;
+    int32_t *linv;               // L11^{-1}, row-major, ld NB
+    int *result;                 // [0] pivots, [1] status
+};
+
+__global__ void __launch_bounds__(256) k_tall_search(TallArgs a, int t) {
+    __shared__ unsigned long long red[8];
+    if (*(volatile int *)a.state) return;
+    const int c = a.C0 + t;
+    unsigned long long best = 0;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t r = a.R0 + t + (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < a.m; r += stride) {
+        const unsigned long long k =
+            ((unsigned long long)(uint32_t)a.W[r * a.ldw + c] << 32) | (0xFFFFFFFFu - (uint32_t)r);
+        best = k > best ? k : best;
+    }
+    best = warp_max_u64(best);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = best;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        best = warp_max_u64(threadIdx.x < 8 ? red[threadIdx.x] : 0ull);
+        if (threadIdx.x == 0 && best) atomicMax(a.key, best);
+    }
+}
+
+__global__ void __launch_bounds__(TALL_NB) k_tall_pivot(TallArgs a, int t) {
+    __shared__ uint32_t s_inv;
+    if (*(volatile int *)a.state) return;
+    const int tid = threadIdx.x;
+    const unsigned long long key = *(volatile unsigned long long *)a.key;
+    const uint32_t pv = (uint32_t)(key >> 32);
+    const int prow = (int)(0xFFFFFFFFu - (uint32_t)key);
+    const int r = a.R0 + t;
+    __syncwarp();
+    if (pv == 0 || (a.l_cols > 0 && a.C0 + t >= a.l_cols)) {
+        if (tid == 0) {
+            a.state[1] = t;
+            a.state[2] = pv == 0 ? PS_ZERO_COL : PS_BOUNDS;
+            a.state[0] = 1;
+        }
+        return;
+    }
+    if (tid == 0) s_inv = mod_inv_euclid_alu(pv, a.M.n);
+    __syncwarp();
+    const uint32_t inv = s_inv;
+    if (tid < a.nbw) {
+        int32_t *wr = a.W + (int64_t)r * a.ldw + a.C0;
+        int32_t *wp = a.W + (int64_t)prow * a.ldw + a.C0;
+        const uint32_t vr = (uint32_t)wr[tid], vp = (uint32_t)wp[tid];
+        // earlier columns: the rows' multipliers move unscaled; from column t on the pivot row is
+        // scaled (each thread reads and writes only its own column)
+        const uint32_t u = tid >= t ? mulmod(vp, inv, a.M) : vp;
+        wr[tid] = (int32_t)u;
+        if (prow != r) wp[tid] = (int32_t)vr;
+        a.urow[tid] = u;
+    }
+    if (tid == 0) {
+        *a.key = 0;
+        a.piv_row[t] = prow;
+        a.piv_val[t] = (int32_t)pv;
+        a.piv_inv[t] = (int32_t)inv;
+    }
+}
+
+// one warp per row, lane j on column t + 1 + j
+__global__ void __launch_bounds__(256) k_tall_update(TallArgs a, int t) {
+    if (*(volatile int *)a.state) return;
+    const int w = a.nbw - t - 1;
+    if (w <= 0) return;
+    const int lane = threadIdx.x & 31;
+    const uint32_t N = a.M.n;
+    const uint32_t u = lane < w ? a.urow[t + 1 + lane] : 0u;
+    const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    for (int64_t r = a.R0 + t + 1 + ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / 32; r < a.m; r += warps) {
+        int32_t *row = a.W + r * a.ldw + a.C0;
+        const uint32_t l = (uint32_t)row[t];
+        if (lane < w && l != 0) {
+            const uint32_t x = (uint32_t)row[t + 1 + lane];
+            row[t + 1 + lane] = (int32_t)p1_red((uint64_t)x + (uint64_t)(N - l) * u, a.M);
+        }
+    }
+}
+
+// one warp: the pivot count and status, and L11^{-1} (pivot values on L11's diagonal,
+// the unscaled multipliers below it): Linv[t][t] = inv_t,
+// Linv[t][s] = inv_t * sum_{s <= q < t} (N - l_t[q]) Linv[q][s]
+__global__ void __launch_bounds__(32) k_tall_finish(TallArgs a, int tmax) {
+    __shared__ uint32_t Li[TALL_NB][TALL_NB + 1];
+    const int s = threadIdx.x;
+    const int stopped = *(volatile int *)a.state;
+    const int npiv = stopped ? a.state[1] : tmax;
+    const int status = stopped ? a.state[2] : PS_DONE;
+    const uint32_t N = a.M.n;
+    for (int t = 0; t < npiv; t++) {
+        const uint32_t inv = (uint32_t)a.piv_inv[t];
+        if (s < t) {
+            const int32_t *lt = a.W + (int64_t)(a.R0 + t) * a.ldw + a.C0;
+            uint64_t acc = 0;
+            for (int q = s; q < t; q++) {
+                const uint32_t l = (uint32_t)lt[q];
+                acc += (uint64_t)(l ? N - l : 0u) * Li[q][s];
+            }
+            Li[t][s] = mulmod(p1_red(acc, a.M), inv, a.M);
+        } else if (s == t) {
+            Li[t][t] = inv;
+        }
+        __syncwarp();
+    }
+    for (int i = 0; i < npiv; i++)
+        if (s < npiv) a.linv[i * NB + s] = s <= i ? (int32_t)Li[i][s] : 0;
+    if (s == 0) {
+        a.result[0] = npiv;
+        a.result[1] = status;
+    }
+}
+
 }  // namespace elim

@@ -460,12 +460,57 @@ static int permute_rows2(const Work &w, const PermArgs &perm, int c_left, int c_
     return GFFM_OK;
 }
 
+// rows the cooperative panel holds in shared memory (one CTA per SM, PANEL_MAX_R rows each)
+static int panel_capacity() { return std::min(gffm::sm_count(), MAX_PANEL_CTAS) * PANEL_MAX_R; }
+// the width of a panel with `rows` rows from its first pivot row down
+static int panel_width(int rows) { return rows <= P1_MAX_ROWS ? P1_NB : (rows <= panel_capacity() ? NB : TALL_NB); }
+
+// a panel with more rows below it than the cooperative panel holds: TALL_NB columns, right-looking
+static int tall_panel(Work &w, int m, int R0, int C0, int nbw, const ModP &M, int lcols_check, cudaStream_t s) {
+    using namespace gffm;
+    // the kernels' key, state and scaled pivot row live in the (otherwise idle) exchange area
+    uint8_t *ex = reinterpret_cast<uint8_t *>(w.old_row);
+    TallArgs a;
+    a.W = w.W;
+    a.ldw = w.ldw;
+    a.m = m;
+    a.R0 = R0;
+    a.C0 = C0;
+    a.nbw = nbw;
+    a.M = M;
+    a.l_cols = lcols_check;
+    a.key = reinterpret_cast<unsigned long long *>(ex);
+    a.state = reinterpret_cast<int *>(ex + 64);
+    a.urow = reinterpret_cast<uint32_t *>(ex + 128);
+    a.piv_row = w.piv_row;
+    a.piv_val = w.piv_val;
+    a.piv_inv = w.piv_inv;
+    a.linv = w.linv;
+    a.result = w.result;
+    GFFM_CUDA(cudaMemsetAsync(ex, 0, 128, s));
+    const int rows = m - R0;
+    const int tmax = std::min(nbw, rows);
+    const int sms = sm_count();
+    const unsigned search_blocks = (unsigned)std::min<int64_t>((rows + 255) / 256, 4 * sms);
+    const unsigned update_blocks = (unsigned)std::min<int64_t>((rows + 7) / 8, 8 * sms);
+    for (int t = 0; t < tmax; t++) {
+        k_tall_search<<<search_blocks, 256, 0, s>>>(a, t);
+        k_tall_pivot<<<1, TALL_NB, 0, s>>>(a, t);
+        k_tall_update<<<update_blocks, 256, 0, s>>>(a, t);
+    }
+    k_tall_finish<<<1, 32, 0, s>>>(a, tmax);
+    GFFM_LAUNCH_CHECK("k_tall_*");
+    return GFFM_OK;
+}
+
 static int run_panel(Work &w, int m, int n, int R0, int C0, int nbw, const ModP &M, int lcols_check,
                      cudaStream_t s, void *stage, int h_res[2], std::vector<int32_t> &h_prow, std::vector<int32_t> &h_pv,
                      int max_g = 0) {
     using namespace gffm;
     const int rows = m - R0;
     const int sms = sm_count();
+    const bool tall = rows > panel_capacity();
+    if (tall && nbw > TALL_NB) return set_error(GFFM_ERR_ARG, "elimination: a tall panel is at most %d columns", TALL_NB);
     // rows per CTA: at least 64, and at most 128 CTAs while the rows fit; at most
     // max_g CTAs when the panel shares the GPU with a trailing update
     int R = 64;
@@ -476,11 +521,13 @@ static int run_panel(Work &w, int m, int n, int R0, int C0, int nbw, const ModP 
     }
     const int G = std::max(1, (rows + R - 1) / R);
     const bool one = rows <= P1_MAX_ROWS && nbw <= P1_NB;   // the whole panel in one CTA
-    if (!one && G > std::min(sms, MAX_PANEL_CTAS))
-        return set_error(GFFM_ERR_UNSUPPORTED, "elimination panel: %d rows exceed the panel kernel's capacity (%d)",
-                         rows, std::min(sms, MAX_PANEL_CTAS) * PANEL_MAX_R);
     const size_t smem = one ? p1_smem_bytes(rows) : panel_smem_bytes(R);
-    if (!one) GFFM_CUDA(cudaMemsetAsync(w.old_row, 0, exchange_bytes(G), s));
+    if (tall) {
+        int st = tall_panel(w, m, R0, C0, nbw, M, lcols_check, s);
+        if (st) return st;
+    } else if (!one) {
+        GFFM_CUDA(cudaMemsetAsync(w.old_row, 0, exchange_bytes(G), s));
+    }
     PanelArgs a;
     a.W = w.W;
     a.ldw = w.ldw;
@@ -500,7 +547,9 @@ static int run_panel(Work &w, int m, int n, int R0, int C0, int nbw, const ModP 
     a.linv = w.linv;
     a.result = w.result;
     a.err = device_error_flag();
-    if (one) {
+    if (tall) {
+        // factored above
+    } else if (one) {
         GFFM_CUDA(ensure_dynamic_smem<k_panel1>((int)smem));
         k_panel1<<<1, P1_THREADS, smem, s>>>(a);
         GFFM_LAUNCH_CHECK("k_panel1");
@@ -613,8 +662,9 @@ static int forward(Work &w, int m, int n, int64_t N, int mode, int lcols, cudaSt
     la.s = s;
     const bool use_look = !w.plain;
     while (row < m && col < n) {
-        // panels of 32 in one CTA once the rows fit it, of NB across CTAs before
-        const int nbw = std::min(m - row <= P1_MAX_ROWS ? P1_NB : NB, n - col);
+        // panels of 32 in one CTA once the rows fit it, of NB across CTAs before, of
+        // TALL_NB in global memory while the rows exceed the cooperative panel's capacity
+        const int nbw = std::min(panel_width(m - row), n - col);
         int st = run_panel(w, m, n, row, col, nbw, M, mode == MODE_PLUQ ? lcols : 0, s, stage.p, h_res, h_prow, h_pv,
                            la.pending ? la.next_g : 0);
         if (st) return st;
@@ -680,8 +730,9 @@ static int forward(Work &w, int m, int n, int64_t N, int mode, int lcols, cudaSt
                                    w.W + (int64_t)row * w.ldw + cs, w.ldw, t, n - cs, t, limb::EPI_STORE_I32, s);
                 if (st) return st;
                 if (row + t < m) {
-                    const int look = m - row - t <= P1_MAX_ROWS ? P1_NB : NB;   // the next panel's width
-                    if (use_look && t == nbw && n - cs > look && m - row - t >= 1024)
+                    const int look = panel_width(m - row - t);   // the next panel's width
+                    if (use_look && t == nbw && n - cs > look && m - row - t >= 1024 &&
+                        m - row - t <= panel_capacity())
                         st = update_lookahead(w, N, row, t, col, cs, m, n, look, la);
                     else
                         st = rowmajor_gemm(w, N, w.W + (int64_t)(row + t) * w.ldw + cs, w.ldw,

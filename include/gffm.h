@@ -213,10 +213,11 @@ GFFM_API int gffm_elim_workspace_size(int64_t m, int64_t n, int64_t l_cols, size
  * (m+32) x (m+32)) holds the pivot values at (row, col) and the eliminated
  * entries below.  row_swaps / col_swaps receive the swap stacks as 1-based
  * (i, j) pairs (capacity 2*m and 2*n int64), in order.  GFFM_ERR_BOUNDS where
- * the reference would index L out of bounds.  GFFM_ERR_UNSUPPORTED for more
- * than min(SMs, 160) * 288 rows (the cooperative panel keeps at most 288 rows
- * per SM in shared memory: 43776 on a 152-SM GB300), before the first panel.  The
- * same holds for the LU, RREF and inverse entries below. */
+ * the reference would index L out of bounds.  There is no row limit: while
+ * more rows lie below a panel than the cooperative panel keeps in shared
+ * memory (min(SMs, 160) * 288: 43776 on a 152-SM GB300), panels are 32
+ * columns wide and factor right-looking in global memory, with the same
+ * results.  The same holds for the LU, RREF and inverse entries below. */
 GFFM_API int gffm_pluq_f64(int64_t m, int64_t n, const double *A, int64_t lda, double *U, int64_t ldu, double *L,
                            int64_t ldl, int64_t l_cols, int64_t N, int64_t *row_swaps, int64_t *n_row_swaps,
                            int64_t *col_swaps, int64_t *n_col_swaps, int64_t *rank, void *workspace,

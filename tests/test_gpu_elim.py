@@ -343,19 +343,29 @@ def test_rref_and_inverse_need_a_prime(gffm):
     status_ok(gffm)
 
 
-def test_panel_row_capacity(gffm):
-    """The cooperative panel keeps at most 288 rows per CTA, one CTA per SM: a
-    matrix one row taller fails with GFFM_ERR_UNSUPPORTED before its first panel,
-    and the device stays usable."""
+def test_pluq_taller_than_the_cooperative_panel(gffm):
+    """More rows than the cooperative panel keeps in shared memory (min(SMs, 160) * 288):
+    the first panels factor as 32-column tall panels in global memory, exact against the
+    oracle -- a 50,000 x 64 matrix, and one row over the capacity."""
     sms = torch.cuda.get_device_properties(0).multi_processor_count
-    rows = min(sms, 160) * 288 + 1
-    A = gffm.CuModMatrix(np.ones((rows, 33), dtype=np.int64), 65521, elem_type=torch.float64)
-    with pytest.raises(gffm.GFFMError) as ei:
-        gffm.pluq_gpu_kernel(A)
-    assert "capacity" in str(ei.value)
-    status_ok(gffm)
-    # one row fewer factors
-    B = gffm.CuModMatrix(np.eye(rows - 1, 33, dtype=np.int64), 65521, elem_type=torch.float64)
-    U, L, rs, cs = gffm.pluq_gpu_kernel(B)
-    assert rs == [] and cs == []
+    cap = min(sms, 160) * 288
+    rng = np.random.default_rng(50000)
+    for (m, n, N, kind) in [(50000, 64, P26, "uniform"), (cap + 1, 40, 65521, "ties"), (50000, 70, 13, "zero_cols")]:
+        A = make(kind, m, n, N, rng)
+        U0, L0, rs0, cs0, rk0 = oracle.pluq(A, N, l_cols=n + 32)
+        U, L, rs, cs = gffm.pluq_gpu_kernel(gffm.CuModMatrix(A, N, elem_type=torch.float64))
+        assert rs == rs0 and cs == cs0
+        assert np.array_equal(np.rint(U.data[:n, :m].cpu().numpy().T).astype(np.int64), U0)
+        # L is the reference's (m+32) x (m+32): its first n + 32 columns hold every non-zero
+        # (the oracle's L is truncated there; its swap width is capped the same way)
+        Ld = L.data[:n + 32, :m].cpu().numpy().T
+        assert np.array_equal(np.rint(Ld).astype(np.int64), L0)
+        assert not bool(L.data[n + 32:, :].any()) and not bool(L.data[:, m:].any())
+        status_ok(gffm)
+    # RREF (zero columns skipped, not swapped) through the same tall panels
+    A = make("rank50", 46000, 60, P26, rng)
+    R0, rank0, piv0 = oracle.rref(A, P26)
+    R, rank, piv = gffm.rref_gpu_type(gffm.CuModMatrix(A, P26, elem_type=torch.float64), return_pivots=True)
+    assert rank == rank0 == 50 and piv == [c + 1 for c in piv0]
+    assert np.array_equal(as_int(R), R0)
     status_ok(gffm)
