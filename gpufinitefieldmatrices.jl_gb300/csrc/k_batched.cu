@@ -451,6 +451,10 @@ struct gffm_batch_plan_s {
         int64_t ldc, m, n;
     };
     std::vector<ZeroK> zero_k;   // products with an empty inner dimension: C = 0
+    // PLUQ instances taller than the persistent kernel takes: factored after the graph by
+    // the single-matrix elimination, their swap stacks staged through these host buffers
+    std::vector<gffm_batch_desc> tall;
+    std::vector<int64_t> h_rows, h_cols;
 };
 
 namespace {
@@ -468,6 +472,9 @@ using gffm::set_error;
 
 size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
+// PLUQ instances with more rows run after the graph on the single-matrix elimination
+constexpr int64_t kGraphPluqMaxRows = 1024;
+
 int check_desc(const gffm_batch_desc &d, int64_t i) {
     if (d.op != GFFM_BATCH_MATMUL && d.op != GFFM_BATCH_PLUQ)
         return set_error(GFFM_ERR_ARG, "instance %lld: unknown op %lld", (long long)i, (long long)d.op);
@@ -481,7 +488,6 @@ int check_desc(const gffm_batch_desc &d, int64_t i) {
         if (d.m > 0 && d.n > 0 && (!d.C || (d.k > 0 && (!d.A || !d.B))))
             return set_error(GFFM_ERR_ARG, "instance %lld: null data pointer", (long long)i);
     } else {
-        if (d.m > 1024) return set_error(GFFM_ERR_UNSUPPORTED, "instance %lld: batched PLUQ needs m <= 1024", (long long)i);
         if (d.n > (int64_t(1) << 20)) return set_error(GFFM_ERR_ARG, "instance %lld: n above 2^20", (long long)i);
         if (d.lda < std::max<int64_t>(d.m, 1) || d.ldc < std::max<int64_t>(d.m, 1) || d.ldl < std::max<int64_t>(d.m, 1))
             return set_error(GFFM_ERR_ARG, "instance %lld: leading dimension smaller than m", (long long)i);
@@ -598,6 +604,10 @@ int create(const gffm_batch_desc *descs, int64_t count, const gffm_batch_tuning 
     std::vector<int64_t> mm_ids, pq_ids;
     for (int64_t i = 0; i < count; i++) {
         const gffm_batch_desc &d = descs[i];
+        if (d.op == GFFM_BATCH_PLUQ && d.m > kGraphPluqMaxRows && d.n > 0) {
+            p->tall.push_back(d);
+            continue;
+        }
         if (d.m == 0 || d.n == 0) {
             if (d.op == GFFM_BATCH_PLUQ) pq_ids.push_back(i);   // still reports its info
             continue;
@@ -838,7 +848,7 @@ int gffm_batched_plan_info(gffm_batch_plan plan, int64_t *info) {
     if (!plan || !info) return set_error(GFFM_ERR_ARG, "null argument");
     info[0] = (int64_t)plan->mem_bytes;
     info[1] = plan->n_mm;
-    info[2] = plan->n_pq;
+    info[2] = plan->n_pq + (int64_t)plan->tall.size();
     info[3] = plan->nitems;
     info[4] = plan->gemm_grid;
     info[5] = plan->pq_grid;
@@ -847,11 +857,31 @@ int gffm_batched_plan_info(gffm_batch_plan plan, int64_t *info) {
 
 int gffm_batched_run(gffm_batch_plan plan, gffm_stream_t stream) {
     if (!plan) return set_error(GFFM_ERR_ARG, "plan is NULL");
-    if (!plan->exec) return GFFM_OK;
+    if (!plan->exec && plan->tall.empty()) return GFFM_OK;
     int dev = 0;
     GFFM_CUDA(cudaGetDevice(&dev));
     if (dev != plan->device) return set_error(GFFM_ERR_ARG, "the plan belongs to device %d", plan->device);
-    GFFM_CUDA(cudaGraphLaunch(plan->exec, gffm::as_stream(stream)));
+    const cudaStream_t s = gffm::as_stream(stream);
+    if (plan->exec) GFFM_CUDA(cudaGraphLaunch(plan->exec, s));
+    // the tall PLUQs, one after another on the same stream (each call synchronizes it)
+    for (const gffm_batch_desc &d : plan->tall) {
+        plan->h_rows.assign(2 * d.m, 0);
+        plan->h_cols.assign(2 * d.n, 0);
+        int64_t nr = 0, nc = 0, rank = 0;
+        int st = gffm_pluq_f64(d.m, d.n, d.A, d.lda, d.C, d.ldc, d.L, d.ldl, d.l_cols, d.N, plan->h_rows.data(), &nr,
+                               plan->h_cols.data(), &nc, &rank, nullptr, 0, stream);
+        int64_t info[4] = {nr, nc, rank, 0};
+        if (st == GFFM_ERR_BOUNDS) {
+            info[0] = info[1] = info[2] = 0;     // the reference's BoundsError for this instance
+            info[3] = GFFM_ERR_BOUNDS;
+        } else if (st) {
+            return st;
+        }
+        if (info[0]) GFFM_CUDA(cudaMemcpyAsync(d.row_swaps, plan->h_rows.data(), 2 * info[0] * 8, cudaMemcpyHostToDevice, s));
+        if (info[1]) GFFM_CUDA(cudaMemcpyAsync(d.col_swaps, plan->h_cols.data(), 2 * info[1] * 8, cudaMemcpyHostToDevice, s));
+        GFFM_CUDA(cudaMemcpyAsync(d.info, info, sizeof(info), cudaMemcpyHostToDevice, s));
+        GFFM_CUDA(cudaStreamSynchronize(s));   // the host staging is reused by the next instance
+    }
     return GFFM_OK;
 }
 

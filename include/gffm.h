@@ -351,7 +351,7 @@ enum gffm_batch_op { GFFM_BATCH_MATMUL = 0, GFFM_BATCH_PLUQ = 1 };
 
 typedef struct gffm_batch_desc {
     int64_t op;            /* gffm_batch_op */
-    int64_t m, n, k;       /* MATMUL: C (m x n) = A (m x k) * B (k x n) mod N; PLUQ: A is m x n, m <= 1024 */
+    int64_t m, n, k;       /* MATMUL: C (m x n) = A (m x k) * B (k x n) mod N; PLUQ: A is m x n */
     int64_t N;
     const double *A;       /* column-major Float64 residues (device) */
     int64_t lda;
@@ -385,7 +385,11 @@ GFFM_API int gffm_batched_plan_create(const gffm_batch_desc *descs, int64_t coun
                                       gffm_batch_plan *plan);
 /* info[0..5]: device bytes held, products, PLUQs, product output tiles, gemm CTAs, PLUQ CTAs */
 GFFM_API int gffm_batched_plan_info(gffm_batch_plan plan, int64_t *info);
-/* Launch the plan's graph on `stream` (asynchronous; the PLUQ results are in the descriptors' device arrays). */
+/* Launch the plan's graph on `stream` (asynchronous; the PLUQ results are in the descriptors' device arrays).
+ * PLUQ instances of more than 1024 rows are not in the graph: after it, run
+ * factors them one by one with the single-matrix elimination (gffm_pluq_f64)
+ * on the same stream, which synchronizes the stream, and fills the same
+ * descriptor arrays. */
 GFFM_API int gffm_batched_run(gffm_batch_plan plan, gffm_stream_t stream);
 GFFM_API int gffm_batched_plan_destroy(gffm_batch_plan plan);
 

@@ -133,13 +133,34 @@ def test_batched_errors(gffm):
     with pytest.raises(gffm.GFFMError) as ei:
         gffm.BatchPlan([("matmul", A, A)])
     assert ei.value.status == 3
-    big = gffm.zeros(torch.float64, 1100, 4, 7)
-    with pytest.raises(gffm.GFFMError) as ei:
-        gffm.BatchPlan([("pluq", big)])
-    assert ei.value.status == 10
     with pytest.raises(gffm.GFFMError) as ei:
         gffm.BatchPlan([("pluq", gffm.zeros(torch.float64, 4, 4, 7))], gffm.BatchTuning(12, 0, 0, 0, 0))
     assert ei.value.status == 1
     empty = gffm.BatchPlan([])
     empty.run()
+    assert gffm.load_library().gffm_device_status(None) == 0
+
+
+def test_batched_pluq_taller_than_1024_rows(gffm):
+    """PLUQ instances of more than 1024 rows are factored after the graph by the
+    single-matrix elimination, into the same result arrays; mixed with graph instances."""
+    rng = np.random.default_rng(1100)
+    specs = [("uniform", 1100, 4, 7), ("uniform", 1300, 200, P26), ("wide_quirk", 1025, 1100, 11),
+             ("rank30", 2000, 90, 65521), ("uniform", 300, 300, 1021)]
+    inst, want = [], []
+    for (kind, m, n, N) in specs:
+        A = make(kind, m, n, N, rng)
+        inst.append(("pluq", gffm.CuModMatrix(A, N, elem_type=torch.float64)))
+        try:
+            want.append(("pluq", oracle.pluq(A, N)))
+        except IndexError:
+            want.append(("pluq", None))
+    A, B = rng.integers(0, 65521, size=(200, 300)), rng.integers(0, 65521, size=(300, 100))
+    inst.append(("matmul", gffm.CuModMatrix(A, 65521, elem_type=torch.float64),
+                 gffm.CuModMatrix(B, 65521, elem_type=torch.float64)))
+    want.append(("matmul", oracle.matmul(A, B, 65521)))
+    plan = gffm.BatchPlan(inst)
+    assert plan.info()["pluqs"] == len(specs)
+    for _ in range(2):                      # a plan runs again on the same buffers
+        check(gffm, inst, want, plan.run().results())
     assert gffm.load_library().gffm_device_status(None) == 0
