@@ -15,13 +15,22 @@ struct FMod;
 
 template <>
 struct FMod<double> {
-    // x: an integer-valued double in [0, 2^53); returns x mod n exactly.
+    // x: an integer-valued double with |x| < 2^53; returns x mod n in [0, n) exactly
+    // (floor's quotient is off by at most one either way; the corrections fix it).
     __device__ static __forceinline__ double red(double x, double n, double inv) {
         double q = floor(x * inv);
         double r = fma(-q, n, x);
         if (r < 0.0) r += n;
         if (r >= n) r -= n;
         return r;
+    }
+    // x: an integer-valued double with |x| < 2^52 + 2^26 (one product plus a value in
+    // (-n, n)); returns a value congruent to x mod n in (-n, n), exactly: x * inv is
+    // within 2^-25 of x / n, so q = rint(x / n) leaves |x - q n| <= n/2 + 1, an integer
+    // the fma computes without rounding.  With the product's fma that is four FP64
+    // instructions per multiply-add instead of the two corrections of red().
+    __device__ static __forceinline__ double red_signed(double x, double n, double inv) {
+        return fma(-rint(x * inv), n, x);
     }
     __device__ static __forceinline__ double fma_(double a, double b, double c) { return fma(a, b, c); }
 };
@@ -34,6 +43,9 @@ struct FMod<float> {
         if (r < 0.0f) r += n;
         if (r >= n) r -= n;
         return r;
+    }
+    __device__ static __forceinline__ float red_signed(float x, float n, float inv) {
+        return fmaf(-rintf(x * inv), n, x);
     }
     __device__ static __forceinline__ float fma_(float a, float b, float c) { return fmaf(a, b, c); }
 };
@@ -88,10 +100,19 @@ __global__ void __launch_bounds__(256) k_matmul_plain(int64_t m, int64_t n, int6
 #pragma unroll
                 for (int j = 0; j < 4; j++) acc[i][j] = FMod<T>::fma_(a[i], b[j], acc[i][j]);
             if (++cnt == stripe) {
+                if (stripe == 1) {
+                    // one product per stripe (N near the type's limit): the accumulators stay
+                    // in (-N, N), so acc + a b stays below (N-1)^2 + N, exact
 #pragma unroll
-                for (int i = 0; i < 4; i++)
+                    for (int i = 0; i < 4; i++)
 #pragma unroll
-                    for (int j = 0; j < 4; j++) acc[i][j] = FMod<T>::red(acc[i][j], Nt, inv);
+                        for (int j = 0; j < 4; j++) acc[i][j] = FMod<T>::red_signed(acc[i][j], Nt, inv);
+                } else {
+#pragma unroll
+                    for (int i = 0; i < 4; i++)
+#pragma unroll
+                        for (int j = 0; j < 4; j++) acc[i][j] = FMod<T>::red(acc[i][j], Nt, inv);
+                }
                 cnt = 0;
             }
         }
@@ -104,7 +125,7 @@ __global__ void __launch_bounds__(256) k_matmul_plain(int64_t m, int64_t n, int6
 #pragma unroll
         for (int i = 0; i < 4; i++) {
             int64_t gr = r0 + tx + 16 * i;
-            if (gr < m) C[gr + gc * ldc] = FMod<T>::red(acc[i][j], Nt, inv);
+            if (gr < m) C[gr + gc * ldc] = FMod<T>::red(acc[i][j], Nt, inv);   // also for acc in (-N, 0)
         }
     }
 }

@@ -392,27 +392,35 @@ def test_limb_gemm_forms_match_oracle(gffm, N, shape, form):
 @pytest.mark.parametrize("N", [8388593, P26])
 def test_karatsuba_form_f32_storage_and_workspace(gffm, N):
     """The Karatsuba form through the Float32 entry point (N < 2^24 only) and with a caller
-    workspace of exactly the queried size."""
+    workspace of exactly the queried size; a tune table entry selects the form (the
+    Float32 entry point takes no tuning argument)."""
     import ctypes
+    from gffm import autotune
     rng = np.random.default_rng(N)
     m, n, k = 190, 250, 3000
     A, B = rng.integers(0, N, size=(m, k)), rng.integers(0, N, size=(k, n))
     L = gffm.load_library()
-    ws = ctypes.c_size_t(0)
-    assert L.gffm_matmul_limb_workspace_size(m, n, k, N, ctypes.byref(ws)) == 0
-    # six planes of 128-row padded A and B digits
-    assert ws.value == 6 * 2 * (256 + 256) * 3008
-    buf = torch.empty(ws.value, dtype=torch.uint8, device="cuda")
-    for dt, sfx in ((torch.float64, "f64"), (torch.float32, "f32")):
-        if dt == torch.float32 and N >= 2 ** 24:
-            continue
-        Ag = gffm.CuModMatrix(A, N, elem_type=dt)
-        Bg = gffm.CuModMatrix(B, N, elem_type=dt)
-        C = gffm.zeros(dt, m, n, N)
-        st = getattr(L, "gffm_matmul_limb_" + sfx)(m, n, k, Ag.data.data_ptr(), Ag.ld, Bg.data.data_ptr(), Bg.ld,
-                                                  C.data.data_ptr(), C.ld, N, buf.data_ptr(), ws.value, None)
-        assert st == 0
-        assert np.array_equal(as_int(C), oracle.matmul(A, B, N))
+    table = {"gemm": [{"N_lo": 2080640, "N_hi": 2 ** 26 - 1, "work_lo": 0, "work_hi": 1e30, "digit_bits": 7,
+                       "form": 2}], "batched": {}}
+    try:
+        assert autotune.apply(table) == 1
+        ws = ctypes.c_size_t(0)
+        assert L.gffm_matmul_limb_workspace_size(m, n, k, N, ctypes.byref(ws)) == 0
+        # six planes of 128-row padded A and B digits
+        assert ws.value == 6 * 2 * (256 + 256) * 3008
+        buf = torch.empty(ws.value, dtype=torch.uint8, device="cuda")
+        for dt, sfx in ((torch.float64, "f64"), (torch.float32, "f32")):
+            if dt == torch.float32 and N >= 2 ** 24:
+                continue
+            Ag = gffm.CuModMatrix(A, N, elem_type=dt)
+            Bg = gffm.CuModMatrix(B, N, elem_type=dt)
+            C = gffm.zeros(dt, m, n, N)
+            st = getattr(L, "gffm_matmul_limb_" + sfx)(m, n, k, Ag.data.data_ptr(), Ag.ld, Bg.data.data_ptr(), Bg.ld,
+                                                      C.data.data_ptr(), C.ld, N, buf.data_ptr(), ws.value, None)
+            assert st == 0
+            assert np.array_equal(as_int(C), oracle.matmul(A, B, N))
+    finally:
+        autotune.apply()                                  # back to the shipped table
     status_ok(gffm)
 
 
