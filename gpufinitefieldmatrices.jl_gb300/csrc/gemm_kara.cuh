@@ -338,10 +338,11 @@ __device__ __forceinline__ void digits6(int32_t c, __half (&d)[PLANES]) {
     d[5] = __int2half_rn(a1 + a3);
 }
 
-// A (m x k, column-major, lda) -> planes D[pl][r][kk] (K-major, Mpad x Kpad per plane)
-template <typename T>
-__global__ void __launch_bounds__(256) k_split_a6(const T *__restrict__ A, int64_t lda, int m, int k,
-                                                  __half *__restrict__ D, int Mpad, int Kpad, limb::ModN M) {
+// A (m x k, column-major, lda) -> planes D[pl][r][kk] (K-major, Mpad x Kpad per plane); MODE is
+// limb::SPLIT_CENTRED, or limb::SPLIT_SUM for the centred (A + A2) mod N
+template <typename T, int MODE>
+__global__ void __launch_bounds__(256) k_split_a6(const T *__restrict__ A, const T *__restrict__ A2, int64_t lda, int m,
+                                                  int k, __half *__restrict__ D, int Mpad, int Kpad, limb::ModN M) {
     __shared__ int32_t tile[32][33];
     const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
     const int64_t r0 = (int64_t)blockIdx.y * 32, k0 = (int64_t)blockIdx.x * 32;
@@ -349,7 +350,10 @@ __global__ void __launch_bounds__(256) k_split_a6(const T *__restrict__ A, int64
     for (int i = 0; i < 4; i++) {
         const int64_t kk = k0 + ty + 8 * i, r = r0 + tx;
         int32_t v = 0;
-        if (r < m && kk < k) v = limb::split_value<limb::SPLIT_CENTRED>(A[r + kk * lda], T(0), M);
+        if (r < m && kk < k) {
+            const int64_t off = r + kk * lda;
+            v = limb::split_value<MODE>(A[off], MODE == limb::SPLIT_SUM ? A2[off] : T(0), M);
+        }
         tile[ty + 8 * i][tx] = v;
     }
     __syncthreads();
@@ -365,17 +369,18 @@ __global__ void __launch_bounds__(256) k_split_a6(const T *__restrict__ A, int64
 }
 
 // B (k x n, column-major, ldb) -> planes D[pl][c][kk] (K-major, Npad x Kpad per plane); two k per thread
-template <typename T>
-__global__ void __launch_bounds__(256) k_split_b6(const T *__restrict__ B, int64_t ldb, int k, int n,
-                                                  __half *__restrict__ D, int Npad, int Kpad, limb::ModN M) {
+template <typename T, int MODE>
+__global__ void __launch_bounds__(256) k_split_b6(const T *__restrict__ B, const T *__restrict__ B2, int64_t ldb, int k,
+                                                  int n, __half *__restrict__ D, int Npad, int Kpad, limb::ModN M) {
     const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int64_t pairs_per_col = Kpad / 2;
     if (idx >= pairs_per_col * Npad) return;
     const int64_t c = idx / pairs_per_col;
     const int64_t kk = (idx - c * pairs_per_col) * 2;
     const int64_t off = kk + c * ldb;
-    const int32_t v0 = (c < n && kk < k) ? limb::split_value<limb::SPLIT_CENTRED>(B[off], T(0), M) : 0;
-    const int32_t v1 = (c < n && kk + 1 < k) ? limb::split_value<limb::SPLIT_CENTRED>(B[off + 1], T(0), M) : 0;
+    const bool sum = MODE == limb::SPLIT_SUM;
+    const int32_t v0 = (c < n && kk < k) ? limb::split_value<MODE>(B[off], sum ? B2[off] : T(0), M) : 0;
+    const int32_t v1 = (c < n && kk + 1 < k) ? limb::split_value<MODE>(B[off + 1], sum ? B2[off + 1] : T(0), M) : 0;
     __half d0[PLANES], d1[PLANES];
     digits6(v0, d0);
     digits6(v1, d1);

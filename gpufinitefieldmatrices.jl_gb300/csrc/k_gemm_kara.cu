@@ -20,20 +20,28 @@ Layout layout(int64_t m, int64_t n, int64_t k) {
 }
 
 template <typename T>
-int split_a(const T *A, int64_t lda, int64_t m, int64_t k, __half *D, const Layout &g, int64_t N, cudaStream_t s) {
+int split_a(const T *A, int64_t lda, int64_t m, int64_t k, __half *D, const Layout &g, int64_t N, cudaStream_t s,
+            const T *A2) {
     limb::ModN M{N, ~uint64_t(0) / (uint64_t)N};
     dim3 grid((unsigned)(g.Kpad / 32), (unsigned)(g.Mpad / 32));
-    k_split_a6<T><<<grid, 256, 0, s>>>(A, lda, (int)m, (int)k, D, (int)g.Mpad, (int)g.Kpad, M);
+    if (A2)
+        k_split_a6<T, limb::SPLIT_SUM><<<grid, 256, 0, s>>>(A, A2, lda, (int)m, (int)k, D, (int)g.Mpad, (int)g.Kpad, M);
+    else
+        k_split_a6<T, limb::SPLIT_CENTRED><<<grid, 256, 0, s>>>(A, A, lda, (int)m, (int)k, D, (int)g.Mpad, (int)g.Kpad, M);
     GFFM_LAUNCH_CHECK("k_split_a6");
     return GFFM_OK;
 }
 
 template <typename T>
-int split_b(const T *B, int64_t ldb, int64_t k, int64_t n, __half *D, const Layout &g, int64_t N, cudaStream_t s) {
+int split_b(const T *B, int64_t ldb, int64_t k, int64_t n, __half *D, const Layout &g, int64_t N, cudaStream_t s,
+            const T *B2) {
     limb::ModN M{N, ~uint64_t(0) / (uint64_t)N};
     const int64_t total = (g.Kpad / 2) * g.Npad;
-    k_split_b6<T><<<(unsigned)((total + 255) / 256), 256, 0, s>>>(B, ldb, (int)k, (int)n, D, (int)g.Npad,
-                                                                    (int)g.Kpad, M);
+    const unsigned blocks = (unsigned)((total + 255) / 256);
+    if (B2)
+        k_split_b6<T, limb::SPLIT_SUM><<<blocks, 256, 0, s>>>(B, B2, ldb, (int)k, (int)n, D, (int)g.Npad, (int)g.Kpad, M);
+    else
+        k_split_b6<T, limb::SPLIT_CENTRED><<<blocks, 256, 0, s>>>(B, B, ldb, (int)k, (int)n, D, (int)g.Npad, (int)g.Kpad, M);
     GFFM_LAUNCH_CHECK("k_split_b6");
     return GFFM_OK;
 }
@@ -105,14 +113,16 @@ int gemm_digits(const Layout &g, const __half *Ad, const __half *Bd, int64_t m, 
 }
 
 template int split_a<double>(const double *, int64_t, int64_t, int64_t, __half *, const Layout &, int64_t,
-                             cudaStream_t);
-template int split_a<float>(const float *, int64_t, int64_t, int64_t, __half *, const Layout &, int64_t, cudaStream_t);
+                             cudaStream_t, const double *);
+template int split_a<float>(const float *, int64_t, int64_t, int64_t, __half *, const Layout &, int64_t, cudaStream_t,
+                            const float *);
 template int split_a<int32_t>(const int32_t *, int64_t, int64_t, int64_t, __half *, const Layout &, int64_t,
-                              cudaStream_t);
+                              cudaStream_t, const int32_t *);
 template int split_b<double>(const double *, int64_t, int64_t, int64_t, __half *, const Layout &, int64_t,
-                             cudaStream_t);
-template int split_b<float>(const float *, int64_t, int64_t, int64_t, __half *, const Layout &, int64_t, cudaStream_t);
+                             cudaStream_t, const double *);
+template int split_b<float>(const float *, int64_t, int64_t, int64_t, __half *, const Layout &, int64_t, cudaStream_t,
+                            const float *);
 template int split_b<int32_t>(const int32_t *, int64_t, int64_t, int64_t, __half *, const Layout &, int64_t,
-                              cudaStream_t);
+                              cudaStream_t, const int32_t *);
 
 }  // namespace kara

@@ -28,6 +28,7 @@
 // KaratsubaKernels.jl:2-125) work on the value x exactly: one HBM pass, the
 // digits recovered with a Barrett quotient by N1.
 #include "gffm_common.cuh"
+#include "kara_host.h"
 #include "limb_host.h"
 
 namespace {
@@ -197,8 +198,16 @@ int check_mm(int64_t m, int64_t n, int64_t k, int64_t lda, int64_t ldb, int64_t 
     return GFFM_OK;
 }
 
+// The products mod a single modulus below 2^26 take the limb GEMM's Karatsuba digit form
+// (kara_host.h) where it applies, as gffm_matmul_limb_f64 does by default.
+bool kara_form(int64_t N, int64_t k) {
+    return limb::resolve_form(limb::FORM_DEFAULT, 7, 64, N, k) == limb::FORM_KARATSUBA;
+}
+
 struct KaraLayout {
     limb::Layout exact, modn2;
+    kara::Layout kmodn2;
+    bool kform = false;   // the mod-N2 products in the Karatsuba digit form
     size_t da, db, s1;    // digit buffers for A and B, the int64 S1' matrix
     size_t total() const { return da + db + s1; }
 };
@@ -207,10 +216,34 @@ KaraLayout kara_layout(int64_t m, int64_t n, int64_t k, int64_t N1, int64_t N2) 
     KaraLayout kl;
     kl.exact = limb::layout_L(m, n, k, limb::raw_limbs_for(N1));
     kl.modn2 = limb::layout(m, n, k, N2);
-    kl.da = gffm::round_up((int64_t)(kl.exact.a_bytes > kl.modn2.a_bytes ? kl.exact.a_bytes : kl.modn2.a_bytes), 256);
-    kl.db = gffm::round_up((int64_t)(kl.exact.b_bytes > kl.modn2.b_bytes ? kl.exact.b_bytes : kl.modn2.b_bytes), 256);
+    kl.kmodn2 = kara::layout(m, n, k);
+    kl.kform = N2 < (int64_t(1) << 26) && kara_form(N2, k);
+    const size_t a2 = kl.kform ? kl.kmodn2.a_bytes : kl.modn2.a_bytes;
+    const size_t b2 = kl.kform ? kl.kmodn2.b_bytes : kl.modn2.b_bytes;
+    kl.da = gffm::round_up((int64_t)(kl.exact.a_bytes > a2 ? kl.exact.a_bytes : a2), 256);
+    kl.db = gffm::round_up((int64_t)(kl.exact.b_bytes > b2 ? kl.exact.b_bytes : b2), 256);
     kl.s1 = (size_t)(m > 0 ? m : 1) * (size_t)(n > 0 ? n : 1) * 8;
     return kl;
+}
+
+// C (ldc) = A B mod N (Float64), A = the residues of X, or of (X + X2) mod N with X2; the
+// digit planes in dA / dB; the Karatsuba digit form when `kform`
+int product(bool kform, const limb::Layout &g, const kara::Layout &kg, const double *X, const double *X2,
+            int64_t lda, const double *Y, const double *Y2, int64_t ldb, int64_t m, int64_t n, int64_t k, int64_t N,
+            __half *dA, __half *dB, double *C, int64_t ldc, int epi, cudaStream_t s, const double *S0 = nullptr,
+            const double *S2 = nullptr) {
+    int st;
+    if (kform) {
+        st = kara::split_a<double>(X, lda, m, k, dA, kg, N, s, X2);
+        if (!st) st = kara::split_b<double>(Y, ldb, k, n, dB, kg, N, s, Y2);
+        if (!st) st = kara::gemm_digits(kg, dA, dB, m, n, k, N, C, ldc, epi, 0, s, S0, S2);
+        return st;
+    }
+    const int mode = X2 ? limb::SPLIT_SUM : limb::SPLIT_CENTRED;
+    st = limb::split_a<double>(X, lda, m, k, dA, g, N, s, mode, X2);
+    if (!st) st = limb::split_b<double>(Y, ldb, k, n, dB, g, N, s, mode, Y2);
+    if (!st) st = limb::gemm_digits(g, dA, dB, m, n, k, N, C, ldc, epi, 0, s, S0, S2);
+    return st;
 }
 
 int kara_matmul(int64_t m, int64_t n, int64_t k, const double *A1, const double *A2, int64_t lda, const double *B1,
@@ -249,13 +282,13 @@ int kara_matmul(int64_t m, int64_t n, int64_t k, const double *A1, const double 
     if (!st) st = limb::split_b<double>(B1, ldb, k, n, dB, kl.exact, N1, s, limb::SPLIT_RAW);
     if (!st) st = limb::gemm_digits(kl.exact, dA, dB, m, n, k, M12, S1, m, limb::EPI_EXACT_I64, 0, s);
     // S2 = (A1 + A2)(B1 + B2) mod N2 -> C2
-    if (!st) st = limb::split_a<double>(A1, lda, m, k, dA, kl.modn2, N2, s, limb::SPLIT_SUM, A2);
-    if (!st) st = limb::split_b<double>(B1, ldb, k, n, dB, kl.modn2, N2, s, limb::SPLIT_SUM, B2);
-    if (!st) st = limb::gemm_digits(kl.modn2, dA, dB, m, n, k, N2, C2, ldc, limb::EPI_STORE_F64, 0, s);
+    if (!st)
+        st = product(kl.kform, kl.modn2, kl.kmodn2, A1, A2, lda, B1, B2, ldb, m, n, k, N2, dA, dB, C2, ldc,
+                     limb::EPI_STORE_F64, s);
     // S3 = A2 B2 mod N2 -> C1
-    if (!st) st = limb::split_a<double>(A2, lda, m, k, dA, kl.modn2, N2, s);
-    if (!st) st = limb::split_b<double>(B2, ldb, k, n, dB, kl.modn2, N2, s);
-    if (!st) st = limb::gemm_digits(kl.modn2, dA, dB, m, n, k, N2, C1, ldc, limb::EPI_STORE_F64, 0, s);
+    if (!st)
+        st = product(kl.kform, kl.modn2, kl.kmodn2, A2, nullptr, lda, B2, nullptr, ldb, m, n, k, N2, dA, dB, C1, ldc,
+                     limb::EPI_STORE_F64, s);
     if (st) return st;
     const int row_blocks = (int)((m + 255) / 256);
     k_kara_combine<<<(unsigned)(row_blocks * n), 256, 0, s>>>(C1, C2, ldc, S1, m, (int)m, (int)n, row_blocks,
@@ -287,22 +320,22 @@ int poly_matmul(int64_t m, int64_t n, int64_t k, const double *A0, const double 
         for (double *C : {C0, C1, C2}) GFFM_CUDA(cudaMemset2DAsync(C, (size_t)ldc * 8, 0, (size_t)m * 8, (size_t)n, s));
         return GFFM_OK;
     }
-    limb::Layout g = limb::layout(m, n, k, p);
-    const size_t da = gffm::round_up((int64_t)g.a_bytes, 256);
+    const limb::Layout g = limb::layout(m, n, k, p);
+    const kara::Layout kg = kara::layout(m, n, k);
+    const bool kform = kara_form(p, k);
+    const size_t da = gffm::round_up((int64_t)(kform ? kg.a_bytes : g.a_bytes), 256);
     Scratch scr;
-    st = scr.acquire(ws, ws_bytes, da + g.b_bytes, s);
+    st = scr.acquire(ws, ws_bytes, da + (kform ? kg.b_bytes : g.b_bytes), s);
     if (st) return st;
     __half *dA = static_cast<__half *>(scr.ptr);
     __half *dB = reinterpret_cast<__half *>(static_cast<uint8_t *>(scr.ptr) + da);
-    st = limb::split_a<double>(A0, lda, m, k, dA, g, p, s);
-    if (!st) st = limb::split_b<double>(B0, ldb, k, n, dB, g, p, s);
-    if (!st) st = limb::gemm_digits(g, dA, dB, m, n, k, p, C0, ldc, limb::EPI_STORE_F64, 0, s);
-    if (!st) st = limb::split_a<double>(A1, lda, m, k, dA, g, p, s);
-    if (!st) st = limb::split_b<double>(B1, ldb, k, n, dB, g, p, s);
-    if (!st) st = limb::gemm_digits(g, dA, dB, m, n, k, p, C2, ldc, limb::EPI_STORE_F64, 0, s);
-    if (!st) st = limb::split_a<double>(A0, lda, m, k, dA, g, p, s, limb::SPLIT_SUM, A1);
-    if (!st) st = limb::split_b<double>(B0, ldb, k, n, dB, g, p, s, limb::SPLIT_SUM, B1);
-    if (!st) st = limb::gemm_digits(g, dA, dB, m, n, k, p, C1, ldc, limb::EPI_KSUB_F64, 0, s, C0, C2);
+    st = product(kform, g, kg, A0, nullptr, lda, B0, nullptr, ldb, m, n, k, p, dA, dB, C0, ldc, limb::EPI_STORE_F64, s);
+    if (!st)
+        st = product(kform, g, kg, A1, nullptr, lda, B1, nullptr, ldb, m, n, k, p, dA, dB, C2, ldc, limb::EPI_STORE_F64,
+                     s);
+    if (!st)
+        st = product(kform, g, kg, A0, A1, lda, B0, B1, ldb, m, n, k, p, dA, dB, C1, ldc, limb::EPI_KSUB_F64, s, C0,
+                     C2);
     return st;
 }
 
@@ -330,8 +363,12 @@ int gffm_karatsuba_poly_workspace_size(int64_t m, int64_t n, int64_t k, int64_t 
     if (!bytes) return set_error(GFFM_ERR_ARG, "bytes is NULL");
     int st = limb::check_args(m, n, k, m > 1 ? m : 1, k > 1 ? k : 1, m > 1 ? m : 1, p);
     if (st) return st;
-    limb::Layout g = limb::layout(m, n, k, p);
-    *bytes = (m == 0 || n == 0 || k == 0) ? 0 : gffm::round_up((int64_t)g.a_bytes, 256) + g.b_bytes;
+    const limb::Layout g = limb::layout(m, n, k, p);
+    const kara::Layout kg = kara::layout(m, n, k);
+    const bool kform = kara_form(p, k);
+    *bytes = (m == 0 || n == 0 || k == 0) ? 0
+                                           : gffm::round_up((int64_t)(kform ? kg.a_bytes : g.a_bytes), 256) +
+                                                 (kform ? kg.b_bytes : g.b_bytes);
     return GFFM_OK;
 }
 

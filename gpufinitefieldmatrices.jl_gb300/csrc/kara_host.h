@@ -19,10 +19,14 @@ struct Layout {
 bool applies(int64_t N);
 Layout layout(int64_t m, int64_t n, int64_t k);
 
+// six digit planes of A (m x k) / B (k x n), column-major inputs of type T: the centred residues, or
+// with A2 / B2 (Float64 only) the centred (A + A2) mod N, the Karatsuba sum of two operands
 template <typename T>
-int split_a(const T *A, int64_t lda, int64_t m, int64_t k, __half *D, const Layout &g, int64_t N, cudaStream_t s);
+int split_a(const T *A, int64_t lda, int64_t m, int64_t k, __half *D, const Layout &g, int64_t N, cudaStream_t s,
+            const T *A2 = nullptr);
 template <typename T>
-int split_b(const T *B, int64_t ldb, int64_t k, int64_t n, __half *D, const Layout &g, int64_t N, cudaStream_t s);
+int split_b(const T *B, int64_t ldb, int64_t k, int64_t n, __half *D, const Layout &g, int64_t N, cudaStream_t s,
+            const T *B2 = nullptr);
 
 // C (m x n, ldc) <- epilogue(A*B mod N) from the six-plane digit arrays; epi is limb::EPI_STORE_F64 /
 // EPI_STORE_F32 / EPI_STORE_I32 / EPI_KSUB_F64 (X, Y: the subtrahends of the last one).
