@@ -81,13 +81,13 @@ def _time(fn, reps):
     return e0.elapsed_time(e1) / reps
 
 
-def time_gemm(m, n, k, N, digit_bits, max_ctas=0, reps=5, generator=None, tile_n=0):
+def time_gemm(m, n, k, N, digit_bits, max_ctas=0, reps=5, generator=None, tile_n=0, form=0):
     """Milliseconds of one C = A*B mod N (resident Float64 operands) with a given tuning."""
     from .cumod import rand, zeros
     A = rand(torch.float64, m, k, N, generator=generator)
     B = rand(torch.float64, k, n, N, generator=generator)
     C = zeros(torch.float64, m, n, N)
-    tu = _LimbTuning(digit_bits, max_ctas, tile_n, 0)
+    tu = _LimbTuning(digit_bits, max_ctas, tile_n, form)
     ws = ctypes.c_size_t(0)
     call("gffm_matmul_limb_tuned_workspace_size", m, n, k, N, ctypes.byref(tu), ctypes.byref(ws))
     buf = torch.empty(max(1, ws.value), dtype=torch.uint8, device="cuda")
@@ -100,10 +100,16 @@ def time_gemm(m, n, k, N, digit_bits, max_ctas=0, reps=5, generator=None, tile_n
     return _time(run, reps)
 
 
+# moduli of four 7-bit digits where the Karatsuba form applies (kara_host.h), beyond the
+# ranges where 8-bit digits save a digit
+KARA_RANGE = (16711424, 2 ** 26 - 1)
+
+
 def tune_gemm(shapes=((512, 512, 512), (2048, 2048, 2048), (8192, 8192, 8192)),
-              moduli=(32749, 8388593), reps=5):
-    """For each modulus (one per range where 8-bit digits save a digit) and size,
-    time 7- and 8-bit digits and a few grid sizes; return table entries covering
+              moduli=(32749, 8388593, 67108859), reps=5):
+    """For each modulus (one per range where 8-bit digits save a digit, and one where only
+    the Karatsuba form saves products) and size, time 7- and 8-bit schoolbook digits, the
+    Karatsuba form where it applies, and a few grid sizes; return table entries covering
     each modulus range over a work range around each size."""
     sms = torch.cuda.get_device_properties(0).multi_processor_count
     g = torch.Generator(device="cuda")
@@ -111,23 +117,26 @@ def tune_gemm(shapes=((512, 512, 512), (2048, 2048, 2048), (8192, 8192, 8192)),
     entries, log = [], []
     works = sorted(m * n * k for (m, n, k) in shapes)
     for N in moduli:
-        rng = next(((lo, hi) for lo, hi in BITS8_RANGES if lo <= N <= hi), (N, N))
+        rng = next(((lo, hi) for lo, hi in BITS8_RANGES + [KARA_RANGE] if lo <= N <= hi), (N, N))
+        kara = 2080639 < N < 2 ** 26
         for (m, n, k) in shapes:
             best = None
-            for bits in (7, 8):
-                for ctas in (0, sms // 2):
-                    for tile_n in (64, 32):
-                        t = time_gemm(m, n, k, N, bits, ctas, reps, g, tile_n)
-                        log.append({"N": N, "m": m, "n": n, "k": k, "digit_bits": bits, "max_ctas": ctas,
-                                    "tile_n": tile_n, "ms": round(t, 4)})
-                        if best is None or t < best[0]:
-                            best = (t, bits, ctas, tile_n)
+            cands = [(bits, ctas, tile_n, 1) for bits in (7, 8) for ctas in (0, sms // 2) for tile_n in (64, 32)]
+            if kara:
+                cands += [(7, ctas, 64, 2) for ctas in (0, sms // 2)]
+            for bits, ctas, tile_n, form in cands:
+                t = time_gemm(m, n, k, N, bits, ctas, reps, g, tile_n, form)
+                log.append({"N": N, "m": m, "n": n, "k": k, "digit_bits": bits, "max_ctas": ctas,
+                            "tile_n": tile_n, "form": form, "ms": round(t, 4)})
+                if best is None or t < best[0]:
+                    best = (t, bits, ctas, tile_n, form)
             w = m * n * k
             i = works.index(w)
             lo = 0.0 if i == 0 else (works[i - 1] * w) ** 0.5
             hi = 1e30 if i == len(works) - 1 else (works[i + 1] * w) ** 0.5
             entries.append({"N_lo": rng[0], "N_hi": rng[1], "work_lo": lo, "work_hi": hi,
-                            "digit_bits": best[1], "max_ctas": best[2], "tile_n": best[3], "tuned_on": [m, n, k, N],
+                            "digit_bits": best[1], "max_ctas": best[2], "tile_n": best[3], "form": best[4],
+                            "tuned_on": [m, n, k, N],
                             "ms": round(best[0], 4)})
     return entries, log
 
@@ -182,11 +191,19 @@ def main():
     ap.add_argument("--out", default=TABLE)
     ap.add_argument("--batch", type=int, default=4096)
     ap.add_argument("--log", default=None)
+    ap.add_argument("--gemm-only", action="store_true", help="retune the GEMM entries, keep the batched ones")
     args = ap.parse_args()
     load()
     table = load_table(args.out)
     entries, glog = tune_gemm()
     table["gemm"] = entries
+    if args.gemm_only:
+        save_table(table, args.out)
+        if args.log:
+            with open(args.log, "w") as f:
+                json.dump({"gemm": glog}, f, indent=1)
+        print(json.dumps({"gemm": entries}))
+        return
     from . import batched
     specs = batched.config4_specs(args.batch, seed=1234)
     g = torch.Generator(device="cuda")
