@@ -37,6 +37,14 @@
 // 2^24.  After each chunk the epilogue drains the three accumulators into
 // int64 registers, exactly as the schoolbook kernel (gemm_limb.cuh) does.
 //
+// Accumulator slots.  TMEM's 512 columns are four 128-column slots; exact
+// chunk g keeps its shifts 0, 1, 2 in slots (g & 1) + 0, 1, 2, so consecutive
+// chunks share two slots and each has one of its own.  The epilogue drains the
+// shared slots first and frees each slot on its own barrier, and the mma
+// issuer waits for a slot only before its first write of the chunk: the next
+// chunk's mma's start once two of the previous chunk's three accumulators are
+// drained, and the third drain runs beside them.
+//
 // Warp roles (576 threads): warp 0 TMA producer, warp 1 TMEM allocator and
 // single-thread mma issuer, warps 2..17 the epilogue (four per TMEM lane
 // quadrant, 32 of the 128 columns each).  Every wait is bounded; on timeout
@@ -58,7 +66,7 @@ constexpr int STAGES = 3;
 constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024;
 constexpr int EPI_WARPS = 16;
 constexpr int THREADS = 64 + 32 * EPI_WARPS;
-constexpr int TMEM_COLS = 512;           // three 128-column shift accumulators (384), allocated as 512
+constexpr int TMEM_COLS = 512;           // four 128-column slots: a chunk's three shift accumulators at slot 0 or 1
 static_assert(SMEM_BYTES <= 227 * 1024, "stages exceed shared memory");
 
 struct Params {
@@ -88,7 +96,7 @@ __global__ void __launch_bounds__(THREADS, 1)
     extern __shared__ uint8_t dsmem_raw[];
     __shared__ uint64_t full_bar[STAGES];
     __shared__ uint64_t empty_bar[STAGES];
-    __shared__ uint64_t acc_full_bar, acc_empty_bar, drain_bar;
+    __shared__ uint64_t acc_full_bar, slot_free_bar[4], drain_bar;
     __shared__ uint32_t tmem_base_s;
     __shared__ int abort_sh;
     volatile int &abort_s = abort_sh;
@@ -104,7 +112,7 @@ __global__ void __launch_bounds__(THREADS, 1)
             gffm_dev::mbar_init(&empty_bar[s], 1);
         }
         gffm_dev::mbar_init(&acc_full_bar, 1);
-        gffm_dev::mbar_init(&acc_empty_bar, EPI_WARPS);
+        for (int q = 0; q < 4; q++) gffm_dev::mbar_init(&slot_free_bar[q], EPI_WARPS);
         gffm_dev::mbar_init(&drain_bar, 1);
         abort_s = 0;
         gffm_dev::fence_mbar_init();
@@ -163,21 +171,32 @@ __global__ void __launch_bounds__(THREADS, 1)
         // ---------------- MMA issuer ----------------
         if (lane == 0) {
             int stage = 0;
-            uint32_t phase = 0, acc_phase = 0;
+            uint32_t phase = 0;
             bool issued_any = false;
             const uint32_t idesc_wide = gffm_dev::idesc_f16_f32(BM, 2 * BN);
             const uint32_t idesc_one = gffm_dev::idesc_f16_f32(BM, BN);
+            // before chunk g's first write of slot q: the slot's previous chunk is drained.  Slots
+            // 1 and 2 serve every chunk, slot 0 the even chunks, slot 3 the odd ones, so the
+            // chunks before g that used slot q are g, g / 2 or (g - 1) / 2, and the slot's
+            // barrier has completed one phase per drained use.
+            auto claim = [&](int q, int g) {
+                const int prior = (q == 1 || q == 2) ? g : (q == 0 ? g >> 1 : (g - 1) >> 1);
+                if (prior > 0 && !gffm_dev::mbar_wait(&slot_free_bar[q], (uint32_t)(prior - 1) & 1)) {
+                    atomicOr(p.err, 2);
+                    abort_s = 1;
+                    return false;
+                }
+                gffm_dev::tc_fence_after();
+                return true;
+            };
+            int g = 0;   // chunk counter: the slot base alternates
             for (int t = blockIdx.x; t < ntiles_total && !abort_s; t += gridDim.x) {
                 for (int prod = 0; prod < 3 && !abort_s; prod++) {
                     const int ckb = p.chunk_kb[prod];
-                    for (int kb0 = 0; kb0 < p.kblocks && !abort_s; kb0 += ckb) {
+                    for (int kb0 = 0; kb0 < p.kblocks && !abort_s; kb0 += ckb, g++) {
                         const int kb1 = kb0 + ckb < p.kblocks ? kb0 + ckb : p.kblocks;
-                        if (!gffm_dev::mbar_wait(&acc_empty_bar, acc_phase ^ 1)) {
-                            atomicOr(p.err, 2);
-                            abort_s = 1;
-                            break;
-                        }
-                        gffm_dev::tc_fence_after();
+                        const int sb = g & 1;   // slot of this chunk's shift 0
+                        const uint32_t acc = tmem + (uint32_t)(BN * sb);
                         for (int kb = kb0; kb < kb1; kb++) {
                             if (!gffm_dev::mbar_wait(&full_bar[stage], phase)) {
                                 atomicOr(p.err, 4);
@@ -186,23 +205,27 @@ __global__ void __launch_bounds__(THREADS, 1)
                             }
                             gffm_dev::tc_fence_after();
                             const uint32_t sa = gffm_dev::smem_u32(smem + stage * STAGE_BYTES);
-                            const uint32_t sb = sa + 2 * TILE;
+                            const uint32_t sbb = sa + 2 * TILE;
 #pragma unroll
                             for (int kk = 0; kk < BK / 16; kk++) {
-                                const uint64_t bdesc = gffm_dev::umma_desc_sw128(sb + kk * 32);
+                                const uint64_t bdesc = gffm_dev::umma_desc_sw128(sbb + kk * 32);
                                 const uint64_t a0 = gffm_dev::umma_desc_sw128(sa + kk * 32);
                                 const uint64_t a1 = gffm_dev::umma_desc_sw128(sa + TILE + kk * 32);
                                 if (kb == kb0 && kk == 0) {
-                                    // first k-step of a chunk: initialise the three shift accumulators once
-                                    gffm_dev::mma_f16(tmem, a0, bdesc, idesc_wide, 0);
-                                    gffm_dev::mma_f16(tmem + BN, a1, bdesc, idesc_one, 1);
-                                    gffm_dev::mma_f16(tmem + 2 * BN, a1, gffm_dev::umma_desc_sw128(sb + TILE + kk * 32),
+                                    // first k-step of a chunk: initialise the three shift accumulators
+                                    // once, each slot claimed just before its first write
+                                    if (!claim(sb, g) || !claim(sb + 1, g)) break;
+                                    gffm_dev::mma_f16(acc, a0, bdesc, idesc_wide, 0);
+                                    gffm_dev::mma_f16(acc + BN, a1, bdesc, idesc_one, 1);
+                                    if (!claim(sb + 2, g)) break;
+                                    gffm_dev::mma_f16(acc + 2 * BN, a1, gffm_dev::umma_desc_sw128(sbb + TILE + kk * 32),
                                                       idesc_one, 0);
                                 } else {
-                                    gffm_dev::mma_f16(tmem, a0, bdesc, idesc_wide, 1);
-                                    gffm_dev::mma_f16(tmem + BN, a1, bdesc, idesc_wide, 1);
+                                    gffm_dev::mma_f16(acc, a0, bdesc, idesc_wide, 1);
+                                    gffm_dev::mma_f16(acc + BN, a1, bdesc, idesc_wide, 1);
                                 }
                             }
+                            if (abort_s) break;
                             issued_any = true;
                             gffm_dev::mma_commit(&empty_bar[stage]);
                             if (++stage == STAGES) {
@@ -212,7 +235,6 @@ __global__ void __launch_bounds__(THREADS, 1)
                         }
                         if (abort_s) break;
                         gffm_dev::mma_commit(&acc_full_bar);
-                        acc_phase ^= 1;
                     }
                 }
             }
@@ -228,6 +250,7 @@ __global__ void __launch_bounds__(THREADS, 1)
         const int part = (warp - 2) >> 2;          // which 32 of the tile's 128 columns
         const uint32_t lane_base = (uint32_t)(quad * 32) << 16;
         uint32_t acc_phase = 0;
+        int g = 0;   // chunk counter, as the mma issuer's
         for (int t = blockIdx.x; t < ntiles_total; t += gridDim.x) {
             int tm, tn;
             tile_coords(t, p.mtiles, p.ntiles, tm, tn);
@@ -240,31 +263,42 @@ __global__ void __launch_bounds__(THREADS, 1)
             int chunk = 0;
             for (int prod = 0; prod < 3 && ok; prod++) {
                 const int ckb = p.chunk_kb[prod];
-                for (int kb0 = 0; kb0 < p.kblocks; kb0 += ckb, chunk++) {
+                for (int kb0 = 0; kb0 < p.kblocks; kb0 += ckb, chunk++, g++) {
                     if (!gffm_dev::mbar_wait(&acc_full_bar, acc_phase)) {
                         atomicOr(p.err, 8);
                         abort_s = 1;
                         ok = false;
                         break;
                     }
+                    acc_phase ^= 1;
                     gffm_dev::tc_fence_after();
-#pragma unroll
-                    for (int s = 0; s < 3; s++) {
+                    // shift s of this chunk sits in slot `slot`; once drained the slot is freed
+                    auto drain = [&](int s, int slot) {
                         const int w = p.W[prod][s];
 #pragma unroll
                         for (int h = 0; h < CW / 8; h++) {
                             uint32_t v[8];
-                            gffm_dev::tmem_ld_32x32b_x8(tmem + lane_base + BN * s + CW * part + 8 * h, v);
+                            gffm_dev::tmem_ld_32x32b_x8(tmem + lane_base + BN * slot + CW * part + 8 * h, v);
                             gffm_dev::tmem_ld_wait();
 #pragma unroll
                             for (int j = 0; j < 8; j++)
                                 acc[8 * h + j] += (int64_t)__float2int_rz(__uint_as_float(v[j])) * w;
                         }
+                        gffm_dev::tc_fence_before();
+                        __syncwarp();
+                        if (lane == 0) gffm_dev::mbar_arrive(&slot_free_bar[slot]);
+                    };
+                    // the slots the next chunk writes first are drained first: shifts 1, 2, 0 after a
+                    // chunk at slot 0, shifts 0, 1, 2 after a chunk at slot 1
+                    if ((g & 1) == 0) {
+                        drain(1, 1);
+                        drain(2, 2);
+                        drain(0, 0);
+                    } else {
+                        drain(0, 1);
+                        drain(1, 2);
+                        drain(2, 3);
                     }
-                    gffm_dev::tc_fence_before();
-                    __syncwarp();
-                    if (lane == 0) gffm_dev::mbar_arrive(&acc_empty_bar);
-                    acc_phase ^= 1;
                     // each chunk adds less than 3 * 2^50 in magnitude: reduce every 64 chunks
                     if ((chunk & 63) == 63) {
 #pragma unroll
