@@ -129,8 +129,9 @@ def measured_peaks():
 # GEMM kernel, from an ncu capture of the same kernel (one pass, -c 1,
 # --clock-control none); a benchmark run cannot read DRAM counters itself, so the
 # figure is reported with its source and is not measured in the run.
-GEMM_TRAFFIC = {"bytes": 1.1336e10, "source": "ncu dram__bytes_{read,write}.sum of a 4096^3 capture, scaled x8 "
-                                              "to 8192^3 (not measured in this run)"}
+GEMM_TRAFFIC = {"bytes": 9.425913088e9 + 5.21232384e8,
+                "source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of this benchmark's own 8192^3 "
+                          "k_gemm_kara launch (one pass, -c 1; not measured in this run)"}
 
 
 # ---------------------------------------------------------------------------
