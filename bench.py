@@ -56,6 +56,9 @@ def parse_args():
     ap.add_argument("--no-karatsuba", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--batch", type=int, default=4096, help="instances of the batched workload")
+    ap.add_argument("--batch-uniform", default=None, metavar="COUNTxN",
+                    help="with --only batched: COUNT seeded full-rank N x N PLUQ instances mod 67108859 instead of "
+                         "the mixed workload (a case for profiling the batched PLUQ kernel)")
     ap.add_argument("--only", default=None, choices=["gemm", "pluq", "karatsuba", "batched"],
                     help="run one leg alone and print its fields (for profiling; not the benchmark line)")
     ap.add_argument("--size", type=int, default=8192, help="m = n = k (8192 is the benchmark workload)")
@@ -132,6 +135,24 @@ def measured_peaks():
 GEMM_TRAFFIC = {"bytes": 9.425913088e9 + 5.21232384e8,
                 "source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of this benchmark's own 8192^3 "
                           "k_gemm_kara launch (one pass, -c 1; not measured in this run)"}
+
+
+# ---------------------------------------------------------------------------
+# replicas: one process per GPU, independent products, the slowest rank's time
+# ---------------------------------------------------------------------------
+def job_time_ms(ms, dist=None, dev="cpu"):
+    """The whole job's time: the slowest rank's, agreed on by every rank (max over ranks)."""
+    if dist is None:
+        return ms
+    import torch
+    t = torch.tensor([ms], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_rate_gops(ops_per_rank_step, steps, world, ms):
+    """Whole-job Gop/s: the work of every rank over the job's (slowest rank's) time."""
+    return ops_per_rank_step * steps * world / (ms / 1e3) / 1e9
 
 
 # ---------------------------------------------------------------------------
@@ -277,12 +298,9 @@ def run_ours(args):
     clk = clocks.stop()
     ms = e0.elapsed_time(e1)
     kern_ms = [a.elapsed_time(b) for a, b in kev]
-    if dist is not None:
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = job_time_ms(ms, dist, dev)
     ops_step = 2.0 * M * N * K
-    value = ops_step * args.steps * world / (ms / 1e3) / 1e9
+    value = job_rate_gops(ops_step, args.steps, world, ms)
     st = L.gffm_device_status(sp)
     if st != 0:
         raise RuntimeError("device status %d" % st)
@@ -391,12 +409,7 @@ def e2e_run(args, L, sp, dev, world, dist):
             fn()
         e1.record()
         torch.cuda.synchronize()
-        ms = e0.elapsed_time(e1)
-        if dist is not None:
-            t = torch.tensor([ms], device=dev)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            ms = float(t.item())
-        return ms
+        return job_time_ms(e0.elapsed_time(e1), dist, dev)
 
     steps = max(5, args.steps // 6)
     ms = timed(step, steps)
@@ -420,7 +433,7 @@ def e2e_run(args, L, sp, dev, world, dist):
     h2d = (M * K + K * N) * 8
     d2h = M * N * 8
     blocks = [(x + 2047) // 2048 for x in (M, N)]
-    gops = lambda t: round(2.0 * M * N * K * steps * world / (t / 1e3) / 1e9, 1)
+    gops = lambda t: round(job_rate_gops(2.0 * M * N * K, steps, world, t), 1)
     return {"value": gops(ms), "unit": "Gop/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
             "steps": steps, "ms_per_step": round(ms / steps, 3),
             "call": "gffm_matmul_host_f64 (%d x %d blocks)" % tuple(blocks),
@@ -697,7 +710,11 @@ def batched_run(args, dev, large_gemm_gops):
     import torch
     import gffm
     from gffm import batched
-    specs = batched.config4_specs(args.batch, seed=1234)
+    if args.batch_uniform:
+        count, n = (int(x) for x in args.batch_uniform.lower().split("x"))
+        specs = [("pluq", n, P26)] * count
+    else:
+        specs = batched.config4_specs(args.batch, seed=1234)
     g = torch.Generator(device=dev)
     g.manual_seed(1234)
     inst = batched.build_config4(specs, generator=g)
