@@ -7,8 +7,12 @@
 //     c  = lo + 2^13 hi,          lo in [-4096, 4095], |hi| <= 4096
 //     lo = a0 + 2^7 a1,           a0 in [-64, 63],     |a1| <= 32
 //     hi = a2 + 2^7 a3,           a2 in [-64, 63],     |a3| <= 32
-// plus the Karatsuba sums s0 = a0 + a2 in [-128, 126], s1 = a1 + a3 in [-64, 64]:
-// six digit planes [a0, a1, a2, a3, s0, s1], every value exact in fp16.
+// plus the balanced digits of the Karatsuba sum S = lo + hi (|S| <= 8192):
+//     S  = s0 + 2^7 s1,           s0 in [-64, 63],     |s1| <= 64
+// (any digit split of S serves, since the middle product only has to equal
+// (A_lo + A_hi)(B_lo + B_hi); this one keeps its per-k sums at half of what
+// s0 = a0 + a2, s1 = a1 + a3 would give): six digit planes
+// [a0, a1, a2, a3, s0, s1], every value exact in fp16.
 //
 // Products.  With X = 2^7 and Y = 2^13, for each pair of half-numbers
 //     P0 = (a0 + X a1)(b0 + X b1)    planes 0, 1
@@ -32,8 +36,9 @@
 // per-instruction floor, against 128 cycles for N = 256).
 //
 // Exactness.  Per k, |C_s| <= 4096 for P0 and P2 (|a0 b0| <= 4096,
-// |a0 b1| + |a1 b0| <= 4096, |a1 b1| <= 1024) and <= 16384 for Pm, so chunks of
-// 4096 (P0, P2) and 1024 (Pm) values of k keep every fp32 partial sum within
+// |a0 b1| + |a1 b0| <= 4096, |a1 b1| <= 1024) and <= 8192 for Pm
+// (|s0 t0| <= 4096, |s0 t1| + |s1 t0| <= 8192, |s1 t1| <= 4096), so chunks of
+// 4096 (P0, P2) and 2048 (Pm) values of k keep every fp32 partial sum within
 // 2^24.  After each chunk the epilogue drains the three accumulators into
 // int64 registers, exactly as the schoolbook kernel (gemm_limb.cuh) does.
 //
@@ -368,8 +373,10 @@ __device__ __forceinline__ void digits6(int32_t c, __half (&d)[PLANES]) {
     d[1] = __int2half_rn(a1);
     d[2] = __int2half_rn(a2);
     d[3] = __int2half_rn(a3);
-    d[4] = __int2half_rn(a0 + a2);
-    d[5] = __int2half_rn(a1 + a3);
+    const int32_t S = lo + hi;                                  // |S| <= 8192
+    const int32_t s0 = ((S + 64) & 127) - 64, s1 = (S - s0) >> 7;
+    d[4] = __int2half_rn(s0);
+    d[5] = __int2half_rn(s1);
 }
 
 // A (m x k, column-major, lda) -> planes D[pl][r][kk] (K-major, Mpad x Kpad per plane); MODE is

@@ -77,10 +77,10 @@ int gemm_digits(const Layout &g, const __half *Ad, const __half *Bd, int64_t m, 
     p.Npad = (int)g.Npad;
     p.mtiles = (int)((m + BM - 1) / BM);
     p.ntiles = (int)((n + BN - 1) / BN);
-    // exact chunks: |C_s| <= 4096 per k for P0 and P2, <= 16384 for Pm (fp32 sums within 2^24)
+    // exact chunks: |C_s| <= 4096 per k for P0 and P2, <= 8192 for Pm (fp32 sums within 2^24)
     p.chunk_kb[0] = 4096 / BK;
     p.chunk_kb[1] = 4096 / BK;
-    p.chunk_kb[2] = 1024 / BK;
+    p.chunk_kb[2] = 2048 / BK;
     p.N = N;
     p.minv = ~uint64_t(0) / (uint64_t)N;
     p.bias = N * (((int64_t(1) << 60) + N - 1) / N);

@@ -332,8 +332,8 @@ def test_limb_gemm_32_column_tiles(gffm, N, bits, shape):
 
 # ---- the two product forms: schoolbook (16 digit products) and one-level Karatsuba (12) ----
 KARA_MODULI = [2080640, 8388593, P25, P26, 2 ** 26 - 1]
-KARA_SHAPES = [(1, 1, 1), (130, 200, 1024), (129, 257, 1025), (64, 130, 2112), (200, 64, 4096), (70, 300, 4161),
-               (256, 256, 8256)]
+KARA_SHAPES = [(1, 1, 1), (130, 200, 1024), (129, 257, 1025), (64, 130, 2048), (64, 130, 2112), (200, 64, 4096),
+               (70, 300, 4161), (256, 256, 8256)]
 
 
 def kara_extreme(N, rng, shape):
@@ -360,13 +360,22 @@ def kara_extreme(N, rng, shape):
 
 
 def kara_worst(N):
-    """One residue with digits (-64, 32, -64, 32) or the largest that fits N: the Karatsuba
-    middle product's sums s0 = -128, s1 = 64 reach the exactness bound 16384 per k."""
-    for a3 in (32, 16, 8, 0):
-        c = (-64 + 128 * 32) + 8192 * (-64 + 128 * a3)
+    """One residue whose Karatsuba digits sit at the exactness bounds: halves lo = hi = 4032
+    give a0 = a2 = -64 with a1 = a3 = 32 (P0 and P2: |a0 b1| + |a1 b0| = 4096 per k) and the
+    sum S = 8064 = 128 * 63 (Pm's last shift: |s1 t1| = 3969 per k);
+    smaller halves where N is too small for them."""
+    for h in (4032, 2048, 1024, 0):
+        c = 4032 + 8192 * h
         if abs(c) <= (N - 1) // 2:
             return c % N
     return 1
+
+
+def kara_sigma_worst(N):
+    """A residue whose Karatsuba sum S = lo + hi = 8128 has digits s0 = -64, s1 = 64: the middle
+    product's cross shift |s0 t1| + |s1 t0| reaches its bound 8192 per k."""
+    c = 4064 + 8192 * 4064          # lo = hi = 4064, S = 8128 = -64 + 128 * 64
+    return c % N if abs(c) <= (N - 1) // 2 else kara_worst(N)
 
 
 @pytest.mark.parametrize("N", KARA_MODULI)
@@ -381,6 +390,9 @@ def test_limb_gemm_forms_match_oracle(gffm, N, shape, form):
     w = kara_worst(N)
     cases.append(("kara_worst", np.full((m, k), w), np.full((k, n), w)))
     cases.append(("kara_worst_neg", np.full((m, k), w), np.full((k, n), (N - w) % N)))
+    v = kara_sigma_worst(N)
+    cases.append(("kara_sigma_worst", np.full((m, k), v), np.full((k, n), v)))
+    cases.append(("kara_sigma_worst_neg", np.full((m, k), v), np.full((k, n), (N - v) % N)))
     for name, A, B in cases:
         got = as_int(gffm.mat_mul_gpu_type(gffm.CuModMatrix(A, N, elem_type=torch.float64),
                                            gffm.CuModMatrix(B, N, elem_type=torch.float64), method="limb", tuning=tu))
