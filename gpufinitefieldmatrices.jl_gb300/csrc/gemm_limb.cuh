@@ -26,6 +26,13 @@
 // sum_s C_s * (2^(7s) mod N) into int64 registers; the final value is reduced
 // mod N with Barrett's method and stored.
 //
+// Tile schedule.  A CTA's tiles are blockIdx.x, + gridDim.x, ... or, with a
+// tile counter, whatever a global atomic counter hands out: then several
+// launches of the same product share its tiles, and CTAs launched later (on
+// SMs that became free) take over the remaining ones.  The producer draws the
+// tiles and passes them to the mma issuer and the epilogue through a small ring
+// in shared memory.
+//
 // Warp roles (576 threads): warp 0 issues TMA loads, warp 1 allocates TMEM
 // and one lane issues the mma's, warps 2..17 are the epilogue (four per 32-lane
 // TMEM quadrant, each owning 16 of the 64 output columns).  With one
@@ -51,6 +58,7 @@ constexpr int B_TILE = BN * BK * 2;
 __host__ __device__ constexpr int epi_warps(int) { return 16; }
 __host__ __device__ constexpr int gemm_threads(int epi) { return 64 + 32 * epi_warps(epi); }
 constexpr int MAX_SHIFTS = 7;
+constexpr int TILE_RING = 4;       // tiles the producer hands ahead to the mma issuer and the epilogue
 constexpr int TILE_GROUP = 16;     // output-tile rows per raster group (L2 reuse)
 
 // Tile width BNV: 64 (one accumulator set) or 32 (two accumulator sets in TMEM,
@@ -86,6 +94,7 @@ struct Params {
     int64_t ldc;
     const double *X, *Y;   // EPI_KSUB_F64 subtrahends
     int *err;
+    int *tile_counter;         // nullptr: static tile schedule; else tiles drawn from this counter
     // EPI_SUB_I32M (EPI_SUB_I32 with odd N, one exact chunk whose shift sums stay below 2^22):
     // the chunk values are read by adding 1.5 * 2^23 in fp32 (the integer lands in the
     // mantissa) and reduced by a 32-bit Montgomery step, the weights carrying 2^32.
@@ -123,6 +132,8 @@ __global__ void __launch_bounds__(gemm_threads(EPI), 1)
     __shared__ uint64_t empty_bar[C_::STAGES];
     __shared__ uint64_t acc_full_bar[AB], acc_empty_bar[AB];
     __shared__ uint64_t drain_bar;
+    __shared__ uint64_t tile_full[TILE_RING], tile_empty[TILE_RING];
+    __shared__ int tile_ring[TILE_RING];
     __shared__ uint32_t tmem_base_s;
     __shared__ int abort_sh;
     volatile int &abort_s = abort_sh;
@@ -142,6 +153,10 @@ __global__ void __launch_bounds__(gemm_threads(EPI), 1)
             gffm_dev::mbar_init(&acc_empty_bar[b], EPB);
         }
         gffm_dev::mbar_init(&drain_bar, 1);
+        for (int q = 0; q < TILE_RING; q++) {
+            gffm_dev::mbar_init(&tile_full[q], 1);
+            gffm_dev::mbar_init(&tile_empty[q], 1 + EW);   // the mma issuer and every epilogue warp
+        }
         abort_s = 0;
         gffm_dev::fence_mbar_init();
         gffm_dev::prefetch_tmap(&tmA);
@@ -159,7 +174,19 @@ __global__ void __launch_bounds__(gemm_threads(EPI), 1)
             int stage = 0;
             uint32_t phase = 0;
             uint32_t issued_parity_mask = 0, issued_mask = 0;
-            for (int t = blockIdx.x; t < ntiles_total && !abort_s; t += gridDim.x) {
+            for (int i = 0;; i++) {
+                // the next tile, handed to the consumers (-1: none left)
+                int t = p.tile_counter ? atomicAdd(p.tile_counter, 1) : blockIdx.x + i * (int)gridDim.x;
+                if (abort_s || t >= ntiles_total) t = -1;
+                const int slot = i % TILE_RING;
+                if (i >= TILE_RING && !gffm_dev::mbar_wait(&tile_empty[slot], (uint32_t)(i / TILE_RING - 1) & 1)) {
+                    atomicOr(p.err, 1);
+                    abort_s = 1;
+                    t = -1;
+                }
+                tile_ring[slot] = t;
+                gffm_dev::mbar_arrive(&tile_full[slot]);
+                if (t < 0) break;
                 int tm, tn;
                 tile_coords(t, p.mtiles, p.ntiles, tm, tn);
                 for (int kb = 0; kb < p.kblocks; kb++) {
@@ -205,7 +232,16 @@ __global__ void __launch_bounds__(gemm_threads(EPI), 1)
             const uint32_t idesc_lo = gffm_dev::idesc_f16_f32(BM, BNV * (L > 1 ? L - 1 : 1));
             const uint32_t idesc_one = gffm_dev::idesc_f16_f32(BM, BNV);
             int local = 0;
-            for (int t = blockIdx.x; t < ntiles_total && !abort_s; t += gridDim.x, local++) {
+            for (int i = 0; !abort_s; i++, local++) {
+                const int slot = i % TILE_RING;
+                if (!gffm_dev::mbar_wait(&tile_full[slot], (uint32_t)(i / TILE_RING) & 1)) {
+                    atomicOr(p.err, 2);
+                    abort_s = 1;
+                    break;
+                }
+                const int t = tile_ring[slot];
+                gffm_dev::mbar_arrive(&tile_empty[slot]);
+                if (t < 0) break;
                 const int buf = AB == 2 ? (local & 1) : 0;
                 const uint32_t acc = tmem + (uint32_t)(buf * C_::BUF_COLS);
                 for (int kb0 = 0; kb0 < p.kblocks && !abort_s; kb0 += p.chunk_kb) {
@@ -275,7 +311,17 @@ __global__ void __launch_bounds__(gemm_threads(EPI), 1)
         const int part = grp % (EPB / 4);
         uint32_t acc_phase = 0;
         int local = 0;
-        for (int t = blockIdx.x; t < ntiles_total; t += gridDim.x, local++) {
+        for (int i = 0;; i++, local++) {
+            const int slot = i % TILE_RING;
+            if (!gffm_dev::mbar_wait(&tile_full[slot], (uint32_t)(i / TILE_RING) & 1)) {
+                atomicOr(p.err, 8);
+                abort_s = 1;
+                break;
+            }
+            const int t = tile_ring[slot];
+            __syncwarp();
+            if (lane == 0) gffm_dev::mbar_arrive(&tile_empty[slot]);
+            if (t < 0) break;
             if (AB == 2 && (local & 1) != buf) continue;      // the other warp group's tile
             const uint32_t accb = tmem + (uint32_t)(buf * C_::BUF_COLS) + (uint32_t)(CW * part);
             int tm, tn;

@@ -586,6 +586,12 @@ struct Lookahead {
     cudaEvent_t ea = nullptr, eb = nullptr;
     bool pending = false;   // the side update is in flight on s2
     int next_g = 0;         // CTA cap of the panel that runs beside it
+    // the side update's product, for a second launch on the panel's SMs once the panel is
+    // done: both launches draw tiles from one counter
+    limb::Layout g;
+    int rest = 0, rows_b = 0, k = 0;
+    int32_t *C = nullptr;
+    int *tiles = nullptr;
     ~Lookahead() {          // every exit path: s (and the workspace's release on it) follows s2
         if (pending) cudaStreamWaitEvent(s, eb, 0);
         if (ea) cudaEventDestroy(ea);
@@ -626,12 +632,29 @@ static int update_lookahead(Work &w, int64_t N, int row, int t, int col, int cs,
     GFFM_CUDA(cudaEventRecord(la.ea, la.s));
     GFFM_CUDA(cudaStreamWaitEvent(la.s2, la.ea, 0));
     la.next_g = rows_b <= P1_MAX_ROWS ? 1 : look_ctas(rows_b);   // the next panel's CTAs
+    // the side update takes its tiles from a counter: once the panel is done, a second launch
+    // on the panel's SMs (help_side_update) shares the rest
+    la.tiles = w.result + 8;
+    GFFM_CUDA(cudaMemsetAsync(la.tiles, 0, sizeof(int), la.s2));
+    la.g = gb;
+    la.rest = rest;
+    la.rows_b = rows_b;
+    la.k = t;
+    la.C = C + look;
     st = limb::gemm_digits(gb, w.dA, w.dB, rest, rows_b, t, N, C + look, w.ldw, limb::EPI_SUB_I32,
-                           gffm::sm_count() - la.next_g, la.s2);
+                           gffm::sm_count() - la.next_g, la.s2, nullptr, nullptr, la.tiles);
     if (st) return st;
     GFFM_CUDA(cudaEventRecord(la.eb, la.s2));
     la.pending = true;
     return GFFM_OK;
+}
+
+// After the panel that ran beside a side update: the same product again on the panel's SMs
+// (stream s), drawing the tiles the side update has not taken yet.
+static int help_side_update(Work &w, int64_t N, Lookahead &la) {
+    if (!la.pending || !la.tiles || la.next_g <= 0) return GFFM_OK;
+    return limb::gemm_digits(la.g, w.dA, w.dB, la.rest, la.rows_b, la.k, N, la.C, w.ldw, limb::EPI_SUB_I32, la.next_g,
+                             la.s, nullptr, nullptr, la.tiles);
 }
 
 static int forward(Work &w, int m, int n, int64_t N, int mode, int lcols, cudaStream_t s, Result &res) {
@@ -667,6 +690,9 @@ static int forward(Work &w, int m, int n, int64_t N, int mode, int lcols, cudaSt
         const int nbw = std::min(panel_width(m - row), n - col);
         int st = run_panel(w, m, n, row, col, nbw, M, mode == MODE_PLUQ ? lcols : 0, s, stage.p, h_res, h_prow, h_pv,
                            la.pending ? la.next_g : 0);
+        if (st) return st;
+        // the panel's SMs are free: they take over the side update's remaining tiles
+        st = help_side_update(w, N, la);
         if (st) return st;
         // everything after the panel may touch the columns the side update writes
         st = la.join();

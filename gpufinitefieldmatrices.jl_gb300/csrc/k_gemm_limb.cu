@@ -199,7 +199,8 @@ static int launch_gemm(int L, const CUtensorMap &ta, const CUtensorMap &tb, cons
 
 
 int gemm_digits(const Layout &g, const __half *Ad, const __half *Bd, int64_t m, int64_t n, int64_t k, int64_t N,
-                void *C, int64_t ldc, int epi, int max_ctas, cudaStream_t s, const double *X, const double *Y) {
+                void *C, int64_t ldc, int epi, int max_ctas, cudaStream_t s, const double *X, const double *Y,
+                int *tile_counter) {
     if (epi == EPI_KSUB_F64 && (!X || !Y)) return gffm::set_error(GFFM_ERR_ARG, "subtracting epilogue without X, Y");
     if (N < 2 || N >= (epi == EPI_EXACT_I64 ? (int64_t(1) << 52) : (int64_t(1) << 26)))
         return gffm::set_error(GFFM_ERR_MODULUS, "modulus %lld out of range for epilogue %d", (long long)N, epi);
@@ -252,6 +253,7 @@ int gemm_digits(const Layout &g, const __half *Ad, const __half *Bd, int64_t m, 
     p.X = X;
     p.Y = Y;
     p.err = gffm::device_error_flag();
+    p.tile_counter = tile_counter;
     if (!p.err) return gffm::check_device();
     int ntiles = p.mtiles * p.ntiles;
     if (ntiles == 0) return GFFM_OK;

@@ -64,8 +64,11 @@ int split_b(const T *B, int64_t ldb, int64_t k, int64_t n, __half *D, const Layo
 int encode_digit_map(void *map, const void *base, int64_t kpad, int64_t rows, int box_rows);
 
 // C (m x n, ldc) <- epilogue(A*B mod N) from digit planes; epi is a limb::Epi.  X, Y: EPI_KSUB_F64 only.
+// tile_counter: nullptr for the static tile schedule, else a device int (zero before the first of
+// them) from which every launch of this same product draws its tiles, so that a launch made later
+// on SMs that became free shares the remaining tiles.
 int gemm_digits(const Layout &g, const __half *Ad, const __half *Bd, int64_t m, int64_t n, int64_t k, int64_t N,
                 void *C, int64_t ldc, int epi, int max_ctas, cudaStream_t s, const double *X = nullptr,
-                const double *Y = nullptr);
+                const double *Y = nullptr, int *tile_counter = nullptr);
 
 }  // namespace limb
