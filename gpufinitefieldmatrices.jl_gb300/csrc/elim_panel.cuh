@@ -39,6 +39,7 @@ __device__ __forceinline__ int pkey_row(unsigned long long k) { return (int)(0x3
 struct alignas(16) Rec {
     unsigned long long key;      // pkey | tag
     unsigned long long row[NB];  // (tag << 32) | residue
+    unsigned long long inv;      // (tag << 32) | the candidate's inverse (the reference's Euclid)
 };
 // The exchange area: the displaced row's words (two parities), then the records.
 constexpr size_t OLD_ROW_WORDS = (size_t)2 * (NB + 1);
@@ -160,13 +161,16 @@ __device__ __forceinline__ void u_row(uint32_t *LU, const uint32_t *piv, const u
 //   A. each CTA publishes its candidate (largest residue of column t in its rows,
 //      lowest row on ties): the key and the row, as tagged words; the owner of
 //      row r = R0 + t publishes that row too,
-//   B. while two auxiliary warps poll the G keys (bounded waits) and four form
-//      Linv's row t-1, the row threads form U's row t-1 and the partial values
+//   B. while two auxiliary warps poll the G keys (bounded waits), four form
+//      Linv's row t-1 and one computes the inverse of the CTA's own candidate
+//      (the reference's Euclid) and publishes it as a tagged word, the row
+//      threads form U's row t-1 and the partial values
 //      y[r] = W[r][t+1] + sum_{s<t} Lneg[r][s] U[s][t+1]; the owner of row r
 //      publishes y[r],
-//   C. every warp picks the same winner; the CTA fetches its row (and, where the
-//      winner lands, the displaced row r with y[r]) while one warp computes the
-//      pivot's inverse by the reference's Euclid,
+//   C. every warp picks the same winner; the CTA fetches its row and its
+//      inverse (and, where the winner lands, the displaced row r with y[r]):
+//      every CTA inverted its own candidate during B, so the winner's inverse
+//      is off the critical path,
 //   D. every warp forms U[t][t+1] = inv (W_t[t+1] + sum_{s<t} Lneg_t[s] U[s][t+1]);
 //      the row threads complete column t+1, v[r] = y[r] + Lneg[r][t] U[t][t+1],
 //      and the CTA's next candidate is its largest v while the auxiliary warps
@@ -265,6 +269,9 @@ __global__ void __launch_bounds__(PANEL_THREADS, 1) k_panel(PanelArgs a) {
                 }
             } else if (x < 64 + NB && t > 0) {
                 linv_row(LU, s_lp, t - 1, s_inv, x - 64, M);
+            } else if (x == 64 + NB && best != 0) {
+                // the inverse of this CTA's candidate, in case it wins
+                st_relaxed_u64(&recs[b].inv, ((unsigned long long)tag << 32) | mod_inv_euclid_alu(pkey_val(best), N));
             }
         } else {
             // B. the row threads: U's row t-1, then the partial values of column t+1
@@ -310,7 +317,13 @@ __global__ void __launch_bounds__(PANEL_THREADS, 1) k_panel(PanelArgs a) {
                 s_old[j] = v;
             }
         } else if (tid == PANEL_THREADS - 32) {
-            s_inv = mod_inv_euclid_alu(pv, N);
+            uint32_t v = 0;
+            if (!wait_row_word(&a.rec[par * G + bw].inv, tag, v)) {
+                atomicOr(a.err, 16);
+                s_stop = 1;
+                s_status = PS_TIMEOUT;
+            }
+            s_inv = v;
         }
         __syncthreads();
         if (s_stop) break;
