@@ -440,8 +440,10 @@ __global__ void __launch_bounds__(PQ_THREADS, 2) k_pluq_batched(PQArgs a) {
                 }
                 best = __shfl_sync(0xffffffffu, best, 0);
                 const uint32_t pv = (uint32_t)(best >> 32);
-                // the column's values above the pivot rows are final either way
-                if (warp == 0 && lane < t) P[t * rs + lane] = (int32_t)s_ut[lane];
+                // the column's values above the pivot rows are final either way.  Warp 1 copies
+                // them: it alone rewrites s_ut (for column t+1, before the next barrier), so each
+                // lane reads its entry before its own next write.
+                if (warp == 1 && lane < t) P[t * rs + lane] = (int32_t)s_ut[lane];
                 if (pv == 0) {
                     zero_hit = 1;
                     break;

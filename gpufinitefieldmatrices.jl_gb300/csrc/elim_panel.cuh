@@ -188,7 +188,7 @@ __global__ void __launch_bounds__(PANEL_THREADS, 1) k_panel(PanelArgs a) {
     __shared__ __align__(16) uint32_t s_lp[NB + 8];  // its negated multipliers, zero from t on
     __shared__ uint32_t s_old[NB + 1];               // the displaced row, and its partial value of column t+1
     __shared__ unsigned long long red[PANEL_WARPS];
-    __shared__ int s_stop, s_status;
+    __shared__ int s_stop, s_stop_c, s_status;   // timeouts while polling keys / fetching the pivot row
     __shared__ uint32_t s_inv;
     __shared__ int32_t s_rec[3][NB];                 // pivot rows, values, inverses (written out after the loop)
     const int b = blockIdx.x, G = gridDim.x, tid = threadIdx.x;
@@ -211,6 +211,7 @@ __global__ void __launch_bounds__(PANEL_THREADS, 1) k_panel(PanelArgs a) {
     for (int i = tid; i < NB + 8; i += PANEL_THREADS) s_lp[i] = 0;
     if (tid == 0) {
         s_stop = 0;
+        s_stop_c = 0;
         s_status = PS_DONE;
     }
     __syncthreads();
@@ -300,7 +301,7 @@ __global__ void __launch_bounds__(PANEL_THREADS, 1) k_panel(PanelArgs a) {
             uint32_t v = 0;
             if (!wait_row_word(&a.rec[par * G + bw].row[tid], tag, v)) {
                 atomicOr(a.err, 16);
-                s_stop = 1;
+                s_stop_c = 1;
                 s_status = PS_TIMEOUT;
             }
             s_piv[tid] = v;
@@ -311,7 +312,7 @@ __global__ void __launch_bounds__(PANEL_THREADS, 1) k_panel(PanelArgs a) {
                 uint32_t v = 0;
                 if (!wait_row_word(&oldw[j], tag, v)) {
                     atomicOr(a.err, 16);
-                    s_stop = 1;
+                    s_stop_c = 1;
                     s_status = PS_TIMEOUT;
                 }
                 s_old[j] = v;
@@ -320,13 +321,13 @@ __global__ void __launch_bounds__(PANEL_THREADS, 1) k_panel(PanelArgs a) {
             uint32_t v = 0;
             if (!wait_row_word(&a.rec[par * G + bw].inv, tag, v)) {
                 atomicOr(a.err, 16);
-                s_stop = 1;
+                s_stop_c = 1;
                 s_status = PS_TIMEOUT;
             }
             s_inv = v;
         }
         __syncthreads();
-        if (s_stop) break;
+        if (s_stop_c) break;
         // D. U[t][t+1] (every warp), column t+1 and the next candidate (row threads),
         //    the row moves (auxiliary threads)
         const uint32_t inv = s_inv;
@@ -529,7 +530,9 @@ __global__ void __launch_bounds__(P1_THREADS, 1) k_panel1(PanelArgs a) {
         }
         best = __shfl_sync(0xffffffffu, best, 0);
         const uint32_t pv = (uint32_t)(best >> 32);
-        if (warp == 0 && lane < t) P[t * rs + lane] = (int32_t)s_ut[lane];
+        // warp 1 alone rewrites s_ut (for column t+1, before the next barrier): it copies
+        // column t's values above the pivot rows, each lane before its own next write
+        if (warp == 1 && lane < t) P[t * rs + lane] = (int32_t)s_ut[lane];
         if (pv == 0) {
             status = PS_ZERO_COL;
             break;
