@@ -1,0 +1,494 @@
+// batched_steps.cuh -- the batched PLUQ in panel steps, its trailing updates on the
+// tensor cores.  Included by k_batched.cu after the grouped GEMM.
+//
+// A PLUQ instance takes this route when it is square with n a multiple of 32 (n >= 64),
+// its prime is odd and L is at least n columns wide.  Step s factors panel s (columns
+// [32 s, 32 s + 32)) of every instance still running, one launch for all:
+//   k_pq_panel   a CTA per instance: the left-looking panel of k_pluq_batched
+//                (pq_factor_panel), the panel's swaps composed into row moves, the
+//                panel and L written back, then the pivot rows of the trailing columns
+//                (Linv times the pivot rows, from their old places) into a side buffer
+//                U12, and both factors of the trailing update as fp16 digit planes:
+//                A = the negated multipliers (rows below the pivots x 32),
+//                B = U12 transposed (trailing columns x 32), 7-bit balanced digits,
+//                K padded to 64 with zeros (the planes' padding is written once).
+//   k_gemm_trail a persistent tcgen05 GEMM over the 128 x 64 tiles of every instance's
+//                trailing block: W[r][c] = W[src(r)][c] + sum_t A[r][t] B[c][t] mod p,
+//                src(r) the row whose old contents row r receives (the panel's moves).
+//                The pivot rows keep their old contents through the GEMM (they are the
+//                moved rows' sources); the next step's panel kernel copies U12 into them.
+// The result is the same factorization as k_pluq_batched, operation for operation: the
+// same pivots, the same row moves, each entry reduced mod p once per panel.  A panel that
+// finds fewer than 32 pivots (a zero column, a rank drop) flags its instance; the instance
+// is then factored from its input again by k_pluq_batched, which covers every case.
+#pragma once
+
+#include "batched_pluq.cuh"
+#include "gemm_limb.cuh"
+
+namespace batched {
+
+constexpr int ST_NB = 32;                   // panel width of the step route
+constexpr int ST_BM = 128, ST_BN = 64;      // trailing GEMM tile (limb::BM x limb::BN)
+constexpr int ST_KPAD = 64;                 // K of the digit planes (32 used, 32 zero)
+static_assert(ST_BM == limb::BM && ST_BN == limb::BN && ST_KPAD == limb::BK, "the step GEMM uses the limb tiles");
+
+struct StepInst {
+    int pq;                      // index in the PLUQ instance array
+    int n;                       // m = n, a multiple of 32
+    int L;                       // 7-bit digits per residue
+    int Mpad, Npad;              // rows per digit plane of A / B (multiples of 128 / 64, >= n - 32)
+    int *srcmap;                 // [n]: the current panel's row sources (local rows)
+    int *ident;                  // [n]: row identities (L is stored by identity)
+    int32_t *U12;                // [32][n]: the last panel's pivot rows of its trailing columns
+    int *nr;                     // running count of row swaps
+    __half *Ad, *Bd;             // L planes of Mpad x 64 / Npad x 64 fp16
+    // the trailing GEMM's epilogue: the grouped GEMM's fast path (odd p, one exact chunk)
+    uint32_t ninv;               // -p^-1 mod 2^32
+    int32_t Wm[limb::MAX_SHIFTS];  // 2^(7 s) 2^32 mod p
+    int64_t fbias;
+};
+
+struct StepArgs {
+    const PQInst *inst;
+    const StepInst *steps;
+    const int *order;            // step instances, largest first
+    const int *live;             // per step: how many of `order` still factor (a prefix)
+    int *next;                   // per step: scheduling counters (zero before the run)
+    int *flags;                  // per PLUQ instance: nonzero = k_pluq_batched factors it
+    const CUtensorMap *tmaps;    // per step instance: A planes, B planes
+    int rcap;                    // rows of the shared panel (>= every n), multiple of 4
+};
+
+// the whole block, after a barrier: L 7-bit balanced digits of the 8 residues v[0..7]
+// (centred mod p) packed as 8 fp16 per plane, stored 16 bytes per plane at dst + l * plane
+__device__ __forceinline__ void put_digits8(const uint32_t (&v)[8], uint32_t N, int L, __half *dst, size_t plane) {
+    __half d[8][4];
+#pragma unroll
+    for (int i = 0; i < 8; i++) {
+        const int32_t c = 2 * v[i] > N ? (int32_t)v[i] - (int32_t)N : (int32_t)v[i];
+        limb::digits<4>(c, d[i], 7);
+    }
+#pragma unroll
+    for (int l = 0; l < 4; l++) {
+        if (l >= L) break;
+        __half2 h[4];
+#pragma unroll
+        for (int i = 0; i < 4; i++) h[i] = __halves2half2(d[2 * i][l], d[2 * i + 1][l]);
+        *reinterpret_cast<int4 *>(dst + l * plane) = *reinterpret_cast<const int4 *>(h);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// prologue: the working copies, row identities and counters of every step instance
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(PQ_THREADS) k_pq_prologue(StepArgs a, int count) {
+    extern __shared__ __align__(16) int32_t pq_smem[];
+    for (int j = blockIdx.x; j < count; j += gridDim.x) {
+        const StepInst J = a.steps[j];
+        const PQInst &I = a.inst[J.pq];
+        const elim::ModP M{I.M.n, I.M.minv};
+        to_rowmajor(I.A, I.lda, I.W, I.ldw, J.n, J.n, M, pq_smem);
+        for (int64_t idx = threadIdx.x; idx < (int64_t)J.n * I.ldlw; idx += blockDim.x) I.LW[idx] = 0;
+        for (int r = threadIdx.x; r < J.n; r += blockDim.x) J.ident[r] = r;
+        if (threadIdx.x == 0) {
+            *J.nr = 0;
+            a.flags[J.pq] = 0;
+        }
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// one panel step of every running instance
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(PQ_THREADS, 2) k_pq_panel(StepArgs a, int s) {
+    extern __shared__ __align__(16) int32_t pq_smem[];
+    __shared__ PQShared S;
+    __shared__ uint32_t Lv[PQ_MAX_NB * 33];
+    __shared__ uint32_t s_ut[PQ_MAX_NB];
+    const int tid = threadIdx.x;
+    const int rs = a.rcap + 4;
+    int32_t *P = pq_smem;
+    int32_t *Us = pq_smem + (size_t)PQ_MAX_NB * rs;
+    int *srcmap = Us + PQ_MAX_NB * PQ_CW;
+    const int r0 = ST_NB * s, c0 = r0;
+
+    for (;;) {
+        if (tid == 0) {
+            const int k = atomicAdd(a.next + s, 1);
+            S.inst = k < a.live[s] ? a.order[k] : -1;
+        }
+        __syncthreads();
+        const int jj = S.inst;
+        if (jj < 0) break;
+        const StepInst &J = a.steps[jj];
+        const PQInst &I = a.inst[J.pq];
+        const int n = J.n, R = n - r0, T = n - c0 - ST_NB;
+        const elim::ModP M{I.M.n, I.M.minv};
+        const uint32_t N = M.n;
+        int32_t *const W = I.W;
+        const int ldw = I.ldw;
+        if (a.flags[J.pq] == 0) {
+            // the previous panel's pivot rows, columns [c0, n): U12 -> W (their old contents
+            // were the previous trailing update's row sources)
+            if (s > 0) {
+                const int w4 = (n - c0) >> 2;
+                for (int idx = tid; idx < ST_NB * w4; idx += blockDim.x) {
+                    const int t = idx / w4, q = idx - t * w4;
+                    *reinterpret_cast<int4 *>(W + (int64_t)(r0 - ST_NB + t) * ldw + c0 + 4 * q) =
+                        *reinterpret_cast<const int4 *>(J.U12 + (int64_t)t * n + 4 * q);
+                }
+            }
+            // the panel, W[r0 + lr][c0 + j] -> P[j][lr]: 16-byte loads, four in flight a thread
+            for (int base = 0; base < R * 8; base += 4 * PQ_THREADS) {
+                int4 v[4];
+#pragma unroll
+                for (int i = 0; i < 4; i++) {
+                    const int idx = base + tid + i * PQ_THREADS, lr = idx >> 3, q = idx & 7;
+                    if (idx < R * 8) v[i] = *reinterpret_cast<const int4 *>(W + (int64_t)(r0 + lr) * ldw + c0 + 4 * q);
+                }
+#pragma unroll
+                for (int i = 0; i < 4; i++) {
+                    const int idx = base + tid + i * PQ_THREADS, lr = idx >> 3, q = idx & 7;
+                    if (idx < R * 8) {
+                        P[(4 * q) * rs + lr] = v[i].x;
+                        P[(4 * q + 1) * rs + lr] = v[i].y;
+                        P[(4 * q + 2) * rs + lr] = v[i].z;
+                        P[(4 * q + 3) * rs + lr] = v[i].w;
+                    }
+                }
+            }
+            int zero_hit = 0, stop = 0;
+            const int npiv = pq_factor_panel(P, rs, R, r0, n, ST_NB, c0, I.l_cols, M, S, Lv, s_ut, zero_hit, stop);
+            if (npiv < ST_NB) {
+                // a zero column or a rank drop: k_pluq_batched factors this instance from its input
+                if (tid == 0) a.flags[J.pq] = 1;
+            } else {
+                if (tid == 0) {
+                    int nr = *J.nr;
+                    pq_compose(S, npiv, r0, Us, a.rcap, I.row_swaps, nr);
+                    *J.nr = nr;
+                }
+                // the panel back to W, a row a thread in 16-byte stores: U on and above the
+                // diagonal, zero below
+                for (int lr = tid; lr < R; lr += blockDim.x) {
+                    srcmap[lr] = lr;
+                    int4 *wrow = reinterpret_cast<int4 *>(W + (int64_t)(r0 + lr) * ldw + c0);
+#pragma unroll
+                    for (int q = 0; q < ST_NB / 4; q++) {
+                        int32_t x[4];
+#pragma unroll
+                        for (int i = 0; i < 4; i++) x[i] = lr > 4 * q + i ? 0 : P[(4 * q + i) * rs + lr];
+                        wrow[q] = make_int4(x[0], x[1], x[2], x[3]);
+                    }
+                }
+                __syncthreads();
+                int id_moved = 0;
+                for (int k = tid; k < S.nmv; k += blockDim.x) srcmap[S.mv_dst[k] - r0] = S.mv_src[k] - r0;
+                if (tid < S.nmv) id_moved = J.ident[S.mv_src[tid]];
+                __syncthreads();
+                if (tid < S.nmv) J.ident[S.mv_dst[tid]] = id_moved;
+                for (int lr = tid; lr < R; lr += blockDim.x) J.srcmap[lr] = srcmap[lr];
+                __syncthreads();
+                // L: the pivots and the multipliers, by row identity (L's swap width covers n), a
+                // row a thread in 16-byte stores (zero above the diagonal, as L is there)
+                for (int lr = tid; lr < R; lr += blockDim.x) {
+                    int4 *lrow = reinterpret_cast<int4 *>(I.LW + (int64_t)J.ident[r0 + lr] * I.ldlw + c0);
+#pragma unroll
+                    for (int q = 0; q < ST_NB / 4; q++) {
+                        int32_t x[4];
+#pragma unroll
+                        for (int i = 0; i < 4; i++) {
+                            const int t = 4 * q + i;
+                            const uint32_t v = (uint32_t)P[t * rs + lr];
+                            x[i] = lr < t ? 0 : (int32_t)(lr == t ? S.piv_val[t] : (v ? N - v : 0u));
+                        }
+                        lrow[q] = make_int4(x[0], x[1], x[2], x[3]);
+                    }
+                }
+                // A planes: the negated multipliers of rows [32, R), 8 per thread and store
+                {
+                    const size_t plane = (size_t)J.Mpad * ST_KPAD;
+                    for (int idx = tid; idx < (R - ST_NB) * 4; idx += blockDim.x) {
+                        const int lr = ST_NB + (idx >> 2), t0 = 8 * (idx & 3);
+                        uint32_t v[8];
+#pragma unroll
+                        for (int i = 0; i < 8; i++) v[i] = (uint32_t)P[(t0 + i) * rs + lr];
+                        put_digits8(v, N, J.L, J.Ad + (size_t)(lr - ST_NB) * ST_KPAD + t0, plane);
+                    }
+                }
+                // the pivot rows of the trailing columns, PQ_CW at a time: U12 and the B planes
+                for (int cb = c0 + ST_NB; cb < n; cb += PQ_CW) {
+                    const int cw = min(PQ_CW, n - cb);
+                    const int cl = cb - c0 - ST_NB;   // column within the trailing block
+                    pq_pivot_rows<true>(W, ldw, r0, cb, cw, ST_NB, true, srcmap, Us, Lv, M);
+                    const int w4 = cw >> 2;
+                    for (int idx = tid; idx < ST_NB * w4; idx += blockDim.x) {
+                        const int t = idx / w4, q = idx - t * w4;
+                        *reinterpret_cast<int4 *>(J.U12 + (int64_t)t * n + cl + 4 * q) =
+                            *reinterpret_cast<const int4 *>(Us + t * PQ_CW + 4 * q);
+                    }
+                    const size_t plane = (size_t)J.Npad * ST_KPAD;
+                    for (int idx = tid; idx < cw * 4; idx += blockDim.x) {
+                        const int c = idx >> 2, t0 = 8 * (idx & 3);
+                        uint32_t v[8];
+#pragma unroll
+                        for (int i = 0; i < 8; i++) v[i] = (uint32_t)Us[(t0 + i) * PQ_CW + c];
+                        put_digits8(v, N, J.L, J.Bd + (size_t)(cl + c) * ST_KPAD + t0, plane);
+                    }
+                    __syncthreads();   // Us is refilled by the next chunk
+                }
+                (void)T;
+            }
+        }
+        __syncthreads();   // every thread has read S.inst before the next pick
+    }
+}
+
+// ---------------------------------------------------------------------------
+// the trailing update of every running instance, tcgen05, in place
+// ---------------------------------------------------------------------------
+// One tile: its L x L digit products over K = 32 (two K = 16 steps), drained shift by
+// shift and combined by the grouped GEMM's fast epilogue, plus the old value of the
+// output row's source row, reduced and stored over the row.
+__global__ void __launch_bounds__(G_THREADS, 1)
+    k_gemm_trail(StepArgs a, int s, const WorkItem *__restrict__ items, int nitems, int *err) {
+    extern __shared__ uint8_t dsmem_raw[];
+    __shared__ uint64_t full_bar[G_STAGES];
+    __shared__ uint64_t empty_bar[G_STAGES];
+    __shared__ uint64_t acc_full_bar, acc_empty_bar, drain_bar;
+    __shared__ uint32_t tmem_base_s;
+    __shared__ int abort_sh;
+    volatile int &abort_s = abort_sh;
+
+    uint8_t *smem = (uint8_t *)(((uintptr_t)dsmem_raw + 1023) & ~(uintptr_t)1023);
+    const int warp = threadIdx.x >> 5;
+    const int lane = threadIdx.x & 31;
+    const int r0 = ST_NB * s;
+
+    if (threadIdx.x == 0) {
+        for (int q = 0; q < G_STAGES; q++) {
+            gffm_dev::mbar_init(&full_bar[q], 1);
+            gffm_dev::mbar_init(&empty_bar[q], 1);
+        }
+        gffm_dev::mbar_init(&acc_full_bar, 1);
+        gffm_dev::mbar_init(&acc_empty_bar, G_EPI_WARPS);
+        gffm_dev::mbar_init(&drain_bar, 1);
+        abort_s = 0;
+        gffm_dev::fence_mbar_init();
+    }
+    if (warp == 1) gffm_dev::tmem_alloc(&tmem_base_s, G_TMEM_COLS);
+    gffm_dev::tc_fence_before();
+    __syncthreads();
+    gffm_dev::tc_fence_after();
+    const uint32_t tmem = tmem_base_s;
+
+    if (warp == 0) {
+        // ---------------- TMA producer ----------------
+        if (lane == 0) {
+            int stage = 0;
+            uint32_t phase = 0;
+            uint32_t issued_parity_mask = 0, issued_mask = 0;
+            int last = -1;
+            for (int t = blockIdx.x; t < nitems && !abort_s; t += gridDim.x) {
+                const WorkItem it = items[t];
+                const StepInst &J = a.steps[it.inst];
+                if (a.flags[J.pq]) continue;
+                const int L = J.L;
+                const CUtensorMap *tmA = a.tmaps + 2 * it.inst;
+                const CUtensorMap *tmB = tmA + 1;
+                if (it.inst != last) {
+                    tmap_acquire(tmA);
+                    tmap_acquire(tmB);
+                    last = it.inst;
+                }
+                if (!gffm_dev::mbar_wait(&empty_bar[stage], phase ^ 1)) {
+                    atomicOr(err, 1);
+                    abort_s = 1;
+                    break;
+                }
+                uint8_t *sa = smem + stage * G_STAGE_BYTES;
+                uint8_t *sb = sa + 4 * A_TILE;
+                gffm_dev::mbar_arrive_expect_tx(&full_bar[stage], (uint32_t)L * (A_TILE + B_TILE));
+                for (int l = 0; l < L; l++)
+                    gffm_dev::tma_load_2d(sa + l * A_TILE, tmA, &full_bar[stage], 0, l * J.Mpad + it.tm * ST_BM);
+                for (int l = 0; l < L; l++)
+                    gffm_dev::tma_load_2d(sb + l * B_TILE, tmB, &full_bar[stage], 0, l * J.Npad + it.tn * ST_BN);
+                issued_mask |= 1u << stage;
+                issued_parity_mask = (issued_parity_mask & ~(1u << stage)) | (phase << stage);
+                if (++stage == G_STAGES) {
+                    stage = 0;
+                    phase ^= 1;
+                }
+            }
+            if (abort_s) {
+                for (int q = 0; q < G_STAGES; q++)
+                    if (issued_mask & (1u << q)) gffm_dev::mbar_wait(&full_bar[q], (issued_parity_mask >> q) & 1);
+            }
+        }
+    } else if (warp == 1) {
+        // ---------------- MMA issuer ----------------
+        if (lane == 0) {
+            int stage = 0;
+            uint32_t phase = 0, acc_phase = 0;
+            bool issued_any = false;
+            for (int t = blockIdx.x; t < nitems && !abort_s; t += gridDim.x) {
+                const WorkItem it = items[t];
+                const StepInst &J = a.steps[it.inst];
+                if (a.flags[J.pq]) continue;
+                const int L = J.L;
+                const uint32_t idesc_full = gffm_dev::idesc_f16_f32(BM, BN * L);
+                const uint32_t idesc_lo = gffm_dev::idesc_f16_f32(BM, BN * (L > 1 ? L - 1 : 1));
+                const uint32_t idesc_one = gffm_dev::idesc_f16_f32(BM, BN);
+                if (!gffm_dev::mbar_wait(&acc_empty_bar, acc_phase ^ 1)) {
+                    atomicOr(err, 2);
+                    abort_s = 1;
+                    break;
+                }
+                gffm_dev::tc_fence_after();
+                if (!gffm_dev::mbar_wait(&full_bar[stage], phase)) {
+                    atomicOr(err, 4);
+                    abort_s = 1;
+                    break;
+                }
+                gffm_dev::tc_fence_after();
+                const uint32_t sa = gffm_dev::smem_u32(smem + stage * G_STAGE_BYTES);
+                const uint32_t sb = sa + 4 * A_TILE;
+                // K = 32: the first two K = 16 steps of the 64-wide rows (the rest is zero)
+#pragma unroll
+                for (int kk = 0; kk < ST_NB / 16; kk++) {
+                    const uint64_t bdesc = gffm_dev::umma_desc_sw128(sb + kk * 32);
+                    if (kk == 0) {
+                        gffm_dev::mma_f16(tmem, gffm_dev::umma_desc_sw128(sa), bdesc, idesc_full, 0);
+                        for (int i = 1; i < L; i++) {
+                            const uint64_t adesc = gffm_dev::umma_desc_sw128(sa + i * A_TILE);
+                            gffm_dev::mma_f16(tmem + 64 * i, adesc, bdesc, idesc_lo, 1);
+                            gffm_dev::mma_f16(tmem + 64 * (i + L - 1), adesc,
+                                              gffm_dev::umma_desc_sw128(sb + (L - 1) * B_TILE), idesc_one, 0);
+                        }
+                    } else {
+                        for (int i = 0; i < L; i++)
+                            gffm_dev::mma_f16(tmem + 64 * i, gffm_dev::umma_desc_sw128(sa + i * A_TILE + kk * 32),
+                                              bdesc, idesc_full, 1);
+                    }
+                }
+                issued_any = true;
+                gffm_dev::mma_commit(&empty_bar[stage]);
+                if (++stage == G_STAGES) {
+                    stage = 0;
+                    phase ^= 1;
+                }
+                gffm_dev::mma_commit(&acc_full_bar);
+                acc_phase ^= 1;
+            }
+            if (abort_s && issued_any) {
+                gffm_dev::mma_commit(&drain_bar);
+                gffm_dev::mbar_wait(&drain_bar, 0);
+            }
+        }
+    } else {
+        // ---------------- epilogue ----------------
+        // A thread owns one row and 16 columns of the tile.  The row's old values are loaded
+        // before the accumulator is waited for (no tile of this launch writes a row another
+        // tile reads: sources are pivot rows or the row itself), and each shift's TMEM load
+        // is issued before the previous shift is added in.
+        const int quad = warp & 3;
+        const int part = (warp - 2) >> 2;   // which 16 of the tile's 64 columns
+        const uint32_t tq = tmem + ((uint32_t)(quad * 32) << 16) + 16 * part;
+        uint32_t acc_phase = 0;
+        for (int t = blockIdx.x; t < nitems; t += gridDim.x) {
+            const WorkItem it = items[t];
+            const StepInst &J = a.steps[it.inst];
+            const PQInst &I = a.inst[J.pq];
+            if (a.flags[J.pq]) continue;
+            const int n = J.n;
+            const int rt = it.tm * ST_BM + quad * 32 + lane;          // row within the trailing block
+            const int col = r0 + ST_NB + it.tn * ST_BN + part * 16;   // n - col is 0 or >= 16
+            const bool live = rt < n - r0 - ST_NB && col < n;
+            int4 c4[4];
+            if (live) {
+                const int32_t *src = I.W + (int64_t)(r0 + J.srcmap[ST_NB + rt]) * I.ldw + col;
+#pragma unroll
+                for (int q = 0; q < 4; q++) c4[q] = *reinterpret_cast<const int4 *>(src + 4 * q);
+            }
+            const int nshift = 2 * J.L - 1;
+            int64_t acc[16];
+#pragma unroll
+            for (int j = 0; j < 16; j++) acc[j] = J.fbias;
+            if (!gffm_dev::mbar_wait(&acc_full_bar, acc_phase)) {
+                atomicOr(err, 8);
+                abort_s = 1;
+                break;
+            }
+            gffm_dev::tc_fence_after();
+            uint32_t v[2][16];
+            gffm_dev::tmem_ld_32x32b_x16(tq, v[0]);
+#pragma unroll
+            for (int q = 0; q < limb::MAX_SHIFTS; q++) {   // unrolled: v's index is static
+                if (q >= nshift) break;
+                gffm_dev::tmem_ld_wait();
+                if (q + 1 < nshift) gffm_dev::tmem_ld_32x32b_x16(tq + 64 * (q + 1), v[(q + 1) & 1]);
+                const int w = J.Wm[q];
+#pragma unroll
+                for (int j = 0; j < 16; j++)
+                    acc[j] += (int64_t)(int32_t)__float_as_uint(__fadd_rn(__uint_as_float(v[q & 1][j]), 12582912.0f)) * w;
+            }
+            gffm_dev::tc_fence_before();
+            __syncwarp();
+            if (lane == 0) gffm_dev::mbar_arrive(&acc_empty_bar);
+            acc_phase ^= 1;
+            if (live) {
+                const uint32_t n32 = I.M.n;
+                int32_t *dst = I.W + (int64_t)(r0 + ST_NB + rt) * I.ldw + col;
+                const uint32_t ninv = J.ninv;
+                // x in [0, 2^26 p): (x + m p) / 2^32 < 2p is x 2^-32 mod p; then + the old value
+                auto fin = [&](int64_t a64, int32_t old) -> int32_t {
+                    const uint64_t x = (uint64_t)a64;
+                    const uint32_t mq = (uint32_t)x * ninv;
+                    uint32_t r = (uint32_t)((x + (uint64_t)mq * n32) >> 32);
+                    r = r >= n32 ? r - n32 : r;
+                    r += (uint32_t)old;
+                    return (int32_t)(r >= n32 ? r - n32 : r);
+                };
+#pragma unroll
+                for (int q = 0; q < 4; q++) {
+                    const int4 o = make_int4(fin(acc[4 * q], c4[q].x), fin(acc[4 * q + 1], c4[q].y),
+                                             fin(acc[4 * q + 2], c4[q].z), fin(acc[4 * q + 3], c4[q].w));
+                    *reinterpret_cast<int4 *>(dst + 4 * q) = o;
+                }
+            }
+        }
+    }
+
+    gffm_dev::tc_fence_before();
+    __syncthreads();
+    gffm_dev::tc_fence_after();
+    if (warp == 1) gffm_dev::tmem_dealloc(tmem, G_TMEM_COLS);
+}
+
+// ---------------------------------------------------------------------------
+// the outputs of every step instance that was not handed back
+// ---------------------------------------------------------------------------
+// dynamic shared memory: the conversions' 8 x 32 x 33 words, then the row identities
+__global__ void __launch_bounds__(PQ_THREADS) k_pq_finish(StepArgs a, int count) {
+    extern __shared__ __align__(16) int32_t pq_smem[];
+    int *id_s = pq_smem + 8 * 32 * 33;
+    for (int j = blockIdx.x; j < count; j += gridDim.x) {
+        const StepInst J = a.steps[j];
+        if (a.flags[J.pq]) continue;   // uniform over the block; k_pluq_batched writes its outputs
+        const PQInst &I = a.inst[J.pq];
+        for (int r = threadIdx.x; r < J.n; r += blockDim.x) id_s[r] = J.ident[r];
+        to_colmajor(I.W, I.ldw, J.n, I.U, I.ldu, J.n, J.n, pq_smem);   // its barriers order the id_s stores
+        to_colmajor(I.LW, I.ldlw, I.lwc, I.L, I.ldl, J.n, I.l_cols, pq_smem, id_s, I.lsw);
+        if (threadIdx.x == 0) {
+            I.info[0] = *J.nr;
+            I.info[1] = 0;
+            I.info[2] = J.n;
+            I.info[3] = 0;
+        }
+        __syncthreads();
+    }
+}
+
+}  // namespace batched

@@ -61,20 +61,41 @@ constexpr int G_TMEM_COLS = 512;
 // digit split of every product operand
 // ---------------------------------------------------------------------------
 // A block takes one chunk: up to SPLIT_CHUNK consecutive work units (32 x 32 tiles
-// of A, or 256 digit pairs of B) of one operand, found with a single table load.
+// of A, or 256 runs of 8 K values of B) of one operand, found with a single table load.
 constexpr int SPLIT_CHUNK = 8;
+constexpr int SPLIT_B_RUN = 8;   // K values of B per thread and unit (one 16-byte store per plane)
 
 struct SplitChunk {
     int job, local0, count, pad_;
 };
 
+// the L digit planes of n consecutive centred values, packed: one store per plane
+template <int L, int NV>
+__device__ __forceinline__ void store_digit_run(const int32_t (&c)[NV], __half *dst, size_t plane, int bits) {
+    __half d[NV][L];
+#pragma unroll
+    for (int i = 0; i < NV; i++) digits<L>(c[i], d[i], bits);
+#pragma unroll
+    for (int l = 0; l < L; l++) {
+        __half2 h[NV / 2];
+#pragma unroll
+        for (int i = 0; i < NV / 2; i++) h[i] = __halves2half2(d[2 * i][l], d[2 * i + 1][l]);
+        if (NV == 8)
+            *reinterpret_cast<int4 *>(dst + l * plane) = *reinterpret_cast<const int4 *>(h);
+        else
+            *reinterpret_cast<uint2 *>(dst + l * plane) = *reinterpret_cast<const uint2 *>(h);
+    }
+}
+
 // A operand: 32 x 32 tiles transposed through shared memory.  The next unit's
 // values are loaded before the current one is converted and stored, so a
-// thread keeps loads in flight across the units of its chunk.
+// thread keeps loads in flight across the units of its chunk.  After the
+// transpose a thread writes 4 consecutive K values of one row (8 bytes per plane).
 template <int L>
 __device__ __forceinline__ void split_a_chunk(const SplitJob &J, const SplitChunk &ch, int32_t (*tile)[33]) {
     const int kt = J.kpad / 32;
     const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    const int wr = threadIdx.x >> 3, wk = 4 * (threadIdx.x & 7);   // the row and K run this thread writes
     const ModN M{J.N, J.minv};
     const size_t plane = (size_t)J.prow * J.kpad;
     double cur[4], nxt[4];
@@ -93,17 +114,14 @@ __device__ __forceinline__ void split_a_chunk(const SplitJob &J, const SplitChun
         const int64_t local = (int64_t)ch.local0 + u;
         if (u + 1 < ch.count) load(local + 1, nxt, okn);
         const int64_t r0 = (local / kt) * 32, k0 = (local % kt) * 32;
+        // tile[kk][r]: the centred value of A[r0 + r][k0 + kk]
 #pragma unroll
         for (int i = 0; i < 4; i++) tile[ty + 8 * i][tx] = okc[i] ? split_value<SPLIT_CENTRED>(cur[i], 0.0, M) : 0;
         __syncthreads();
+        int32_t c[4];
 #pragma unroll
-        for (int i = 0; i < 4; i++) {
-            const int64_t r = r0 + ty + 8 * i, kk = k0 + tx;
-            __half d[L];
-            digits<L>(tile[tx][ty + 8 * i], d, J.bits);
-#pragma unroll
-            for (int l = 0; l < L; l++) J.dst[l * plane + (size_t)r * J.kpad + kk] = d[l];
-        }
+        for (int j = 0; j < 4; j++) c[j] = tile[wk + j][wr];
+        store_digit_run<L, 4>(c, J.dst + (size_t)(r0 + wr) * J.kpad + k0 + wk, plane, J.bits);
         __syncthreads();   // the tile is reused by the next unit
 #pragma unroll
         for (int i = 0; i < 4; i++) {
@@ -113,49 +131,44 @@ __device__ __forceinline__ void split_a_chunk(const SplitJob &J, const SplitChun
     }
 }
 
-// B operand: 256 digit pairs per unit, the next unit's pair loaded ahead.
+// B operand: a unit is 256 runs of SPLIT_B_RUN consecutive K values of one column (the
+// operand is column-major: contiguous reads, one 16-byte store per plane); the next
+// unit's run is loaded ahead.
 template <int L>
 __device__ __forceinline__ void split_b_chunk(const SplitJob &J, const SplitChunk &ch) {
-    const int64_t ppc = J.kpad / 2;
-    const int64_t total = ppc * J.prow;
+    const int64_t rpc = J.kpad / SPLIT_B_RUN;   // runs per column
+    const int64_t total = rpc * J.prow;
     const ModN M{J.N, J.minv};
     const int k = J.rows, n = J.cols;
     const size_t plane = (size_t)J.prow * J.kpad;
-    double c0 = 0.0, c1 = 0.0, n0 = 0.0, n1 = 0.0;
-    bool k0c = false, k1c = false, k0n = false, k1n = false;
-    auto load = [&](int64_t local, double &v0, double &v1, bool &ok0, bool &ok1) {
+    double cv[SPLIT_B_RUN], nv[SPLIT_B_RUN];
+    auto load = [&](int64_t local, double (&v)[SPLIT_B_RUN]) {
         const int64_t idx = local * 256 + threadIdx.x;
-        const int64_t c = idx / ppc;
-        const int64_t kk = (idx - c * ppc) * 2;
-        ok0 = idx < total && c < n && kk < k;
-        ok1 = idx < total && c < n && kk + 1 < k;
-        v0 = ok0 ? J.src[kk + c * J.ld] : 0.0;
-        v1 = ok1 ? J.src[kk + 1 + c * J.ld] : 0.0;
+        const int64_t c = idx / rpc;
+        const int64_t kk = (idx - c * rpc) * SPLIT_B_RUN;
+        const bool colok = idx < total && c < n;
+#pragma unroll
+        for (int i = 0; i < SPLIT_B_RUN; i++) v[i] = (colok && kk + i < k) ? J.src[kk + i + c * J.ld] : 0.0;
     };
-    load(ch.local0, c0, c1, k0c, k1c);
+    load(ch.local0, cv);
     for (int u = 0; u < ch.count; u++) {
         const int64_t local = (int64_t)ch.local0 + u;
         const int64_t idx = local * 256 + threadIdx.x;
         if (idx >= total) return;
-        if (u + 1 < ch.count) load(local + 1, n0, n1, k0n, k1n);
-        const int64_t c = idx / ppc;
-        const int64_t kk = (idx - c * ppc) * 2;
-        const int32_t v0 = k0c ? split_value<SPLIT_CENTRED>(c0, 0.0, M) : 0;
-        const int32_t v1 = k1c ? split_value<SPLIT_CENTRED>(c1, 0.0, M) : 0;
-        __half d0[L], d1[L];
-        digits<L>(v0, d0, J.bits);
-        digits<L>(v1, d1, J.bits);
+        if (u + 1 < ch.count) load(local + 1, nv);
+        const int64_t c = idx / rpc;
+        const int64_t kk = (idx - c * rpc) * SPLIT_B_RUN;
+        int32_t v[SPLIT_B_RUN];
 #pragma unroll
-        for (int l = 0; l < L; l++)
-            *reinterpret_cast<__half2 *>(J.dst + l * plane + (size_t)c * J.kpad + kk) = __halves2half2(d0[l], d1[l]);
-        c0 = n0;
-        c1 = n1;
-        k0c = k0n;
-        k1c = k1n;
+        for (int i = 0; i < SPLIT_B_RUN; i++)
+            v[i] = (c < n && kk + i < k) ? split_value<SPLIT_CENTRED>(cv[i], 0.0, M) : 0;
+        store_digit_run<L, SPLIT_B_RUN>(v, J.dst + (size_t)c * J.kpad + kk, plane, J.bits);
+#pragma unroll
+        for (int i = 0; i < SPLIT_B_RUN; i++) cv[i] = nv[i];
     }
 }
 
-__global__ void __launch_bounds__(256) k_split_batched(const SplitJob *__restrict__ jobs,
+__global__ void __launch_bounds__(256, 3) k_split_batched(const SplitJob *__restrict__ jobs,
                                                        const SplitChunk *__restrict__ chunks) {
     __shared__ int32_t tile[32][33];
     const SplitChunk ch = chunks[blockIdx.x];
@@ -424,6 +437,8 @@ __global__ void __launch_bounds__(G_THREADS, 1)
 
 }  // namespace batched
 
+#include "batched_steps.cuh"
+
 // ---------------------------------------------------------------------------
 // host: plans
 // ---------------------------------------------------------------------------
@@ -444,7 +459,15 @@ struct gffm_batch_plan_s {
     batched::PQInst *d_pq = nullptr;
     int *d_order = nullptr, *d_next = nullptr;
     int32_t *d_tmp = nullptr;
-    int tmp_ldw = 4, tmp_ldlw = 4;
+    int tmp_ldw = 4;
+    // the panel-step route (batched_steps.cuh)
+    int n_step = 0, n_steps = 0, step_grid = 0, step_misc_grid = 0, trail_grid = 0;
+    batched::StepArgs step{};
+    std::vector<int> step_live;                 // per step: running instances
+    std::vector<int> step_items0;               // per step: first work item (n_steps + 1 entries)
+    batched::WorkItem *d_step_items = nullptr;
+    int *d_counters = nullptr;                  // the PLUQ kernels' scheduling counters
+    int n_counters = 0;
     cudaGraphExec_t exec = nullptr;
     struct ZeroK {
         double *C;
@@ -509,6 +532,21 @@ struct Carve {
     }
 };
 
+// The grouped GEMM's fast epilogue (odd N, one exact chunk): -N^-1 mod 2^32, the shift
+// weights 2^(bits s) 2^32 mod N and the bias that keeps the sum positive.
+void fast_consts(int64_t N, int L, int bits, uint32_t &ninv, int32_t *Wm, int64_t &fbias) {
+    uint32_t inv = 1;                         // N^-1 mod 2^32 by Newton's iteration
+    for (int it = 0; it < 5; it++) inv *= 2u - (uint32_t)N * inv;
+    ninv = 0u - inv;
+    int64_t w = 1 % N, wsum = 0;
+    for (int s = 0; s < limb::MAX_SHIFTS; s++) {
+        Wm[s] = (int32_t)(((__int128)w << 32) % N);
+        if (s < 2 * L - 1) wsum += Wm[s];
+        w = (w << bits) % N;
+    }
+    fbias = N * (int64_t(1) << 25) - (int64_t)0x4B400000 * wsum;
+}
+
 int build_graph(gffm_batch_plan p, bool overlap) {
     using namespace batched;
     cudaStream_t s0, s1 = nullptr;
@@ -531,7 +569,26 @@ int build_graph(gffm_batch_plan p, bool overlap) {
             pq_stream = s1;
         }
         if (p->n_pq > 0) {
-            fail(cudaMemsetAsync(p->d_next, 0, sizeof(int), pq_stream), "cudaMemsetAsync");
+            fail(cudaMemsetAsync(p->d_counters, 0, sizeof(int) * p->n_counters, pq_stream), "cudaMemsetAsync");
+            if (p->n_step > 0) {
+                const size_t conv_smem = (size_t)8 * 32 * 33 * 4;
+                k_pq_prologue<<<p->step_misc_grid, PQ_THREADS, conv_smem, pq_stream>>>(p->step, p->n_step);
+                fail(cudaGetLastError(), "k_pq_prologue");
+                for (int s = 0; s < p->n_steps; s++) {
+                    k_pq_panel<<<std::max(1, std::min(p->step_live[s], p->step_grid)), PQ_THREADS, p->pq_smem,
+                                 pq_stream>>>(p->step, s);
+                    fail(cudaGetLastError(), "k_pq_panel");
+                    const int i0 = p->step_items0[s], ni = p->step_items0[s + 1] - i0;
+                    if (ni > 0) {
+                        k_gemm_trail<<<std::min(ni, p->trail_grid), G_THREADS, G_SMEM_BYTES, pq_stream>>>(
+                            p->step, s, p->d_step_items + i0, ni, gffm::device_error_flag());
+                        fail(cudaGetLastError(), "k_gemm_trail");
+                    }
+                }
+                k_pq_finish<<<p->step_misc_grid, PQ_THREADS, conv_smem + sizeof(int) * p->pq_rcap, pq_stream>>>(
+                    p->step, p->n_step);
+                fail(cudaGetLastError(), "k_pq_finish");
+            }
             PQArgs a;
             a.inst = p->d_pq;
             a.order = p->d_order;
@@ -541,7 +598,7 @@ int build_graph(gffm_batch_plan p, bool overlap) {
             a.next = p->d_next;
             a.tmp = p->d_tmp;
             a.tmp_ldw = p->tmp_ldw;
-            a.tmp_ldlw = p->tmp_ldlw;
+            a.flags = p->step.flags;
             k_pluq_batched<<<p->pq_grid, PQ_THREADS, p->pq_smem, pq_stream>>>(a);
             fail(cudaGetLastError(), "k_pluq_batched");
         }
@@ -658,15 +715,7 @@ int create(const gffm_batch_desc *descs, int64_t count, const gffm_batch_tuning 
         I.fbias = 0;
         if ((d.N & 1) && I.kblocks <= I.chunk_kb &&
             (int64_t)I.kblocks * BK * g.L * (int64_t(1) << (2 * g.bits - 2)) <= (int64_t(1) << 22)) {
-            uint32_t inv = 1;                         // N^-1 mod 2^32 by Newton's iteration
-            for (int it = 0; it < 5; it++) inv *= 2u - (uint32_t)d.N * inv;
-            I.ninv = 0u - inv;
-            int64_t wsum = 0;
-            for (int sft = 0; sft < MAX_SHIFTS; sft++) {
-                I.Wm[sft] = (int32_t)(((__int128)I.W[sft] << 32) % d.N);
-                if (sft < 2 * g.L - 1) wsum += I.Wm[sft];
-            }
-            I.fbias = d.N * (int64_t(1) << 25) - (int64_t)0x4B400000 * wsum;
+            fast_consts(d.N, g.L, g.bits, I.ninv, I.Wm, I.fbias);
             I.fast = 1;
         } else {
             for (int sft = 0; sft < MAX_SHIFTS; sft++) I.Wm[sft] = 0;
@@ -679,7 +728,6 @@ int create(const gffm_batch_desc *descs, int64_t count, const gffm_batch_tuning 
     }
     const size_t o_pq = cv.take(sizeof(PQInst) * std::max(1, p->n_pq));
     const size_t o_order = cv.take(sizeof(int) * std::max(1, p->n_pq));
-    const size_t o_next = cv.take(sizeof(int));
     std::vector<PQInst> pq(p->n_pq);
     std::vector<size_t> o_w(p->n_pq), o_lw(p->n_pq);
     int rcap = 4;
@@ -709,8 +757,63 @@ int create(const gffm_batch_desc *descs, int64_t count, const gffm_batch_tuning 
         o_lw[q] = cv.take((size_t)std::max<int64_t>(d.m, 1) * I.ldlw * 4);
         rcap = std::max(rcap, (int)align_up((size_t)d.m, 4));
         p->tmp_ldw = std::max(p->tmp_ldw, I.ldw);
-        p->tmp_ldlw = std::max(p->tmp_ldlw, I.ldlw);
     }
+    // ---- the panel-step route (batched_steps.cuh): square PLUQs of n = 32 k >= 64 rows, an odd
+    // prime, L at least n columns wide; under the default panel tuning only ----
+    std::vector<int> st_q;   // PLUQ instance indices, largest first
+    if (tu.pluq_panel == 0)
+        for (int q = 0; q < p->n_pq; q++) {
+            const gffm_batch_desc &d = descs[pq_ids[q]];
+            if (d.m == d.n && d.n >= 64 && d.n % ST_NB == 0 && (d.N & 1) && d.l_cols >= d.n) st_q.push_back(q);
+        }
+    std::stable_sort(st_q.begin(), st_q.end(), [&](int x, int y) { return pq[x].n > pq[y].n; });
+    p->n_step = (int)st_q.size();
+    p->n_steps = p->n_step ? pq[st_q[0]].n / ST_NB : 0;
+    std::vector<StepInst> stv(p->n_step);
+    std::vector<size_t> o_src(p->n_step), o_id(p->n_step), o_u12(p->n_step), o_nr(p->n_step), o_ad(p->n_step),
+        o_bd(p->n_step);
+    for (int j = 0; j < p->n_step; j++) {
+        const int q = st_q[j];
+        const gffm_batch_desc &d = descs[pq_ids[q]];
+        StepInst &J = stv[j];
+        J.pq = q;
+        J.n = (int)d.n;
+        J.L = limb::limbs_for(d.N);
+        J.Mpad = (int)align_up((size_t)d.n - ST_NB, ST_BM);
+        J.Npad = (int)align_up((size_t)d.n - ST_NB, ST_BN);
+        fast_consts(d.N, J.L, 7, J.ninv, J.Wm, J.fbias);
+        o_src[j] = cv.take(sizeof(int) * d.n);
+        o_id[j] = cv.take(sizeof(int) * d.n);
+        o_u12[j] = cv.take(sizeof(int32_t) * ST_NB * d.n);
+        o_nr[j] = cv.take(sizeof(int));
+    }
+    const size_t o_planes = align_up(cv.off, 1024);
+    for (int j = 0; j < p->n_step; j++) {
+        o_ad[j] = cv.take((size_t)stv[j].L * stv[j].Mpad * ST_KPAD * 2, 1024);
+        o_bd[j] = cv.take((size_t)stv[j].L * stv[j].Npad * ST_KPAD * 2, 1024);
+    }
+    const size_t planes_bytes = cv.off > o_planes ? cv.off - o_planes : 0;
+    const size_t o_steps = cv.take(sizeof(StepInst) * std::max(1, p->n_step));
+    const size_t o_st_order = cv.take(sizeof(int) * std::max(1, p->n_step));
+    const size_t o_live = cv.take(sizeof(int) * std::max(1, p->n_steps));
+    const size_t o_stmaps = cv.take(sizeof(CUtensorMap) * 2 * std::max(1, p->n_step), 128);
+    const size_t o_flags = cv.take(sizeof(int) * std::max(1, p->n_pq));
+    p->n_counters = 1 + p->n_steps;   // the per-instance kernel's, then one per step
+    const size_t o_counters = cv.take(sizeof(int) * p->n_counters);
+    std::vector<WorkItem> st_items;
+    for (int s = 0; s < p->n_steps; s++) {
+        int live = 0;
+        while (live < p->n_step && stv[live].n > ST_NB * s) live++;
+        p->step_live.push_back(live);
+        p->step_items0.push_back((int)st_items.size());
+        for (int j = 0; j < live; j++) {
+            const int rt = stv[j].n - ST_NB * s - ST_NB;   // rows = columns of the trailing block
+            for (int tm = 0; tm < (rt + ST_BM - 1) / ST_BM; tm++)
+                for (int tn = 0; tn < (rt + ST_BN - 1) / ST_BN; tn++) st_items.push_back(WorkItem{j, tm, tn, 0});
+        }
+    }
+    p->step_items0.push_back((int)st_items.size());
+    const size_t o_st_items = cv.take(sizeof(WorkItem) * std::max<size_t>(1, st_items.size()));
     // PLUQ grid (it sizes the per-CTA row-move buffers)
     p->pq_nb = tu.pluq_panel ? tu.pluq_panel : 32;
     p->pq_rcap = rcap;
@@ -725,7 +828,17 @@ int create(const gffm_batch_desc *descs, int64_t count, const gffm_batch_tuning 
         }
     }
     p->pq_grid = std::max(1, std::min(p->n_pq, tu.pluq_ctas ? tu.pluq_ctas : per_sm * sms));
-    const size_t o_tmp = cv.take((size_t)p->pq_grid * PQ_MAX_MOVES * (p->tmp_ldw + p->tmp_ldlw) * 4);
+    if (p->n_step > 0) {
+        int per_sm_step = 1;
+        PLAN_CUDA(cudaFuncSetAttribute(k_pq_panel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->pq_smem));
+        PLAN_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_step, k_pq_panel, PQ_THREADS, p->pq_smem));
+        p->step_grid = std::max(1, per_sm_step) * sms;
+        if (tu.pluq_ctas) p->step_grid = tu.pluq_ctas;
+        p->step_misc_grid = std::max(1, std::min(p->n_step, 4 * sms));
+        p->trail_grid = sms;
+        PLAN_CUDA(cudaFuncSetAttribute(k_gemm_trail, cudaFuncAttributeMaxDynamicSharedMemorySize, G_SMEM_BYTES));
+    }
+    const size_t o_tmp = cv.take((size_t)p->pq_grid * PQ_MAX_MOVES * p->tmp_ldw * 4);
     // work items (output tiles), largest instances first
     std::vector<int> mm_order(p->n_mm);
     std::iota(mm_order.begin(), mm_order.end(), 0);
@@ -744,7 +857,7 @@ int create(const gffm_batch_desc *descs, int64_t count, const gffm_batch_tuning 
     for (int q = 0; q < p->n_mm; q++) {
         if (mm[q].kblocks == 0) continue;
         const limb::Layout &g = lay[q];
-        const int64_t ua = (g.Kpad / 32) * (g.Mpad / 32), ub = ((g.Kpad / 2) * g.Npad + 255) / 256;
+        const int64_t ua = (g.Kpad / 32) * (g.Mpad / 32), ub = ((g.Kpad / SPLIT_B_RUN) * g.Npad + 255) / 256;
         nchunks += (ua + SPLIT_CHUNK - 1) / SPLIT_CHUNK + (ub + SPLIT_CHUNK - 1) / SPLIT_CHUNK;
     }
     const size_t o_chunks = cv.take(sizeof(SplitChunk) * std::max<int64_t>(1, nchunks));
@@ -759,7 +872,8 @@ int create(const gffm_batch_desc *descs, int64_t count, const gffm_batch_tuning 
     p->d_tmaps = reinterpret_cast<CUtensorMap *>(base + o_tm);
     p->d_pq = reinterpret_cast<PQInst *>(base + o_pq);
     p->d_order = reinterpret_cast<int *>(base + o_order);
-    p->d_next = reinterpret_cast<int *>(base + o_next);
+    p->d_counters = reinterpret_cast<int *>(base + o_counters);
+    p->d_next = p->d_counters;
     p->d_items = reinterpret_cast<WorkItem *>(base + o_items);
     p->d_jobs = reinterpret_cast<SplitJob *>(base + o_jobs);
     p->d_chunks = reinterpret_cast<SplitChunk *>(base + o_chunks);
@@ -779,7 +893,7 @@ int create(const gffm_batch_desc *descs, int64_t count, const gffm_batch_tuning 
             jobs.push_back(ja);
             SplitJob jb{d.B, d.ldb, db, (int)d.k, (int)d.n, (int)g.Npad, (int)g.Kpad, g.L, 1, d.N, mm[q].minv, blk,
                         g.bits, 0};
-            blk += ((g.Kpad / 2) * g.Npad + 255) / 256;
+            blk += ((g.Kpad / SPLIT_B_RUN) * g.Npad + 255) / 256;
             jobs.push_back(jb);
         }
         st = limb::encode_digit_map(&tmaps[2 * q], da, g.Kpad, (int64_t)g.L * g.Mpad, BM);
@@ -805,6 +919,34 @@ int create(const gffm_batch_desc *descs, int64_t count, const gffm_batch_tuning 
         pq[q].W = reinterpret_cast<int32_t *>(base + o_w[q]);
         pq[q].LW = reinterpret_cast<int32_t *>(base + o_lw[q]);
     }
+    for (int j = 0; j < p->n_step; j++) {
+        StepInst &J = stv[j];
+        J.srcmap = reinterpret_cast<int *>(base + o_src[j]);
+        J.ident = reinterpret_cast<int *>(base + o_id[j]);
+        J.U12 = reinterpret_cast<int32_t *>(base + o_u12[j]);
+        J.nr = reinterpret_cast<int *>(base + o_nr[j]);
+        J.Ad = reinterpret_cast<__half *>(base + o_ad[j]);
+        J.Bd = reinterpret_cast<__half *>(base + o_bd[j]);
+    }
+    std::vector<CUtensorMap> stmaps(2 * std::max(1, p->n_step));
+    for (int j = 0; j < p->n_step; j++) {
+        const StepInst &J = stv[j];
+        st = limb::encode_digit_map(&stmaps[2 * j], J.Ad, ST_KPAD, (int64_t)J.L * J.Mpad, ST_BM);
+        if (!st) st = limb::encode_digit_map(&stmaps[2 * j + 1], J.Bd, ST_KPAD, (int64_t)J.L * J.Npad, ST_BN);
+        if (st) {
+            free_plan(p);
+            return st;
+        }
+    }
+    p->step.inst = p->d_pq;
+    p->step.steps = reinterpret_cast<StepInst *>(base + o_steps);
+    p->step.order = reinterpret_cast<int *>(base + o_st_order);
+    p->step.live = reinterpret_cast<int *>(base + o_live);
+    p->step.next = p->d_counters + 1;
+    p->step.flags = reinterpret_cast<int *>(base + o_flags);
+    p->step.tmaps = reinterpret_cast<CUtensorMap *>(base + o_stmaps);
+    p->step.rcap = p->pq_rcap;
+    p->d_step_items = reinterpret_cast<WorkItem *>(base + o_st_items);
     std::iota(order.begin(), order.end(), 0);
     std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
         const int64_t wa = (int64_t)pq[a].m * pq[a].n * std::min(pq[a].m, pq[a].n);
@@ -825,6 +967,27 @@ int create(const gffm_batch_desc *descs, int64_t count, const gffm_batch_tuning 
     PLAN_CUDA(cudaMemcpy(p->d_chunks, chunks.data(), sizeof(SplitChunk) * chunks.size(), cudaMemcpyHostToDevice));
     PLAN_CUDA(cudaMemcpy(p->d_pq, pq.data(), sizeof(PQInst) * pq.size(), cudaMemcpyHostToDevice));
     PLAN_CUDA(cudaMemcpy(p->d_order, order.data(), sizeof(int) * order.size(), cudaMemcpyHostToDevice));
+    {
+        // every PLUQ starts on the per-instance kernel; the prologue hands the step route's back
+        std::vector<int> ones(std::max(1, p->n_pq), 1), st_order(std::max(1, p->n_step));
+        std::iota(st_order.begin(), st_order.end(), 0);
+        PLAN_CUDA(cudaMemcpy(p->step.flags, ones.data(), sizeof(int) * ones.size(), cudaMemcpyHostToDevice));
+        if (p->n_step > 0) {
+            PLAN_CUDA(cudaMemcpy(const_cast<StepInst *>(p->step.steps), stv.data(), sizeof(StepInst) * stv.size(),
+                                 cudaMemcpyHostToDevice));
+            PLAN_CUDA(cudaMemcpy(const_cast<int *>(p->step.order), st_order.data(), sizeof(int) * p->n_step,
+                                 cudaMemcpyHostToDevice));
+            PLAN_CUDA(cudaMemcpy(const_cast<int *>(p->step.live), p->step_live.data(), sizeof(int) * p->n_steps,
+                                 cudaMemcpyHostToDevice));
+            PLAN_CUDA(cudaMemcpy(const_cast<CUtensorMap *>(p->step.tmaps), stmaps.data(),
+                                 sizeof(CUtensorMap) * 2 * p->n_step, cudaMemcpyHostToDevice));
+            if (!st_items.empty())
+                PLAN_CUDA(cudaMemcpy(p->d_step_items, st_items.data(), sizeof(WorkItem) * st_items.size(),
+                                     cudaMemcpyHostToDevice));
+            // the planes' K padding (columns 32..63) is read by the GEMM and never written again
+            PLAN_CUDA(cudaMemset(base + o_planes, 0, planes_bytes));
+        }
+    }
 
     st = build_graph(p, tu.overlap != 0);
     if (st) {

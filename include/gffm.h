@@ -343,10 +343,14 @@ GFFM_API int gffm_karatsuba_to_values_f64(double *A, const double *D1, const dou
  * per call.  A batch holds thousands of independent instances, each with its
  * own sizes and modulus (2 <= N < 2^26), each a product or a PLUQ with the
  * semantics of those calls.  Products run in one grouped tcgen05 kernel over
- * all instances' output tiles, PLUQs in one persistent kernel (a CTA per
- * instance); a plan validates the batch, lays out its workspace, encodes the
- * per-instance TMA descriptors and captures the launches in a CUDA graph once.
- * A plan is bound to the buffers its descriptors name. */
+ * all instances' output tiles.  Square PLUQs of n = 32k >= 64 rows with an odd
+ * prime (and l_cols >= n) run in panel steps: per step one launch factors a
+ * 32-column panel of every running instance and a grouped tcgen05 GEMM applies
+ * all their trailing updates; an instance that loses rank in a panel, and every
+ * other PLUQ, runs in one persistent kernel (a CTA per instance).  Both give
+ * the same factorization.  A plan validates the batch, lays out its workspace,
+ * encodes the per-instance TMA descriptors and captures the launches in a CUDA
+ * graph once.  A plan is bound to the buffers its descriptors name. */
 enum gffm_batch_op { GFFM_BATCH_MATMUL = 0, GFFM_BATCH_PLUQ = 1 };
 
 typedef struct gffm_batch_desc {
@@ -367,8 +371,10 @@ typedef struct gffm_batch_desc {
     int64_t *info;         /* PLUQ, device int64[4]: #row swaps, #col swaps, rank, status (0 or GFFM_ERR_BOUNDS) */
 } gffm_batch_desc;
 
-/* Tuning of a plan; 0 in a field picks the default.  pluq_panel: panel width
- * (8, 16 or 32); gemm_ctas / pluq_ctas: persistent grid sizes; overlap: 1 runs
+/* Tuning of a plan; 0 in a field picks the default.  pluq_panel: 0 takes the
+ * panel-step route where it applies (32-column panels elsewhere); 8, 16 or 32
+ * factor every PLUQ in the persistent kernel with that panel width;
+ * gemm_ctas / pluq_ctas: persistent grid sizes; overlap: 1 runs
  * the products and the PLUQs on two graph branches at once; digit_bits: 7 or 8
  * for every product (0: per instance, whichever needs fewer digits). */
 typedef struct gffm_batch_tuning {

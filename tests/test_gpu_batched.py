@@ -164,3 +164,38 @@ def test_batched_pluq_taller_than_1024_rows(gffm):
     for _ in range(2):                      # a plan runs again on the same buffers
         check(gffm, inst, want, plan.run().results())
     assert gffm.load_library().gffm_device_status(None) == 0
+
+
+# Square PLUQs of n = 32 k >= 64 with an odd prime take the panel-step route (tensor-core
+# trailing updates) under the default tuning; those that lose rank in a panel are factored
+# again by the per-instance kernel.  Sizes, primes and rank patterns of both kinds.
+STEP_PQ = [("uniform", 64, 64, P26), ("uniform", 96, 96, 65521), ("uniform", 128, 128, 2080639),
+           ("uniform", 160, 160, 3), ("uniform", 256, 256, P25), ("uniform", 288, 288, 8191),
+           ("uniform", 448, 448, 65521), ("uniform", 512, 512, P26), ("uniform", 192, 192, 127),
+           ("rank30", 96, 96, P26), ("zero_cols", 128, 128, 13), ("ties", 128, 128, 11),
+           ("lead_zero", 64, 64, 7), ("uniform", 64, 64, 2), ("uniform", 100, 100, P26),
+           ("tall_low", 128, 128, P26)]
+
+
+def test_step_route_matches_oracle(gffm):
+    rng = np.random.default_rng(3232)
+    inst, want = [], []
+    for (kind, m, n, N) in STEP_PQ:
+        A = make(kind, m, n, N, rng)
+        inst.append(("pluq", gffm.CuModMatrix(A, N, elem_type=torch.float64)))
+        want.append(("pluq", oracle.pluq(A, N)))
+    A, B = rng.integers(0, P25, size=(300, 200)), rng.integers(0, P25, size=(200, 260))
+    inst.append(("matmul", gffm.CuModMatrix(A, P25, elem_type=torch.float64),
+                 gffm.CuModMatrix(B, P25, elem_type=torch.float64)))
+    want.append(("matmul", oracle.matmul(A, B, P25)))
+    plan = gffm.BatchPlan(inst)
+    res = plan.run().results()
+    check(gffm, inst, want, res)
+    # the same factorization as the per-instance kernel, bit for bit, and again on a rerun
+    per_inst = gffm.BatchPlan(inst, gffm.BatchTuning(32, 0, 0, 0, 0)).run().results()
+    for (kind, *_), a, b in zip(inst, res, per_inst):
+        if kind == "pluq":
+            assert a[2] == b[2] and a[3] == b[3]
+            assert torch.equal(a[0].data, b[0].data) and torch.equal(a[1].data, b[1].data)
+    check(gffm, inst, want, plan.run().results())
+    assert gffm.load_library().gffm_device_status(None) == 0
