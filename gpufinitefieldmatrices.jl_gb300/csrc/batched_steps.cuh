@@ -11,7 +11,7 @@
 //                U12, and both factors of the trailing update as fp16 digit planes:
 //                A = the negated multipliers (rows below the pivots x 32),
 //                B = U12 transposed (trailing columns x 32), 7-bit balanced digits,
-//                K padded to 64 with zeros (the planes' padding is written once).
+//                rows of 32 fp16 (64 bytes; TMA and the MMA use 64-byte swizzling).
 //   k_gemm_trail a persistent tcgen05 GEMM over the 128 x 64 tiles of every instance's
 //                trailing block: W[r][c] = W[src(r)][c] + sum_t A[r][t] B[c][t] mod p,
 //                src(r) the row whose old contents row r receives (the panel's moves).
@@ -30,8 +30,12 @@ namespace batched {
 
 constexpr int ST_NB = 32;                   // panel width of the step route
 constexpr int ST_BM = 128, ST_BN = 64;      // trailing GEMM tile (limb::BM x limb::BN)
-constexpr int ST_KPAD = 64;                 // K of the digit planes (32 used, 32 zero)
-static_assert(ST_BM == limb::BM && ST_BN == limb::BN && ST_KPAD == limb::BK, "the step GEMM uses the limb tiles");
+constexpr int ST_KPAD = 32;                 // K of the digit planes: 64-byte rows
+constexpr int ST_A_TILE = ST_BM * ST_KPAD * 2, ST_B_TILE = ST_BN * ST_KPAD * 2;   // one digit's tile
+constexpr int ST_STAGES = 4;
+constexpr int ST_STAGE_BYTES = 4 * (ST_A_TILE + ST_B_TILE);
+constexpr int ST_SMEM_BYTES = ST_STAGES * ST_STAGE_BYTES + 1024;
+static_assert(ST_BM == limb::BM && ST_BN == limb::BN, "the step GEMM's epilogue uses the limb tile shape");
 
 struct StepInst {
     int pq;                      // index in the PLUQ instance array
@@ -251,24 +255,30 @@ __global__ void __launch_bounds__(PQ_THREADS, 2) k_pq_panel(StepArgs a, int s) {
 // ---------------------------------------------------------------------------
 // One tile: its L x L digit products over K = 32 (two K = 16 steps), drained shift by
 // shift and combined by the grouped GEMM's fast epilogue, plus the old value of the
-// output row's source row, reduced and stored over the row.
+// output row's source row, reduced and stored over the row.  A CTA takes a contiguous
+// range of the step's tiles (ordered by instance, tile row, tile column), so each role
+// keeps the instance's fields, and the epilogue its row pointers, across tiles instead of
+// starting every tile with a chain of dependent loads.
 __global__ void __launch_bounds__(G_THREADS, 1)
     k_gemm_trail(StepArgs a, int s, const WorkItem *__restrict__ items, int nitems, int *err) {
     extern __shared__ uint8_t dsmem_raw[];
-    __shared__ uint64_t full_bar[G_STAGES];
-    __shared__ uint64_t empty_bar[G_STAGES];
+    __shared__ uint64_t full_bar[ST_STAGES];
+    __shared__ uint64_t empty_bar[ST_STAGES];
     __shared__ uint64_t acc_full_bar, acc_empty_bar, drain_bar;
     __shared__ uint32_t tmem_base_s;
     __shared__ int abort_sh;
+    __shared__ int32_t wm_s[G_EPI_WARPS][8];   // per epilogue warp: its current instance's shift weights
     volatile int &abort_s = abort_sh;
 
     uint8_t *smem = (uint8_t *)(((uintptr_t)dsmem_raw + 1023) & ~(uintptr_t)1023);
     const int warp = threadIdx.x >> 5;
     const int lane = threadIdx.x & 31;
     const int r0 = ST_NB * s;
+    const int t_begin = (int)((int64_t)nitems * blockIdx.x / gridDim.x);
+    const int t_end = (int)((int64_t)nitems * (blockIdx.x + 1) / gridDim.x);
 
     if (threadIdx.x == 0) {
-        for (int q = 0; q < G_STAGES; q++) {
+        for (int q = 0; q < ST_STAGES; q++) {
             gffm_dev::mbar_init(&full_bar[q], 1);
             gffm_dev::mbar_init(&empty_bar[q], 1);
         }
@@ -290,40 +300,47 @@ __global__ void __launch_bounds__(G_THREADS, 1)
             int stage = 0;
             uint32_t phase = 0;
             uint32_t issued_parity_mask = 0, issued_mask = 0;
-            int last = -1;
-            for (int t = blockIdx.x; t < nitems && !abort_s; t += gridDim.x) {
+            int last = -1, L = 0, Mpad = 0, Npad = 0;
+            bool skip = false;
+            const CUtensorMap *tmA = nullptr, *tmB = nullptr;
+            for (int t = t_begin; t < t_end && !abort_s; t++) {
                 const WorkItem it = items[t];
-                const StepInst &J = a.steps[it.inst];
-                if (a.flags[J.pq]) continue;
-                const int L = J.L;
-                const CUtensorMap *tmA = a.tmaps + 2 * it.inst;
-                const CUtensorMap *tmB = tmA + 1;
                 if (it.inst != last) {
-                    tmap_acquire(tmA);
-                    tmap_acquire(tmB);
                     last = it.inst;
+                    const StepInst &J = a.steps[it.inst];
+                    skip = a.flags[J.pq] != 0;
+                    L = J.L;
+                    Mpad = J.Mpad;
+                    Npad = J.Npad;
+                    tmA = a.tmaps + 2 * it.inst;
+                    tmB = tmA + 1;
+                    if (!skip) {
+                        tmap_acquire(tmA);
+                        tmap_acquire(tmB);
+                    }
                 }
+                if (skip) continue;
                 if (!gffm_dev::mbar_wait(&empty_bar[stage], phase ^ 1)) {
                     atomicOr(err, 1);
                     abort_s = 1;
                     break;
                 }
-                uint8_t *sa = smem + stage * G_STAGE_BYTES;
-                uint8_t *sb = sa + 4 * A_TILE;
-                gffm_dev::mbar_arrive_expect_tx(&full_bar[stage], (uint32_t)L * (A_TILE + B_TILE));
+                uint8_t *sa = smem + stage * ST_STAGE_BYTES;
+                uint8_t *sb = sa + 4 * ST_A_TILE;
+                gffm_dev::mbar_arrive_expect_tx(&full_bar[stage], (uint32_t)L * (ST_A_TILE + ST_B_TILE));
                 for (int l = 0; l < L; l++)
-                    gffm_dev::tma_load_2d(sa + l * A_TILE, tmA, &full_bar[stage], 0, l * J.Mpad + it.tm * ST_BM);
+                    gffm_dev::tma_load_2d(sa + l * ST_A_TILE, tmA, &full_bar[stage], 0, l * Mpad + it.tm * ST_BM);
                 for (int l = 0; l < L; l++)
-                    gffm_dev::tma_load_2d(sb + l * B_TILE, tmB, &full_bar[stage], 0, l * J.Npad + it.tn * ST_BN);
+                    gffm_dev::tma_load_2d(sb + l * ST_B_TILE, tmB, &full_bar[stage], 0, l * Npad + it.tn * ST_BN);
                 issued_mask |= 1u << stage;
                 issued_parity_mask = (issued_parity_mask & ~(1u << stage)) | (phase << stage);
-                if (++stage == G_STAGES) {
+                if (++stage == ST_STAGES) {
                     stage = 0;
                     phase ^= 1;
                 }
             }
             if (abort_s) {
-                for (int q = 0; q < G_STAGES; q++)
+                for (int q = 0; q < ST_STAGES; q++)
                     if (issued_mask & (1u << q)) gffm_dev::mbar_wait(&full_bar[q], (issued_parity_mask >> q) & 1);
             }
         }
@@ -333,14 +350,21 @@ __global__ void __launch_bounds__(G_THREADS, 1)
             int stage = 0;
             uint32_t phase = 0, acc_phase = 0;
             bool issued_any = false;
-            for (int t = blockIdx.x; t < nitems && !abort_s; t += gridDim.x) {
+            int last = -1, L = 0;
+            bool skip = false;
+            uint32_t idesc_full = 0, idesc_lo = 0;
+            const uint32_t idesc_one = gffm_dev::idesc_f16_f32(BM, BN);
+            for (int t = t_begin; t < t_end && !abort_s; t++) {
                 const WorkItem it = items[t];
-                const StepInst &J = a.steps[it.inst];
-                if (a.flags[J.pq]) continue;
-                const int L = J.L;
-                const uint32_t idesc_full = gffm_dev::idesc_f16_f32(BM, BN * L);
-                const uint32_t idesc_lo = gffm_dev::idesc_f16_f32(BM, BN * (L > 1 ? L - 1 : 1));
-                const uint32_t idesc_one = gffm_dev::idesc_f16_f32(BM, BN);
+                if (it.inst != last) {
+                    last = it.inst;
+                    const StepInst &J = a.steps[it.inst];
+                    skip = a.flags[J.pq] != 0;
+                    L = J.L;
+                    idesc_full = gffm_dev::idesc_f16_f32(BM, BN * L);
+                    idesc_lo = gffm_dev::idesc_f16_f32(BM, BN * (L > 1 ? L - 1 : 1));
+                }
+                if (skip) continue;
                 if (!gffm_dev::mbar_wait(&acc_empty_bar, acc_phase ^ 1)) {
                     atomicOr(err, 2);
                     abort_s = 1;
@@ -353,29 +377,29 @@ __global__ void __launch_bounds__(G_THREADS, 1)
                     break;
                 }
                 gffm_dev::tc_fence_after();
-                const uint32_t sa = gffm_dev::smem_u32(smem + stage * G_STAGE_BYTES);
-                const uint32_t sb = sa + 4 * A_TILE;
-                // K = 32: the first two K = 16 steps of the 64-wide rows (the rest is zero)
+                const uint32_t sa = gffm_dev::smem_u32(smem + stage * ST_STAGE_BYTES);
+                const uint32_t sb = sa + 4 * ST_A_TILE;
+                // K = 32: two K = 16 steps along the 64-byte rows
 #pragma unroll
                 for (int kk = 0; kk < ST_NB / 16; kk++) {
-                    const uint64_t bdesc = gffm_dev::umma_desc_sw128(sb + kk * 32);
+                    const uint64_t bdesc = gffm_dev::umma_desc_sw64(sb + kk * 32);
                     if (kk == 0) {
-                        gffm_dev::mma_f16(tmem, gffm_dev::umma_desc_sw128(sa), bdesc, idesc_full, 0);
+                        gffm_dev::mma_f16(tmem, gffm_dev::umma_desc_sw64(sa), bdesc, idesc_full, 0);
                         for (int i = 1; i < L; i++) {
-                            const uint64_t adesc = gffm_dev::umma_desc_sw128(sa + i * A_TILE);
+                            const uint64_t adesc = gffm_dev::umma_desc_sw64(sa + i * ST_A_TILE);
                             gffm_dev::mma_f16(tmem + 64 * i, adesc, bdesc, idesc_lo, 1);
                             gffm_dev::mma_f16(tmem + 64 * (i + L - 1), adesc,
-                                              gffm_dev::umma_desc_sw128(sb + (L - 1) * B_TILE), idesc_one, 0);
+                                              gffm_dev::umma_desc_sw64(sb + (L - 1) * ST_B_TILE), idesc_one, 0);
                         }
                     } else {
                         for (int i = 0; i < L; i++)
-                            gffm_dev::mma_f16(tmem + 64 * i, gffm_dev::umma_desc_sw128(sa + i * A_TILE + kk * 32),
+                            gffm_dev::mma_f16(tmem + 64 * i, gffm_dev::umma_desc_sw64(sa + i * ST_A_TILE + kk * 32),
                                               bdesc, idesc_full, 1);
                     }
                 }
                 issued_any = true;
                 gffm_dev::mma_commit(&empty_bar[stage]);
-                if (++stage == G_STAGES) {
+                if (++stage == ST_STAGES) {
                     stage = 0;
                     phase ^= 1;
                 }
@@ -391,57 +415,84 @@ __global__ void __launch_bounds__(G_THREADS, 1)
         // ---------------- epilogue ----------------
         // A thread owns one row and 16 columns of the tile.  The row's old values are loaded
         // before the accumulator is waited for (no tile of this launch writes a row another
-        // tile reads: sources are pivot rows or the row itself), and each shift's TMEM load
-        // is issued before the previous shift is added in.
+        // tile reads: sources are pivot rows or the row itself).
         const int quad = warp & 3;
         const int part = (warp - 2) >> 2;   // which 16 of the tile's 64 columns
         const uint32_t tq = tmem + ((uint32_t)(quad * 32) << 16) + 16 * part;
         uint32_t acc_phase = 0;
-        for (int t = blockIdx.x; t < nitems; t += gridDim.x) {
-            const WorkItem it = items[t];
-            const StepInst &J = a.steps[it.inst];
-            const PQInst &I = a.inst[J.pq];
-            if (a.flags[J.pq]) continue;
-            const int n = J.n;
-            const int rt = it.tm * ST_BM + quad * 32 + lane;          // row within the trailing block
+        int last = -1, last_tm = -1, n = 0, L = 0, ldw = 0;
+        bool skip = false, row_live = false;
+        uint32_t ninv = 0, n32 = 0;
+        int64_t fbias = 0;
+        int32_t *Wm = wm_s[warp - 2];
+        int32_t *W = nullptr;
+        const int *srcmap = nullptr;
+        const int32_t *src_row = nullptr;
+        int32_t *dst_row = nullptr;
+        WorkItem nx = t_begin < t_end ? items[t_begin] : WorkItem{0, 0, 0, 0};
+        for (int t = t_begin; t < t_end; t++) {
+            const WorkItem it = nx;
+            if (t + 1 < t_end) nx = items[t + 1];
+            if (it.inst != last) {
+                last = it.inst;
+                last_tm = -1;
+                const StepInst &J = a.steps[it.inst];
+                const PQInst &I = a.inst[J.pq];
+                skip = a.flags[J.pq] != 0;
+                n = J.n;
+                L = J.L;
+                ninv = J.ninv;
+                fbias = J.fbias;
+                __syncwarp();
+                if (lane < limb::MAX_SHIFTS) Wm[lane] = J.Wm[lane];
+                __syncwarp();
+                W = I.W;
+                ldw = I.ldw;
+                n32 = I.M.n;
+                srcmap = J.srcmap;
+            }
+            if (skip) continue;
+            if (it.tm != last_tm) {
+                last_tm = it.tm;
+                const int rt = it.tm * ST_BM + quad * 32 + lane;   // row within the trailing block
+                row_live = rt < n - r0 - ST_NB;
+                if (row_live) {
+                    src_row = W + (int64_t)(r0 + srcmap[ST_NB + rt]) * ldw;
+                    dst_row = W + (int64_t)(r0 + ST_NB + rt) * ldw;
+                }
+            }
             const int col = r0 + ST_NB + it.tn * ST_BN + part * 16;   // n - col is 0 or >= 16
-            const bool live = rt < n - r0 - ST_NB && col < n;
+            const bool live = row_live && col < n;
             int4 c4[4];
             if (live) {
-                const int32_t *src = I.W + (int64_t)(r0 + J.srcmap[ST_NB + rt]) * I.ldw + col;
 #pragma unroll
-                for (int q = 0; q < 4; q++) c4[q] = *reinterpret_cast<const int4 *>(src + 4 * q);
+                for (int q = 0; q < 4; q++) c4[q] = *reinterpret_cast<const int4 *>(src_row + col + 4 * q);
             }
-            const int nshift = 2 * J.L - 1;
+            const int nshift = 2 * L - 1;
             int64_t acc[16];
 #pragma unroll
-            for (int j = 0; j < 16; j++) acc[j] = J.fbias;
+            for (int j = 0; j < 16; j++) acc[j] = fbias;
             if (!gffm_dev::mbar_wait(&acc_full_bar, acc_phase)) {
                 atomicOr(err, 8);
                 abort_s = 1;
                 break;
             }
             gffm_dev::tc_fence_after();
-            uint32_t v[2][16];
-            gffm_dev::tmem_ld_32x32b_x16(tq, v[0]);
-#pragma unroll
-            for (int q = 0; q < limb::MAX_SHIFTS; q++) {   // unrolled: v's index is static
-                if (q >= nshift) break;
+            for (int q = 0; q < nshift; q++) {
+                uint32_t v[16];
+                gffm_dev::tmem_ld_32x32b_x16(tq + 64 * q, v);
                 gffm_dev::tmem_ld_wait();
-                if (q + 1 < nshift) gffm_dev::tmem_ld_32x32b_x16(tq + 64 * (q + 1), v[(q + 1) & 1]);
-                const int w = J.Wm[q];
+                const int w = Wm[q];
 #pragma unroll
                 for (int j = 0; j < 16; j++)
-                    acc[j] += (int64_t)(int32_t)__float_as_uint(__fadd_rn(__uint_as_float(v[q & 1][j]), 12582912.0f)) * w;
+                    acc[j] += (int64_t)(int32_t)__float_as_uint(__fadd_rn(__uint_as_float(v[j]), 12582912.0f)) * w;
             }
             gffm_dev::tc_fence_before();
             __syncwarp();
             if (lane == 0) gffm_dev::mbar_arrive(&acc_empty_bar);
             acc_phase ^= 1;
             if (live) {
-                const uint32_t n32 = I.M.n;
-                int32_t *dst = I.W + (int64_t)(r0 + ST_NB + rt) * I.ldw + col;
-                const uint32_t ninv = J.ninv;
+                int32_t *dst = dst_row + col;
                 // x in [0, 2^26 p): (x + m p) / 2^32 < 2p is x 2^-32 mod p; then + the old value
                 auto fin = [&](int64_t a64, int32_t old) -> int32_t {
                     const uint64_t x = (uint64_t)a64;

@@ -216,6 +216,18 @@ __device__ __forceinline__ uint64_t umma_desc_sw128(uint32_t smem_addr) {
     d |= (uint64_t)2 << 61;                       // swizzle: 128 B
     return d;
 }
+// Shared-memory matrix descriptor for a K-major operand tile stored with 64-byte
+// swizzling (rows of 64 bytes, 8-row groups 512 bytes apart), as TMA writes it with
+// CU_TENSOR_MAP_SWIZZLE_64B.
+__device__ __forceinline__ uint64_t umma_desc_sw64(uint32_t smem_addr) {
+    uint64_t d = 0;
+    d |= (uint64_t)((smem_addr & 0x3FFFF) >> 4);  // start address
+    d |= (uint64_t)1 << 16;                       // leading byte offset (unused with swizzle)
+    d |= (uint64_t)(512 >> 4) << 32;              // stride byte offset: 8 rows x 64 B
+    d |= (uint64_t)1 << 46;                       // descriptor version (sm_100 family)
+    d |= (uint64_t)4 << 61;                       // swizzle: 64 B
+    return d;
+}
 // Instruction descriptor, kind::f16: fp16 A and B (K-major), fp32 accumulator, M x N.
 __host__ __device__ constexpr uint32_t idesc_f16_f32(int M, int N) {
     return (1u << 4) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);

@@ -580,7 +580,7 @@ int build_graph(gffm_batch_plan p, bool overlap) {
                     fail(cudaGetLastError(), "k_pq_panel");
                     const int i0 = p->step_items0[s], ni = p->step_items0[s + 1] - i0;
                     if (ni > 0) {
-                        k_gemm_trail<<<std::min(ni, p->trail_grid), G_THREADS, G_SMEM_BYTES, pq_stream>>>(
+                        k_gemm_trail<<<std::min(ni, p->trail_grid), G_THREADS, ST_SMEM_BYTES, pq_stream>>>(
                             p->step, s, p->d_step_items + i0, ni, gffm::device_error_flag());
                         fail(cudaGetLastError(), "k_gemm_trail");
                     }
@@ -836,7 +836,7 @@ int create(const gffm_batch_desc *descs, int64_t count, const gffm_batch_tuning 
         if (tu.pluq_ctas) p->step_grid = tu.pluq_ctas;
         p->step_misc_grid = std::max(1, std::min(p->n_step, 4 * sms));
         p->trail_grid = sms;
-        PLAN_CUDA(cudaFuncSetAttribute(k_gemm_trail, cudaFuncAttributeMaxDynamicSharedMemorySize, G_SMEM_BYTES));
+        PLAN_CUDA(cudaFuncSetAttribute(k_gemm_trail, cudaFuncAttributeMaxDynamicSharedMemorySize, ST_SMEM_BYTES));
     }
     const size_t o_tmp = cv.take((size_t)p->pq_grid * PQ_MAX_MOVES * p->tmp_ldw * 4);
     // work items (output tiles), largest instances first
@@ -931,8 +931,8 @@ int create(const gffm_batch_desc *descs, int64_t count, const gffm_batch_tuning 
     std::vector<CUtensorMap> stmaps(2 * std::max(1, p->n_step));
     for (int j = 0; j < p->n_step; j++) {
         const StepInst &J = stv[j];
-        st = limb::encode_digit_map(&stmaps[2 * j], J.Ad, ST_KPAD, (int64_t)J.L * J.Mpad, ST_BM);
-        if (!st) st = limb::encode_digit_map(&stmaps[2 * j + 1], J.Bd, ST_KPAD, (int64_t)J.L * J.Npad, ST_BN);
+        st = limb::encode_digit_map_k32(&stmaps[2 * j], J.Ad, (int64_t)J.L * J.Mpad, ST_BM);
+        if (!st) st = limb::encode_digit_map_k32(&stmaps[2 * j + 1], J.Bd, (int64_t)J.L * J.Npad, ST_BN);
         if (st) {
             free_plan(p);
             return st;
@@ -984,7 +984,7 @@ int create(const gffm_batch_desc *descs, int64_t count, const gffm_batch_tuning 
             if (!st_items.empty())
                 PLAN_CUDA(cudaMemcpy(p->d_step_items, st_items.data(), sizeof(WorkItem) * st_items.size(),
                                      cudaMemcpyHostToDevice));
-            // the planes' K padding (columns 32..63) is read by the GEMM and never written again
+            // rows past an instance's running block are read by the GEMM (their results dropped)
             PLAN_CUDA(cudaMemset(base + o_planes, 0, planes_bytes));
         }
     }

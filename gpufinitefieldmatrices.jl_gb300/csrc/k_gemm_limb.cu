@@ -47,6 +47,20 @@ int encode_digit_map(void *map, const void *base, int64_t kpad, int64_t rows, in
     return make_map(static_cast<CUtensorMap *>(map), base, kpad, rows, box_rows);
 }
 
+int encode_digit_map_k32(void *map, const void *base, int64_t rows, int box_rows) {
+    int st = get_encoder();
+    if (st) return st;
+    cuuint64_t dims[2] = {32, (cuuint64_t)rows};
+    cuuint64_t strides[1] = {64};
+    cuuint32_t box[2] = {32, (cuuint32_t)box_rows};
+    cuuint32_t estr[2] = {1, 1};
+    CUresult r = g_encode(static_cast<CUtensorMap *>(map), CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, const_cast<void *>(base),
+                          dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B,
+                          CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return gffm::set_error(GFFM_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+    return GFFM_OK;
+}
+
 int limbs_for(int64_t N) {
     // largest centred residue floor(N/2) must fit L balanced base-128 digits:
     // max positive value 63 * (128^L - 1) / 127

@@ -62,6 +62,8 @@ int split_b(const T *B, int64_t ldb, int64_t k, int64_t n, __half *D, const Layo
 // Encode the TMA descriptor (a 128-byte CUtensorMap at `map`) of a digit array:
 // `rows` rows of `kpad` fp16, box 64 x box_rows, 128-byte swizzle.
 int encode_digit_map(void *map, const void *base, int64_t kpad, int64_t rows, int box_rows);
+// the same over planes of K = 32 (64-byte rows): box 32 x box_rows, 64-byte swizzle
+int encode_digit_map_k32(void *map, const void *base, int64_t rows, int box_rows);
 
 // C (m x n, ldc) <- epilogue(A*B mod N) from digit planes; epi is a limb::Epi.  X, Y: EPI_KSUB_F64 only.
 // tile_counter: nullptr for the static tile schedule, else a device int (zero before the first of
