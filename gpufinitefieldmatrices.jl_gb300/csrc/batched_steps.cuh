@@ -106,7 +106,10 @@ __global__ void __launch_bounds__(PQ_THREADS) k_pq_prologue(StepArgs a, int coun
 // ---------------------------------------------------------------------------
 // one panel step of every running instance
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(PQ_THREADS, 2) k_pq_panel(StepArgs a, int s) {
+// MIN_BLOCKS: CTAs per SM the registers are sized for (the plan takes 3 where a step's
+// panel height lets three CTAs' shared memory fit)
+template <int MIN_BLOCKS>
+__global__ void __launch_bounds__(PQ_THREADS, MIN_BLOCKS) k_pq_panel(StepArgs a, int s) {
     extern __shared__ __align__(16) int32_t pq_smem[];
     __shared__ PQShared S;
     __shared__ uint32_t Lv[PQ_MAX_NB * 33];

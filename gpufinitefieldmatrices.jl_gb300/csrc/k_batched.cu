@@ -464,6 +464,7 @@ struct gffm_batch_plan_s {
     int n_step = 0, n_steps = 0, step_grid = 0, step_misc_grid = 0, trail_grid = 0;
     batched::StepArgs step{};
     std::vector<int> step_live;                 // per step: running instances
+    std::vector<int> step_rcap, step_smem, step_grid3;   // per step: panel height, shared memory, CTAs (0: 2 per SM)
     std::vector<int> step_items0;               // per step: first work item (n_steps + 1 entries)
     batched::WorkItem *d_step_items = nullptr;
     int *d_counters = nullptr;                  // the PLUQ kernels' scheduling counters
@@ -575,8 +576,15 @@ int build_graph(gffm_batch_plan p, bool overlap) {
                 k_pq_prologue<<<p->step_misc_grid, PQ_THREADS, conv_smem, pq_stream>>>(p->step, p->n_step);
                 fail(cudaGetLastError(), "k_pq_prologue");
                 for (int s = 0; s < p->n_steps; s++) {
-                    k_pq_panel<<<std::max(1, std::min(p->step_live[s], p->step_grid)), PQ_THREADS, p->pq_smem,
-                                 pq_stream>>>(p->step, s);
+                    StepArgs sa = p->step;
+                    sa.rcap = p->step_rcap[s];
+                    if (p->step_grid3[s]) {
+                        k_pq_panel<3><<<std::max(1, std::min(p->step_live[s], p->step_grid3[s])), PQ_THREADS,
+                                        p->step_smem[s], pq_stream>>>(sa, s);
+                    } else {
+                        k_pq_panel<2><<<std::max(1, std::min(p->step_live[s], p->step_grid)), PQ_THREADS,
+                                        p->step_smem[s], pq_stream>>>(sa, s);
+                    }
                     fail(cudaGetLastError(), "k_pq_panel");
                     const int i0 = p->step_items0[s], ni = p->step_items0[s + 1] - i0;
                     if (ni > 0) {
@@ -830,10 +838,22 @@ int create(const gffm_batch_desc *descs, int64_t count, const gffm_batch_tuning 
     p->pq_grid = std::max(1, std::min(p->n_pq, tu.pluq_ctas ? tu.pluq_ctas : per_sm * sms));
     if (p->n_step > 0) {
         int per_sm_step = 1;
-        PLAN_CUDA(cudaFuncSetAttribute(k_pq_panel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->pq_smem));
-        PLAN_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_step, k_pq_panel, PQ_THREADS, p->pq_smem));
+        PLAN_CUDA(cudaFuncSetAttribute(k_pq_panel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->pq_smem));
+        PLAN_CUDA(cudaFuncSetAttribute(k_pq_panel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->pq_smem));
+        PLAN_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_step, k_pq_panel<2>, PQ_THREADS, p->pq_smem));
         p->step_grid = std::max(1, per_sm_step) * sms;
         if (tu.pluq_ctas) p->step_grid = tu.pluq_ctas;
+        // per step: the panel height of its tallest running instance (the first in order), the
+        // shared memory it needs, and three CTAs per SM where they fit
+        for (int s = 0; s < p->n_steps; s++) {
+            const int rc = (int)align_up((size_t)stv[0].n - ST_NB * s, 4);
+            const size_t sm = pq_smem_words(rc) * 4;
+            int per3 = 0;
+            PLAN_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per3, k_pq_panel<3>, PQ_THREADS, sm));
+            p->step_rcap.push_back(rc);
+            p->step_smem.push_back((int)sm);
+            p->step_grid3.push_back(per3 >= 3 && !tu.pluq_ctas ? 3 * sms : 0);
+        }
         p->step_misc_grid = std::max(1, std::min(p->n_step, 4 * sms));
         p->trail_grid = sms;
         PLAN_CUDA(cudaFuncSetAttribute(k_gemm_trail, cudaFuncAttributeMaxDynamicSharedMemorySize, ST_SMEM_BYTES));

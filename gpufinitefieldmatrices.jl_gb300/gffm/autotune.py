@@ -11,8 +11,10 @@ and keeps the winners in a small JSON table, ``gffm/tuning.json``:
   need one digit fewer), the persistent grid size and the output tile width
   (64 columns, or 32 with two accumulator sets).
 * ``"batched"``: per batch signature (the multiset of instance shapes, ops and
-  digit counts), the best ``gffm_batch_tuning`` -- panel width of the PLUQ
-  kernel, grid split, overlap of the two graph branches, digit width.
+  digit counts), the best ``gffm_batch_tuning`` -- the PLUQ route (0: panel
+  steps with tensor-core trailing updates where they apply; 8/16/32: the
+  persistent kernel with that panel width), grid split, overlap of the two
+  graph branches, digit width.
   ``BatchPlan(instances, tuning="auto")`` looks it up.
 
 The table is plain data and ships with the package; re-tuning rewrites it.
@@ -156,6 +158,9 @@ def batch_signature(instances):
 
 
 BATCH_CANDIDATES = [
+    {"pluq_panel": 0, "gemm_ctas": 0, "pluq_ctas": 0, "overlap": 0, "digit_bits": 0},
+    {"pluq_panel": 0, "gemm_ctas": 0, "pluq_ctas": 0, "overlap": 1, "digit_bits": 0},
+    {"pluq_panel": 0, "gemm_ctas": 0, "pluq_ctas": 0, "overlap": 1, "digit_bits": 7},
     {"pluq_panel": 32, "gemm_ctas": 0, "pluq_ctas": 0, "overlap": 0, "digit_bits": 0},
     {"pluq_panel": 32, "gemm_ctas": 0, "pluq_ctas": 0, "overlap": 0, "digit_bits": 7},
     {"pluq_panel": 16, "gemm_ctas": 0, "pluq_ctas": 0, "overlap": 0, "digit_bits": 0},
@@ -192,10 +197,11 @@ def main():
     ap.add_argument("--batch", type=int, default=4096)
     ap.add_argument("--log", default=None)
     ap.add_argument("--gemm-only", action="store_true", help="retune the GEMM entries, keep the batched ones")
+    ap.add_argument("--batched-only", action="store_true", help="retune the batched entry, keep the GEMM ones")
     args = ap.parse_args()
     load()
     table = load_table(args.out)
-    entries, glog = tune_gemm()
+    entries, glog = (table.get("gemm", []), []) if args.batched_only else tune_gemm()
     table["gemm"] = entries
     if args.gemm_only:
         save_table(table, args.out)
