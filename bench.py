@@ -56,6 +56,7 @@ def parse_args():
     ap.add_argument("--no-karatsuba", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--batch", type=int, default=4096, help="instances of the batched workload")
+    ap.add_argument("--batch-pluqs", action="store_true", help="the batched leg with its PLUQ half only")
     ap.add_argument("--batch-uniform", default=None, metavar="COUNTxN",
                     help="with --only batched: COUNT seeded full-rank N x N PLUQ instances mod 67108859 instead of "
                          "the mixed workload (a case for profiling the batched PLUQ kernel)")
@@ -718,6 +719,9 @@ def batched_run(args, dev, large_gemm_gops):
     g = torch.Generator(device=dev)
     g.manual_seed(1234)
     inst = batched.build_config4(specs, generator=g)
+    if args.batch_pluqs:
+        keep = [i for i, s in enumerate(specs) if s[0] == "pluq"]
+        specs, inst = [specs[i] for i in keep], [inst[i] for i in keep]
     ops = batched.ops_of(specs)
 
     def timed(plan, reps=5):
@@ -747,7 +751,8 @@ def batched_run(args, dev, large_gemm_gops):
     if args.only == "batched":
         return out
     best = (ms, None)
-    for tu in ((0, 0, 0, 1, 0), (16, 0, 0, 0, 0), (32, 0, 0, 0, 7)):
+    # the step route without branch overlap, and the per-instance kernel (32- and 16-column panels)
+    for tu in ((0, 0, 0, 0, 0), (32, 0, 0, 1, 0), (16, 0, 0, 0, 0)):
         p2 = gffm.BatchPlan(inst, gffm.BatchTuning(*tu))
         t2 = timed(p2)
         out["tuning_%d_%d_%d_%d_%d_ms" % tu] = round(t2, 3)
