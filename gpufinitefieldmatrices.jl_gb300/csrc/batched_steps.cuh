@@ -31,6 +31,8 @@ namespace batched {
 constexpr int ST_NB = 32;                   // panel width of the step route
 constexpr int ST_BM = 128, ST_BN = 64;      // trailing GEMM tile (limb::BM x limb::BN)
 constexpr int ST_KPAD = 32;                 // K of the digit planes: 64-byte rows
+constexpr int ST_MAX_GROUPS = 2;            // step chains run side by side (graph branches)
+constexpr int ST_GROUP_MIN = 64;            // step instances needed before a batch is split into groups
 constexpr int ST_A_TILE = ST_BM * ST_KPAD * 2, ST_B_TILE = ST_BN * ST_KPAD * 2;   // one digit's tile
 constexpr int ST_STAGES = 4;
 constexpr int ST_STAGE_BYTES = 4 * (ST_A_TILE + ST_B_TILE);

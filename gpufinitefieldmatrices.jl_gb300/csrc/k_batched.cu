@@ -461,11 +461,18 @@ struct gffm_batch_plan_s {
     int32_t *d_tmp = nullptr;
     int tmp_ldw = 4;
     // the panel-step route (batched_steps.cuh)
-    int n_step = 0, n_steps = 0, step_grid = 0, step_misc_grid = 0, trail_grid = 0;
+    int n_step = 0, step_grid = 0, step_misc_grid = 0, trail_grid = 0;
     batched::StepArgs step{};
-    std::vector<int> step_live;                 // per step: running instances
-    std::vector<int> step_rcap, step_smem, step_grid3;   // per step: panel height, shared memory, CTAs (0: 2 per SM)
-    std::vector<int> step_items0;               // per step: first work item (n_steps + 1 entries)
+    // the step-route instances in groups, each factored by its own chain of step launches on
+    // its own graph branch, so that one group's launches fill the other's step tails
+    struct StepGroup {
+        batched::StepArgs args;                 // order, live and counters of the group
+        int n_steps = 0;
+        std::vector<int> live;                  // per step: running instances of the group
+        std::vector<int> rcap, smem, grid3;     // per step: panel height, shared memory, CTAs (0: 2 per SM)
+        std::vector<int> items0;                // per step: first work item (n_steps + 1 entries)
+    };
+    std::vector<StepGroup> groups;
     batched::WorkItem *d_step_items = nullptr;
     int *d_counters = nullptr;                  // the PLUQ kernels' scheduling counters
     int n_counters = 0;
@@ -555,6 +562,10 @@ int build_graph(gffm_batch_plan p, bool overlap) {
     cudaGraph_t graph = nullptr;
     int st = GFFM_OK;
     cudaEvent_t fork = nullptr, join = nullptr;
+    // the step-route groups' branches
+    cudaEvent_t gfork = nullptr;
+    cudaEvent_t gjoin[batched::ST_MAX_GROUPS] = {};
+    cudaStream_t gstreams[batched::ST_MAX_GROUPS] = {};
     auto fail = [&](cudaError_t e, const char *what) {
         if (st == GFFM_OK && e != cudaSuccess) st = gffm::cuda_error(e, what);
     };
@@ -575,22 +586,41 @@ int build_graph(gffm_batch_plan p, bool overlap) {
                 const size_t conv_smem = (size_t)8 * 32 * 33 * 4;
                 k_pq_prologue<<<p->step_misc_grid, PQ_THREADS, conv_smem, pq_stream>>>(p->step, p->n_step);
                 fail(cudaGetLastError(), "k_pq_prologue");
-                for (int s = 0; s < p->n_steps; s++) {
-                    StepArgs sa = p->step;
-                    sa.rcap = p->step_rcap[s];
-                    if (p->step_grid3[s]) {
-                        k_pq_panel<3><<<std::max(1, std::min(p->step_live[s], p->step_grid3[s])), PQ_THREADS,
-                                        p->step_smem[s], pq_stream>>>(sa, s);
-                    } else {
-                        k_pq_panel<2><<<std::max(1, std::min(p->step_live[s], p->step_grid)), PQ_THREADS,
-                                        p->step_smem[s], pq_stream>>>(sa, s);
+                const int G = (int)p->groups.size();
+                if (G > 1) {
+                    fail(cudaEventCreateWithFlags(&gfork, cudaEventDisableTiming), "cudaEventCreate");
+                    fail(cudaEventRecord(gfork, pq_stream), "cudaEventRecord");
+                }
+                for (int gi = 0; gi < G; gi++) {
+                    const auto &grp = p->groups[gi];
+                    cudaStream_t gs = pq_stream;
+                    if (gi > 0) {
+                        fail(cudaStreamCreateWithFlags(&gstreams[gi], cudaStreamNonBlocking), "cudaStreamCreate");
+                        fail(cudaStreamWaitEvent(gstreams[gi], gfork, 0), "cudaStreamWaitEvent");
+                        gs = gstreams[gi];
                     }
-                    fail(cudaGetLastError(), "k_pq_panel");
-                    const int i0 = p->step_items0[s], ni = p->step_items0[s + 1] - i0;
-                    if (ni > 0) {
-                        k_gemm_trail<<<std::min(ni, p->trail_grid), G_THREADS, ST_SMEM_BYTES, pq_stream>>>(
-                            p->step, s, p->d_step_items + i0, ni, gffm::device_error_flag());
-                        fail(cudaGetLastError(), "k_gemm_trail");
+                    for (int s = 0; s < grp.n_steps; s++) {
+                        StepArgs sa = grp.args;
+                        sa.rcap = grp.rcap[s];
+                        if (grp.grid3[s]) {
+                            k_pq_panel<3><<<std::max(1, std::min(grp.live[s], grp.grid3[s])), PQ_THREADS, grp.smem[s],
+                                            gs>>>(sa, s);
+                        } else {
+                            k_pq_panel<2><<<std::max(1, std::min(grp.live[s], p->step_grid)), PQ_THREADS, grp.smem[s],
+                                            gs>>>(sa, s);
+                        }
+                        fail(cudaGetLastError(), "k_pq_panel");
+                        const int i0 = grp.items0[s], ni = grp.items0[s + 1] - i0;
+                        if (ni > 0) {
+                            k_gemm_trail<<<std::min(ni, p->trail_grid), G_THREADS, ST_SMEM_BYTES, gs>>>(
+                                sa, s, p->d_step_items + i0, ni, gffm::device_error_flag());
+                            fail(cudaGetLastError(), "k_gemm_trail");
+                        }
+                    }
+                    if (gi > 0) {
+                        fail(cudaEventCreateWithFlags(&gjoin[gi], cudaEventDisableTiming), "cudaEventCreate");
+                        fail(cudaEventRecord(gjoin[gi], gs), "cudaEventRecord");
+                        fail(cudaStreamWaitEvent(pq_stream, gjoin[gi], 0), "cudaStreamWaitEvent");
                     }
                 }
                 k_pq_finish<<<p->step_misc_grid, PQ_THREADS, conv_smem + sizeof(int) * p->pq_rcap, pq_stream>>>(
@@ -630,6 +660,11 @@ int build_graph(gffm_batch_plan p, bool overlap) {
     if (graph) cudaGraphDestroy(graph);
     if (fork) cudaEventDestroy(fork);
     if (join) cudaEventDestroy(join);
+    if (gfork) cudaEventDestroy(gfork);
+    for (int gi = 0; gi < batched::ST_MAX_GROUPS; gi++) {
+        if (gjoin[gi]) cudaEventDestroy(gjoin[gi]);
+        if (gstreams[gi]) cudaStreamDestroy(gstreams[gi]);
+    }
     if (s1) cudaStreamDestroy(s1);
     cudaStreamDestroy(s0);
     return st;
@@ -776,7 +811,6 @@ int create(const gffm_batch_desc *descs, int64_t count, const gffm_batch_tuning 
         }
     std::stable_sort(st_q.begin(), st_q.end(), [&](int x, int y) { return pq[x].n > pq[y].n; });
     p->n_step = (int)st_q.size();
-    p->n_steps = p->n_step ? pq[st_q[0]].n / ST_NB : 0;
     std::vector<StepInst> stv(p->n_step);
     std::vector<size_t> o_src(p->n_step), o_id(p->n_step), o_u12(p->n_step), o_nr(p->n_step), o_ad(p->n_step),
         o_bd(p->n_step);
@@ -802,25 +836,40 @@ int create(const gffm_batch_desc *descs, int64_t count, const gffm_batch_tuning 
     }
     const size_t planes_bytes = cv.off > o_planes ? cv.off - o_planes : 0;
     const size_t o_steps = cv.take(sizeof(StepInst) * std::max(1, p->n_step));
+    // groups: the instances dealt round-robin in size order (similar mixes of sizes)
+    const int n_groups = p->n_step >= ST_GROUP_MIN ? ST_MAX_GROUPS : 1;
+    std::vector<std::vector<int>> gmembers(n_groups);
+    for (int j = 0; j < p->n_step; j++) gmembers[j % n_groups].push_back(j);
+    p->groups.resize(p->n_step > 0 ? n_groups : 0);
+    int total_steps = 0;
+    for (size_t gi = 0; gi < p->groups.size(); gi++) {
+        p->groups[gi].n_steps = gmembers[gi].empty() ? 0 : stv[gmembers[gi][0]].n / ST_NB;
+        total_steps += p->groups[gi].n_steps;
+    }
     const size_t o_st_order = cv.take(sizeof(int) * std::max(1, p->n_step));
-    const size_t o_live = cv.take(sizeof(int) * std::max(1, p->n_steps));
+    const size_t o_live = cv.take(sizeof(int) * std::max(1, total_steps));
     const size_t o_stmaps = cv.take(sizeof(CUtensorMap) * 2 * std::max(1, p->n_step), 128);
     const size_t o_flags = cv.take(sizeof(int) * std::max(1, p->n_pq));
-    p->n_counters = 1 + p->n_steps;   // the per-instance kernel's, then one per step
+    p->n_counters = 1 + total_steps;   // the per-instance kernel's, then one per group and step
     const size_t o_counters = cv.take(sizeof(int) * p->n_counters);
     std::vector<WorkItem> st_items;
-    for (int s = 0; s < p->n_steps; s++) {
-        int live = 0;
-        while (live < p->n_step && stv[live].n > ST_NB * s) live++;
-        p->step_live.push_back(live);
-        p->step_items0.push_back((int)st_items.size());
-        for (int j = 0; j < live; j++) {
-            const int rt = stv[j].n - ST_NB * s - ST_NB;   // rows = columns of the trailing block
-            for (int tm = 0; tm < (rt + ST_BM - 1) / ST_BM; tm++)
-                for (int tn = 0; tn < (rt + ST_BN - 1) / ST_BN; tn++) st_items.push_back(WorkItem{j, tm, tn, 0});
+    for (size_t gi = 0; gi < p->groups.size(); gi++) {
+        auto &grp = p->groups[gi];
+        const auto &mem = gmembers[gi];
+        for (int s = 0; s < grp.n_steps; s++) {
+            int live = 0;
+            while (live < (int)mem.size() && stv[mem[live]].n > ST_NB * s) live++;
+            grp.live.push_back(live);
+            grp.items0.push_back((int)st_items.size());
+            for (int q = 0; q < live; q++) {
+                const int j = mem[q];
+                const int rt = stv[j].n - ST_NB * s - ST_NB;   // rows = columns of the trailing block
+                for (int tm = 0; tm < (rt + ST_BM - 1) / ST_BM; tm++)
+                    for (int tn = 0; tn < (rt + ST_BN - 1) / ST_BN; tn++) st_items.push_back(WorkItem{j, tm, tn, 0});
+            }
         }
+        grp.items0.push_back((int)st_items.size());
     }
-    p->step_items0.push_back((int)st_items.size());
     const size_t o_st_items = cv.take(sizeof(WorkItem) * std::max<size_t>(1, st_items.size()));
     // PLUQ grid (it sizes the per-CTA row-move buffers)
     p->pq_nb = tu.pluq_panel ? tu.pluq_panel : 32;
@@ -843,16 +892,19 @@ int create(const gffm_batch_desc *descs, int64_t count, const gffm_batch_tuning 
         PLAN_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_step, k_pq_panel<2>, PQ_THREADS, p->pq_smem));
         p->step_grid = std::max(1, per_sm_step) * sms;
         if (tu.pluq_ctas) p->step_grid = tu.pluq_ctas;
-        // per step: the panel height of its tallest running instance (the first in order), the
-        // shared memory it needs, and three CTAs per SM where they fit
-        for (int s = 0; s < p->n_steps; s++) {
-            const int rc = (int)align_up((size_t)stv[0].n - ST_NB * s, 4);
-            const size_t sm = pq_smem_words(rc) * 4;
-            int per3 = 0;
-            PLAN_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per3, k_pq_panel<3>, PQ_THREADS, sm));
-            p->step_rcap.push_back(rc);
-            p->step_smem.push_back((int)sm);
-            p->step_grid3.push_back(per3 >= 3 && !tu.pluq_ctas ? 3 * sms : 0);
+        // per group and step: the panel height of its tallest running instance (the first in
+        // the group's order), the shared memory it needs, and three CTAs per SM where they fit
+        for (size_t gi = 0; gi < p->groups.size(); gi++) {
+            auto &grp = p->groups[gi];
+            for (int s = 0; s < grp.n_steps; s++) {
+                const int rc = (int)align_up((size_t)stv[gmembers[gi][0]].n - ST_NB * s, 4);
+                const size_t sm = pq_smem_words(rc) * 4;
+                int per3 = 0;
+                PLAN_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per3, k_pq_panel<3>, PQ_THREADS, sm));
+                grp.rcap.push_back(rc);
+                grp.smem.push_back((int)sm);
+                grp.grid3.push_back(per3 >= 3 && !tu.pluq_ctas ? 3 * sms : 0);
+            }
         }
         p->step_misc_grid = std::max(1, std::min(p->n_step, 4 * sms));
         p->trail_grid = sms;
@@ -967,6 +1019,20 @@ int create(const gffm_batch_desc *descs, int64_t count, const gffm_batch_tuning 
     p->step.tmaps = reinterpret_cast<CUtensorMap *>(base + o_stmaps);
     p->step.rcap = p->pq_rcap;
     p->d_step_items = reinterpret_cast<WorkItem *>(base + o_st_items);
+    {
+        // each group's arguments: the shared ones (set above), with its own slices of the
+        // order, live counts and counters
+        int order_off = 0, step_off = 0;
+        for (size_t gi = 0; gi < p->groups.size(); gi++) {
+            auto &grp = p->groups[gi];
+            grp.args = p->step;
+            grp.args.order = p->step.order + order_off;
+            grp.args.live = p->step.live + step_off;
+            grp.args.next = p->step.next + step_off;
+            order_off += (int)gmembers[gi].size();
+            step_off += grp.n_steps;
+        }
+    }
     std::iota(order.begin(), order.end(), 0);
     std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
         const int64_t wa = (int64_t)pq[a].m * pq[a].n * std::min(pq[a].m, pq[a].n);
@@ -989,15 +1055,18 @@ int create(const gffm_batch_desc *descs, int64_t count, const gffm_batch_tuning 
     PLAN_CUDA(cudaMemcpy(p->d_order, order.data(), sizeof(int) * order.size(), cudaMemcpyHostToDevice));
     {
         // every PLUQ starts on the per-instance kernel; the prologue hands the step route's back
-        std::vector<int> ones(std::max(1, p->n_pq), 1), st_order(std::max(1, p->n_step));
-        std::iota(st_order.begin(), st_order.end(), 0);
+        std::vector<int> ones(std::max(1, p->n_pq), 1), st_order, st_live;
+        for (size_t gi = 0; gi < p->groups.size(); gi++) {
+            st_order.insert(st_order.end(), gmembers[gi].begin(), gmembers[gi].end());
+            st_live.insert(st_live.end(), p->groups[gi].live.begin(), p->groups[gi].live.end());
+        }
         PLAN_CUDA(cudaMemcpy(p->step.flags, ones.data(), sizeof(int) * ones.size(), cudaMemcpyHostToDevice));
         if (p->n_step > 0) {
             PLAN_CUDA(cudaMemcpy(const_cast<StepInst *>(p->step.steps), stv.data(), sizeof(StepInst) * stv.size(),
                                  cudaMemcpyHostToDevice));
             PLAN_CUDA(cudaMemcpy(const_cast<int *>(p->step.order), st_order.data(), sizeof(int) * p->n_step,
                                  cudaMemcpyHostToDevice));
-            PLAN_CUDA(cudaMemcpy(const_cast<int *>(p->step.live), p->step_live.data(), sizeof(int) * p->n_steps,
+            PLAN_CUDA(cudaMemcpy(const_cast<int *>(p->step.live), st_live.data(), sizeof(int) * st_live.size(),
                                  cudaMemcpyHostToDevice));
             PLAN_CUDA(cudaMemcpy(const_cast<CUtensorMap *>(p->step.tmaps), stmaps.data(),
                                  sizeof(CUtensorMap) * 2 * p->n_step, cudaMemcpyHostToDevice));
