@@ -88,10 +88,11 @@ __device__ __forceinline__ void put_digits8(const uint32_t (&v)[8], uint32_t N, 
 // ---------------------------------------------------------------------------
 // prologue: the working copies, row identities and counters of every step instance
 // ---------------------------------------------------------------------------
+// the first `count` instances of a.order (a group's)
 __global__ void __launch_bounds__(PQ_THREADS) k_pq_prologue(StepArgs a, int count) {
     extern __shared__ __align__(16) int32_t pq_smem[];
-    for (int j = blockIdx.x; j < count; j += gridDim.x) {
-        const StepInst J = a.steps[j];
+    for (int q = blockIdx.x; q < count; q += gridDim.x) {
+        const StepInst J = a.steps[a.order[q]];
         const PQInst &I = a.inst[J.pq];
         const elim::ModP M{I.M.n, I.M.minv};
         to_rowmajor(I.A, I.lda, I.W, I.ldw, J.n, J.n, M, pq_smem);
@@ -527,11 +528,12 @@ __global__ void __launch_bounds__(G_THREADS, 1)
 // the outputs of every step instance that was not handed back
 // ---------------------------------------------------------------------------
 // dynamic shared memory: the conversions' 8 x 32 x 33 words, then the row identities
+// the first `count` instances of a.order (a group's)
 __global__ void __launch_bounds__(PQ_THREADS) k_pq_finish(StepArgs a, int count) {
     extern __shared__ __align__(16) int32_t pq_smem[];
     int *id_s = pq_smem + 8 * 32 * 33;
-    for (int j = blockIdx.x; j < count; j += gridDim.x) {
-        const StepInst J = a.steps[j];
+    for (int q = blockIdx.x; q < count; q += gridDim.x) {
+        const StepInst J = a.steps[a.order[q]];
         if (a.flags[J.pq]) continue;   // uniform over the block; k_pluq_batched writes its outputs
         const PQInst &I = a.inst[J.pq];
         for (int r = threadIdx.x; r < J.n; r += blockDim.x) id_s[r] = J.ident[r];

@@ -467,7 +467,7 @@ struct gffm_batch_plan_s {
     // its own graph branch, so that one group's launches fill the other's step tails
     struct StepGroup {
         batched::StepArgs args;                 // order, live and counters of the group
-        int n_steps = 0;
+        int n_steps = 0, members = 0;
         std::vector<int> live;                  // per step: running instances of the group
         std::vector<int> rcap, smem, grid3;     // per step: panel height, shared memory, CTAs (0: 2 per SM)
         std::vector<int> items0;                // per step: first work item (n_steps + 1 entries)
@@ -584,8 +584,6 @@ int build_graph(gffm_batch_plan p, bool overlap) {
             fail(cudaMemsetAsync(p->d_counters, 0, sizeof(int) * p->n_counters, pq_stream), "cudaMemsetAsync");
             if (p->n_step > 0) {
                 const size_t conv_smem = (size_t)8 * 32 * 33 * 4;
-                k_pq_prologue<<<p->step_misc_grid, PQ_THREADS, conv_smem, pq_stream>>>(p->step, p->n_step);
-                fail(cudaGetLastError(), "k_pq_prologue");
                 const int G = (int)p->groups.size();
                 if (G > 1) {
                     fail(cudaEventCreateWithFlags(&gfork, cudaEventDisableTiming), "cudaEventCreate");
@@ -599,6 +597,11 @@ int build_graph(gffm_batch_plan p, bool overlap) {
                         fail(cudaStreamWaitEvent(gstreams[gi], gfork, 0), "cudaStreamWaitEvent");
                         gs = gstreams[gi];
                     }
+                    // the group's working copies, its steps, then its outputs
+                    const int gcount = (int)grp.members;
+                    k_pq_prologue<<<std::max(1, std::min(gcount, p->step_misc_grid)), PQ_THREADS, conv_smem, gs>>>(
+                        grp.args, gcount);
+                    fail(cudaGetLastError(), "k_pq_prologue");
                     for (int s = 0; s < grp.n_steps; s++) {
                         StepArgs sa = grp.args;
                         sa.rcap = grp.rcap[s];
@@ -617,15 +620,15 @@ int build_graph(gffm_batch_plan p, bool overlap) {
                             fail(cudaGetLastError(), "k_gemm_trail");
                         }
                     }
+                    k_pq_finish<<<std::max(1, std::min(gcount, p->step_misc_grid)), PQ_THREADS,
+                                  conv_smem + sizeof(int) * p->pq_rcap, gs>>>(grp.args, gcount);
+                    fail(cudaGetLastError(), "k_pq_finish");
                     if (gi > 0) {
                         fail(cudaEventCreateWithFlags(&gjoin[gi], cudaEventDisableTiming), "cudaEventCreate");
                         fail(cudaEventRecord(gjoin[gi], gs), "cudaEventRecord");
                         fail(cudaStreamWaitEvent(pq_stream, gjoin[gi], 0), "cudaStreamWaitEvent");
                     }
                 }
-                k_pq_finish<<<p->step_misc_grid, PQ_THREADS, conv_smem + sizeof(int) * p->pq_rcap, pq_stream>>>(
-                    p->step, p->n_step);
-                fail(cudaGetLastError(), "k_pq_finish");
             }
             PQArgs a;
             a.inst = p->d_pq;
@@ -844,6 +847,7 @@ int create(const gffm_batch_desc *descs, int64_t count, const gffm_batch_tuning 
     int total_steps = 0;
     for (size_t gi = 0; gi < p->groups.size(); gi++) {
         p->groups[gi].n_steps = gmembers[gi].empty() ? 0 : stv[gmembers[gi][0]].n / ST_NB;
+        p->groups[gi].members = (int)gmembers[gi].size();
         total_steps += p->groups[gi].n_steps;
     }
     const size_t o_st_order = cv.take(sizeof(int) * std::max(1, p->n_step));
