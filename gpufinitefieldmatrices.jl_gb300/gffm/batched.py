@@ -3,9 +3,11 @@
 The reference runs one product (mul!, src/CuModMatrix/CuModMatrix.jl:767-787)
 or one pluq_gpu_kernel (src/CuModMatrix/rref_lu_pluq/pluq_kernels.jl:46-157)
 per call; a BatchPlan runs thousands of them, each with its own sizes and
-modulus, as one CUDA graph (a grouped tensor-core product kernel and a
-persistent PLUQ kernel).  Instances are CuModArrays; results land in the
-arrays the plan was built with.
+modulus, as one CUDA graph: a grouped tensor-core product kernel, square
+PLUQs (n = 32k, odd prime) in panel steps whose trailing updates are one
+grouped tensor-core GEMM per step, and a persistent per-instance PLUQ kernel
+for the others.  Both PLUQ routes give the reference's factorization.
+Instances are CuModArrays; results land in the arrays the plan was built with.
 """
 import ctypes
 
