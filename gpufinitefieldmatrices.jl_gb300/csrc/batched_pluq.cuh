@@ -149,9 +149,10 @@ __device__ void to_rowmajor(const double *A, int64_t lda, int32_t *W, int ldw, i
 }
 
 // Columns c < map_cols read row rowmap[r] for output row r (rowmap may be null when
-// map_cols is 0).
+// map_cols is 0); with tri_block > 0 such a column is zero in the rows above its block of
+// tri_block columns, which are not read.
 __device__ void to_colmajor(const int32_t *W, int ldw, int wcols, double *A, int64_t lda, int m, int n,
-                            int32_t *scratch, const int *rowmap = nullptr, int map_cols = 0) {
+                            int32_t *scratch, const int *rowmap = nullptr, int map_cols = 0, int tri_block = 0) {
     const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
     const int tc = (n + 31) >> 5, nt = ((m + 31) >> 5) * tc;
     for (int t0 = 0; t0 < nt; t0 += PQ_TPR) {
@@ -162,7 +163,7 @@ __device__ void to_colmajor(const int32_t *W, int ldw, int wcols, double *A, int
 #pragma unroll
             for (int i = 0; i < 4; i++) {
                 const int r = r0 + ty + 8 * i, c = c0 + tx;
-                const bool in = t0 + q < nt && r < m && c < wcols;
+                const bool in = t0 + q < nt && r < m && c < wcols && !(tri_block && c < map_cols && r < c - c % tri_block);
                 v[q][i] = in ? W[(int64_t)(c < map_cols ? rowmap[r] : r) * ldw + c] : 0;
             }
         }

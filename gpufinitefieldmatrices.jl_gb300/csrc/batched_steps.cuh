@@ -39,6 +39,16 @@ constexpr int ST_STAGE_BYTES = 4 * (ST_A_TILE + ST_B_TILE);
 constexpr int ST_SMEM_BYTES = ST_STAGES * ST_STAGE_BYTES + 1024;
 static_assert(ST_BM == limb::BM && ST_BN == limb::BN, "the step GEMM's epilogue uses the limb tile shape");
 
+// Dynamic shared memory of k_pq_panel for panels of up to rcap rows: the panel (32 columns
+// of rcap + 4 words), whose space the trailing columns' pivot rows (32 x PQ_CW words) reuse
+// once the panel has been written out, then the swap composition's scratch (2 rcap words)
+// and the panel's row sources (rcap words).
+__host__ __device__ constexpr size_t st_panel_words(int rcap) {
+    return (size_t)PQ_MAX_NB * (rcap + 4) > (size_t)PQ_MAX_NB * PQ_CW ? (size_t)PQ_MAX_NB * (rcap + 4)
+                                                                       : (size_t)PQ_MAX_NB * PQ_CW;
+}
+__host__ __device__ constexpr size_t st_smem_words(int rcap) { return st_panel_words(rcap) + 3 * (size_t)rcap; }
+
 struct StepInst {
     int pq;                      // index in the PLUQ instance array
     int n;                       // m = n, a multiple of 32
@@ -96,7 +106,7 @@ __global__ void __launch_bounds__(PQ_THREADS) k_pq_prologue(StepArgs a, int coun
         const PQInst &I = a.inst[J.pq];
         const elim::ModP M{I.M.n, I.M.minv};
         to_rowmajor(I.A, I.lda, I.W, I.ldw, J.n, J.n, M, pq_smem);
-        for (int64_t idx = threadIdx.x; idx < (int64_t)J.n * I.ldlw; idx += blockDim.x) I.LW[idx] = 0;
+        // (L's working copy is not cleared: the finish reads only the entries the steps write)
         for (int r = threadIdx.x; r < J.n; r += blockDim.x) J.ident[r] = r;
         if (threadIdx.x == 0) {
             *J.nr = 0;
@@ -120,8 +130,9 @@ __global__ void __launch_bounds__(PQ_THREADS, MIN_BLOCKS) k_pq_panel(StepArgs a,
     const int tid = threadIdx.x;
     const int rs = a.rcap + 4;
     int32_t *P = pq_smem;
-    int32_t *Us = pq_smem + (size_t)PQ_MAX_NB * rs;
-    int *srcmap = Us + PQ_MAX_NB * PQ_CW;
+    int32_t *Us = pq_smem;                                   // the panel's space, after the panel
+    int *scratch = pq_smem + st_panel_words(a.rcap);         // the swap composition's
+    int *srcmap = scratch + 2 * a.rcap;
     const int r0 = ST_NB * s, c0 = r0;
 
     for (;;) {
@@ -177,7 +188,7 @@ __global__ void __launch_bounds__(PQ_THREADS, MIN_BLOCKS) k_pq_panel(StepArgs a,
             } else {
                 if (tid == 0) {
                     int nr = *J.nr;
-                    pq_compose(S, npiv, r0, Us, a.rcap, I.row_swaps, nr);
+                    pq_compose(S, npiv, r0, scratch, a.rcap, I.row_swaps, nr);
                     *J.nr = nr;
                 }
                 // the panel back to W, a row a thread in 16-byte stores: U on and above the
@@ -228,6 +239,7 @@ __global__ void __launch_bounds__(PQ_THREADS, MIN_BLOCKS) k_pq_panel(StepArgs a,
                         put_digits8(v, N, J.L, J.Ad + (size_t)(lr - ST_NB) * ST_KPAD + t0, plane);
                     }
                 }
+                __syncthreads();   // the panel is written out: its space takes the pivot rows
                 // the pivot rows of the trailing columns, PQ_CW at a time: U12 and the B planes
                 for (int cb = c0 + ST_NB; cb < n; cb += PQ_CW) {
                     const int cw = min(PQ_CW, n - cb);
@@ -538,7 +550,8 @@ __global__ void __launch_bounds__(PQ_THREADS) k_pq_finish(StepArgs a, int count)
         const PQInst &I = a.inst[J.pq];
         for (int r = threadIdx.x; r < J.n; r += blockDim.x) id_s[r] = J.ident[r];
         to_colmajor(I.W, I.ldw, J.n, I.U, I.ldu, J.n, J.n, pq_smem);   // its barriers order the id_s stores
-        to_colmajor(I.LW, I.ldlw, I.lwc, I.L, I.ldl, J.n, I.l_cols, pq_smem, id_s, I.lsw);
+        // L by row identity; a column's rows above its panel block were never written: zero
+        to_colmajor(I.LW, I.ldlw, I.lwc, I.L, I.ldl, J.n, I.l_cols, pq_smem, id_s, I.lsw, ST_NB);
         if (threadIdx.x == 0) {
             I.info[0] = *J.nr;
             I.info[1] = 0;

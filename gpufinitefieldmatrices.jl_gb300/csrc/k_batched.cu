@@ -902,12 +902,16 @@ int create(const gffm_batch_desc *descs, int64_t count, const gffm_batch_tuning 
             auto &grp = p->groups[gi];
             for (int s = 0; s < grp.n_steps; s++) {
                 const int rc = (int)align_up((size_t)stv[gmembers[gi][0]].n - ST_NB * s, 4);
-                const size_t sm = pq_smem_words(rc) * 4;
+                const size_t sm = st_smem_words(rc) * 4;
                 int per3 = 0;
                 PLAN_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per3, k_pq_panel<3>, PQ_THREADS, sm));
                 grp.rcap.push_back(rc);
                 grp.smem.push_back((int)sm);
                 grp.grid3.push_back(per3 >= 3 && !tu.pluq_ctas ? 3 * sms : 0);
+                if (sm > p->pq_smem) {   // never for these layouts; kept in step with the attribute
+                    PLAN_CUDA(cudaFuncSetAttribute(k_pq_panel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+                    PLAN_CUDA(cudaFuncSetAttribute(k_pq_panel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+                }
             }
         }
         p->step_misc_grid = std::max(1, std::min(p->n_step, 4 * sms));

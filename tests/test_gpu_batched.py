@@ -199,3 +199,21 @@ def test_step_route_matches_oracle(gffm):
             assert torch.equal(a[0].data, b[0].data) and torch.equal(a[1].data, b[1].data)
     check(gffm, inst, want, plan.run().results())
     assert gffm.load_library().gffm_device_status(None) == 0
+
+
+def test_step_chains_match_per_instance_kernel(gffm):
+    """A batch large enough for the step route's two chains (>= 64 step instances): every
+    PLUQ bit for bit equal to the per-instance kernel's, rank-deficient ones included."""
+    rng = np.random.default_rng(6464)
+    primes = [8191, 65521, 2080639, 16777213, P26]
+    inst = []
+    for i in range(128):
+        n, N = 32 * int(rng.integers(2, 17)), primes[i % len(primes)]
+        kind = "rank%d" % (n - 5) if i % 16 == 3 else ("zero_cols" if i % 16 == 7 else "uniform")
+        inst.append(("pluq", gffm.CuModMatrix(make(kind, n, n, N, rng), N, elem_type=torch.float64)))
+    steps = gffm.BatchPlan(inst).run().results()
+    per_inst = gffm.BatchPlan(inst, gffm.BatchTuning(32, 0, 0, 0, 0)).run().results()
+    for a, b in zip(steps, per_inst):
+        assert a[2] == b[2] and a[3] == b[3]
+        assert torch.equal(a[0].data, b[0].data) and torch.equal(a[1].data, b[1].data)
+    assert gffm.load_library().gffm_device_status(None) == 0
