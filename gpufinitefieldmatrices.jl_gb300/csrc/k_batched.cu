@@ -470,6 +470,7 @@ struct gffm_batch_plan_s {
         int n_steps = 0, members = 0;
         std::vector<int> live;                  // per step: running instances of the group
         std::vector<int> rcap, smem, grid3;     // per step: panel height, shared memory, CTAs (0: 2 per SM)
+        std::vector<int> per_sm;                // per step: panel CTAs per SM (2, 3 or 4)
         std::vector<int> items0;                // per step: first work item (n_steps + 1 entries)
     };
     std::vector<StepGroup> groups;
@@ -505,6 +506,8 @@ size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
 // PLUQ instances with more rows run after the graph on the single-matrix elimination
 constexpr int64_t kGraphPluqMaxRows = 1024;
+// the step route's panel kernel at four CTAs per SM where shared memory allows (64 registers)
+constexpr bool kStepFourPerSM = true;
 
 int check_desc(const gffm_batch_desc &d, int64_t i) {
     if (d.op != GFFM_BATCH_MATMUL && d.op != GFFM_BATCH_PLUQ)
@@ -605,7 +608,10 @@ int build_graph(gffm_batch_plan p, bool overlap) {
                     for (int s = 0; s < grp.n_steps; s++) {
                         StepArgs sa = grp.args;
                         sa.rcap = grp.rcap[s];
-                        if (grp.grid3[s]) {
+                        if (grp.per_sm[s] == 4) {
+                            k_pq_panel<4><<<std::max(1, std::min(grp.live[s], grp.grid3[s])), PQ_THREADS, grp.smem[s],
+                                            gs>>>(sa, s);
+                        } else if (grp.grid3[s]) {
                             k_pq_panel<3><<<std::max(1, std::min(grp.live[s], grp.grid3[s])), PQ_THREADS, grp.smem[s],
                                             gs>>>(sa, s);
                         } else {
@@ -893,6 +899,7 @@ int create(const gffm_batch_desc *descs, int64_t count, const gffm_batch_tuning 
         int per_sm_step = 1;
         PLAN_CUDA(cudaFuncSetAttribute(k_pq_panel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->pq_smem));
         PLAN_CUDA(cudaFuncSetAttribute(k_pq_panel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->pq_smem));
+        PLAN_CUDA(cudaFuncSetAttribute(k_pq_panel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->pq_smem));
         PLAN_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_step, k_pq_panel<2>, PQ_THREADS, p->pq_smem));
         p->step_grid = std::max(1, per_sm_step) * sms;
         if (tu.pluq_ctas) p->step_grid = tu.pluq_ctas;
@@ -903,11 +910,14 @@ int create(const gffm_batch_desc *descs, int64_t count, const gffm_batch_tuning 
             for (int s = 0; s < grp.n_steps; s++) {
                 const int rc = (int)align_up((size_t)stv[gmembers[gi][0]].n - ST_NB * s, 4);
                 const size_t sm = st_smem_words(rc) * 4;
-                int per3 = 0;
+                int per3 = 0, per4 = 0;
                 PLAN_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per3, k_pq_panel<3>, PQ_THREADS, sm));
+                PLAN_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per4, k_pq_panel<4>, PQ_THREADS, sm));
+                const int k = tu.pluq_ctas ? 2 : (per4 >= 4 && kStepFourPerSM ? 4 : (per3 >= 3 ? 3 : 2));
                 grp.rcap.push_back(rc);
                 grp.smem.push_back((int)sm);
-                grp.grid3.push_back(per3 >= 3 && !tu.pluq_ctas ? 3 * sms : 0);
+                grp.per_sm.push_back(k);
+                grp.grid3.push_back(k >= 3 ? k * sms : 0);
                 if (sm > p->pq_smem) {   // never for these layouts; kept in step with the attribute
                     PLAN_CUDA(cudaFuncSetAttribute(k_pq_panel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
                     PLAN_CUDA(cudaFuncSetAttribute(k_pq_panel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
