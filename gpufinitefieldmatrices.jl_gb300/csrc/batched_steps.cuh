@@ -496,14 +496,15 @@ __global__ void __launch_bounds__(G_THREADS, 1)
                 break;
             }
             gffm_dev::tc_fence_after();
+            // one shift at a time: pairing the shifts (limb::fast_pair) spills registers here
+            // and measured slower
             for (int q = 0; q < nshift; q++) {
                 uint32_t v[16];
                 gffm_dev::tmem_ld_32x32b_x16(tq + 64 * q, v);
                 gffm_dev::tmem_ld_wait();
                 const int w = Wm[q];
 #pragma unroll
-                for (int j = 0; j < 16; j++)
-                    acc[j] += (int64_t)(int32_t)__float_as_uint(__fadd_rn(__uint_as_float(v[j]), 12582912.0f)) * w;
+                for (int j = 0; j < 16; j++) acc[j] += (int64_t)(int32_t)fast_bits(v[j]) * w;
             }
             gffm_dev::tc_fence_before();
             __syncwarp();
@@ -511,7 +512,7 @@ __global__ void __launch_bounds__(G_THREADS, 1)
             acc_phase ^= 1;
             if (live) {
                 int32_t *dst = dst_row + col;
-                // x in [0, 2^26 p): (x + m p) / 2^32 < 2p is x 2^-32 mod p; then + the old value
+                // x in (0, 2^32 p): (x + m p) / 2^32 < 2p is x 2^-32 mod p; then + the old value
                 auto fin = [&](int64_t a64, int32_t old) -> int32_t {
                     const uint64_t x = (uint64_t)a64;
                     const uint32_t mq = (uint32_t)x * ninv;

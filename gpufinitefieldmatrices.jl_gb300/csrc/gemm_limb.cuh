@@ -100,7 +100,7 @@ struct Params {
     // mantissa) and reduced by a 32-bit Montgomery step, the weights carrying 2^32.
     uint32_t ninv;             // -N^-1 mod 2^32
     int32_t Wm[MAX_SHIFTS];    // 2^(bits*s) * 2^32 mod N
-    int64_t fbias;             // N * 2^25 - 0x4B400000 * sum_s Wm[s]
+    int64_t fbias;             // the initial value (fast_consts): takes out the magic-number bits
 };
 
 __device__ __forceinline__ void tile_coords(int t, int mtiles, int ntiles, int &tm, int &tn) {
@@ -110,6 +110,22 @@ __device__ __forceinline__ void tile_coords(int t, int mtiles, int ntiles, int &
     int local = t - group * TILE_GROUP * ntiles;
     tm = first_m + local % gsz;
     tn = local / gsz;
+}
+
+// The fast drain reads a shift sum C (|C| <= 2^22, exact in fp32) by adding 1.5 * 2^23:
+// the result's bits are 0x4B400000 + C.  With 7-bit digits the weights of shifts s and
+// s + 1 differ by 2^7, so the pair takes the single weight Wm[s]: bits_s + (bits_{s+1} << 7)
+// in wrapping 32-bit arithmetic is C_s + 2^7 C_{s+1} + FAST_PAIR_OFFSET exactly, where
+// FAST_PAIR_OFFSET = 129 * 0x4B400000 mod 2^32 read as int32 (|C_s + 2^7 C_{s+1}| <= 2^29.01,
+// so the sum stays inside int32).  The constants come out through the initial value
+// (fast_consts), and a 2L - 1 shift drain does L wide multiply-adds instead of 2L - 1.
+constexpr int32_t FAST_MAGIC_BITS = 0x4B400000;
+constexpr int32_t FAST_PAIR_OFFSET = -348127232;
+__device__ __forceinline__ uint32_t fast_bits(uint32_t v) {
+    return __float_as_uint(__fadd_rn(__uint_as_float(v), 12582912.0f));
+}
+__device__ __forceinline__ int32_t fast_pair(uint32_t lo, uint32_t hi) {
+    return (int32_t)(fast_bits(lo) + (fast_bits(hi) << 7));
 }
 
 __device__ __forceinline__ int64_t reduce_signed(int64_t acc, const Params &p) {
@@ -348,8 +364,23 @@ __global__ void __launch_bounds__(gemm_threads(EPI), 1)
                     break;
                 }
                 gffm_dev::tc_fence_after();
+                if (FAST) {
+                    // shifts in pairs, one wide multiply-add per pair (fast_pair)
 #pragma unroll
-                for (int s = 0; s < C_::NSHIFT; s++) {
+                    for (int s = 0; s < C_::NSHIFT; s += 2) {
+                        uint32_t v[CW], u[CW];
+                        const uint32_t ta = accb + ((uint32_t)(quad * 32) << 16) + BNV * s;
+                        gffm_dev::tmem_ld_32x32b<CW>(ta, v);
+                        if (s + 1 < C_::NSHIFT) gffm_dev::tmem_ld_32x32b<CW>(ta + BNV, u);
+                        gffm_dev::tmem_ld_wait();
+                        const int w = p.Wm[s];
+#pragma unroll
+                        for (int j = 0; j < CW; j++)
+                            acc[j] += (int64_t)(s + 1 < C_::NSHIFT ? fast_pair(v[j], u[j]) : (int32_t)fast_bits(v[j])) * w;
+                    }
+                }
+#pragma unroll
+                for (int s = 0; s < (FAST ? 0 : C_::NSHIFT); s++) {
                     uint32_t v[CW];
                     gffm_dev::tmem_ld_32x32b<CW>(accb + ((uint32_t)(quad * 32) << 16) + BNV * s, v);
                     gffm_dev::tmem_ld_wait();
@@ -360,13 +391,6 @@ __global__ void __launch_bounds__(gemm_threads(EPI), 1)
                         for (int j = 0; j < CW; j++)
                             acc[j] = (int64_t)((uint64_t)acc[j] +
                                                ((uint64_t)(int64_t)__float2int_rz(__uint_as_float(v[j])) << (7 * s)));
-                    } else if (FAST) {
-                        // bits(C + 1.5 * 2^23) = 0x4B400000 + C for |C| < 2^22; the constant
-                        // is taken out through the initial value (fbias)
-                        const int w = p.Wm[s];
-#pragma unroll
-                        for (int j = 0; j < CW; j++)
-                            acc[j] += (int64_t)(int32_t)__float_as_uint(__fadd_rn(__uint_as_float(v[j]), 12582912.0f)) * w;
                     } else {
                         const int w = p.W[s];
 #pragma unroll
@@ -392,7 +416,7 @@ __global__ void __launch_bounds__(gemm_threads(EPI), 1)
                 if (SUB) {
                     int32_t *cbase = (int32_t *)p.C + row + col0 * p.ldc;
                     if (FAST) {
-                        // x in [0, 2^26 N): t = (x + m N) / 2^32 < 2N, t = x 2^-32 mod N
+                        // x in (0, 2^32 N): t = (x + m N) / 2^32 < 2N, t = x 2^-32 mod N
                         const uint32_t n32 = (uint32_t)p.N;
 #pragma unroll
                         for (int j = 0; j < CW; j++) {

@@ -28,11 +28,12 @@ struct MMInst {
     int64_t bias;
     double *C;
     int64_t ldc;
-    // fast epilogue (odd N, one exact chunk whose shift sums stay within 2^22): the sums
-    // are read by adding 1.5 * 2^23 in fp32 and reduced by one 32-bit Montgomery step
+    // fast epilogue (fast != 0: odd N, one exact chunk whose shift sums stay within 2^22):
+    // the sums are read by adding 1.5 * 2^23 in fp32 (in pairs when fast == 2, the 7-bit
+    // digits' case; limb::fast_pair) and reduced by one 32-bit Montgomery step
     uint32_t ninv;               // -N^-1 mod 2^32
     int32_t Wm[MAX_SHIFTS];      // 2^(bits s) * 2^32 mod N
-    int64_t fbias;               // N * 2^25 - 0x4B400000 * sum_s Wm[s]
+    int64_t fbias;               // the initial value (limb::fast_consts)
 };
 
 struct WorkItem {
@@ -222,15 +223,37 @@ __device__ __forceinline__ bool grouped_tile(const MMInst &I, const WorkItem &it
             return false;
         }
         gffm_dev::tc_fence_after();
-        for (int s = 0; s < nshift; s++) {
+        if (FAST && I.fast == 2) {
+            // the shifts in pairs, 8 columns of both at a time
+            for (int s = 0; s < nshift; s += 2) {
+                const int w = I.Wm[s];
+                if (s + 1 < nshift) {
+#pragma unroll
+                    for (int h = 0; h < 16; h += 8) {
+                        uint32_t v[8], u[8];
+                        gffm_dev::tmem_ld_32x32b_x8(tq + 64 * s + h, v);
+                        gffm_dev::tmem_ld_32x32b_x8(tq + 64 * (s + 1) + h, u);
+                        gffm_dev::tmem_ld_wait();
+#pragma unroll
+                        for (int j = 0; j < 8; j++) acc[h + j] += (int64_t)fast_pair(v[j], u[j]) * w;
+                    }
+                } else {
+                    uint32_t v[16];
+                    gffm_dev::tmem_ld_32x32b_x16(tq + 64 * s, v);
+                    gffm_dev::tmem_ld_wait();
+#pragma unroll
+                    for (int j = 0; j < 16; j++) acc[j] += (int64_t)(int32_t)fast_bits(v[j]) * w;
+                }
+            }
+        }
+        for (int s = 0; s < (FAST && I.fast == 2 ? 0 : nshift); s++) {
             uint32_t v[16];
             gffm_dev::tmem_ld_32x32b_x16(tq + 64 * s, v);
             gffm_dev::tmem_ld_wait();
             if (FAST) {
                 const int w = I.Wm[s];
 #pragma unroll
-                for (int j = 0; j < 16; j++)
-                    acc[j] += (int64_t)(int32_t)__float_as_uint(__fadd_rn(__uint_as_float(v[j]), 12582912.0f)) * w;
+                for (int j = 0; j < 16; j++) acc[j] += (int64_t)(int32_t)fast_bits(v[j]) * w;
             } else {
                 const int w = I.W[s];
 #pragma unroll
@@ -255,7 +278,7 @@ __device__ __forceinline__ bool grouped_tile(const MMInst &I, const WorkItem &it
         for (int j = 0; j < 16; j++) {
             if (col0 + j < I.n) {
                 if (FAST) {
-                    // x in [0, 2^26 N): t = (x + m N) / 2^32 < 2N, t = x 2^-32 mod N
+                    // x in (0, 2^32 N): t = (x + m N) / 2^32 < 2N, t = x 2^-32 mod N
                     const uint64_t x = (uint64_t)acc[j];
                     const uint32_t mq = (uint32_t)x * I.ninv;
                     uint32_t r = (uint32_t)((x + (uint64_t)mq * n32) >> 32);
@@ -543,21 +566,6 @@ struct Carve {
     }
 };
 
-// The grouped GEMM's fast epilogue (odd N, one exact chunk): -N^-1 mod 2^32, the shift
-// weights 2^(bits s) 2^32 mod N and the bias that keeps the sum positive.
-void fast_consts(int64_t N, int L, int bits, uint32_t &ninv, int32_t *Wm, int64_t &fbias) {
-    uint32_t inv = 1;                         // N^-1 mod 2^32 by Newton's iteration
-    for (int it = 0; it < 5; it++) inv *= 2u - (uint32_t)N * inv;
-    ninv = 0u - inv;
-    int64_t w = 1 % N, wsum = 0;
-    for (int s = 0; s < limb::MAX_SHIFTS; s++) {
-        Wm[s] = (int32_t)(((__int128)w << 32) % N);
-        if (s < 2 * L - 1) wsum += Wm[s];
-        w = (w << bits) % N;
-    }
-    fbias = N * (int64_t(1) << 25) - (int64_t)0x4B400000 * wsum;
-}
-
 int build_graph(gffm_batch_plan p, bool overlap) {
     using namespace batched;
     cudaStream_t s0, s1 = nullptr;
@@ -767,8 +775,8 @@ int create(const gffm_batch_desc *descs, int64_t count, const gffm_batch_tuning 
         I.fbias = 0;
         if ((d.N & 1) && I.kblocks <= I.chunk_kb &&
             (int64_t)I.kblocks * BK * g.L * (int64_t(1) << (2 * g.bits - 2)) <= (int64_t(1) << 22)) {
-            fast_consts(d.N, g.L, g.bits, I.ninv, I.Wm, I.fbias);
-            I.fast = 1;
+            limb::fast_consts(d.N, g.L, g.bits, g.bits == 7, &I.ninv, I.Wm, &I.fbias);
+            I.fast = g.bits == 7 ? 2 : 1;   // 2: the drain reads the shifts in pairs
         } else {
             for (int sft = 0; sft < MAX_SHIFTS; sft++) I.Wm[sft] = 0;
         }
@@ -832,7 +840,7 @@ int create(const gffm_batch_desc *descs, int64_t count, const gffm_batch_tuning 
         J.L = limb::limbs_for(d.N);
         J.Mpad = (int)align_up((size_t)d.n - ST_NB, ST_BM);
         J.Npad = (int)align_up((size_t)d.n - ST_NB, ST_BN);
-        fast_consts(d.N, J.L, 7, J.ninv, J.Wm, J.fbias);
+        limb::fast_consts(d.N, J.L, 7, false, &J.ninv, J.Wm, &J.fbias);
         o_src[j] = cv.take(sizeof(int) * d.n);
         o_id[j] = cv.take(sizeof(int) * d.n);
         o_u12[j] = cv.take(sizeof(int32_t) * ST_NB * d.n);

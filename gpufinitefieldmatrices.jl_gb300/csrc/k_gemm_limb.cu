@@ -85,6 +85,32 @@ int chunk_kblocks(const Layout &g) {
     return g.bits == 8 ? std::max(1, 16 / g.L) : 64 / g.L;
 }
 
+void fast_consts(int64_t N, int L, int bits, bool paired, uint32_t *ninv, int32_t *Wm, int64_t *fbias) {
+    uint32_t inv = 1;                         // N^-1 mod 2^32 by Newton's iteration
+    for (int it = 0; it < 5; it++) inv *= 2u - (uint32_t)N * inv;
+    *ninv = 0u - inv;
+    int64_t w = 1 % N;
+    for (int s = 0; s < MAX_SHIFTS; s++) {
+        Wm[s] = (int32_t)(((__int128)w << 32) % N);
+        w = (w << bits) % N;
+    }
+    const int nshift = 2 * L - 1;
+    if (paired && bits == 7) {
+        // pairs (0, 1), (2, 3), ... read as C_s + 2^7 C_{s+1} + FAST_PAIR_OFFSET with weight
+        // Wm[s], the last shift alone as C + FAST_MAGIC_BITS.  The sum of the L terms is
+        // within +-2^30.6 N, so the bias N 2^31 keeps x in (0, 2^32 N).
+        int64_t b = N * (int64_t(1) << 31);
+        for (int s = 0; s + 1 < nshift; s += 2) b -= (int64_t)FAST_PAIR_OFFSET * Wm[s];
+        *fbias = b - (int64_t)FAST_MAGIC_BITS * Wm[nshift - 1];
+    } else {
+        // one shift at a time: each read as C + FAST_MAGIC_BITS; the sum is within
+        // +-7 2^22 N, so the bias N 2^25 keeps x in (0, 2^26 N)
+        int64_t wsum = 0;
+        for (int s = 0; s < nshift; s++) wsum += Wm[s];
+        *fbias = N * (int64_t(1) << 25) - (int64_t)FAST_MAGIC_BITS * wsum;
+    }
+}
+
 Layout layout_bits(int64_t m, int64_t n, int64_t k, int64_t N, int bits) {
     Layout g = layout_L(m, n, k, limbs_for_bits(N, bits));
     g.bits = bits == 8 ? 8 : 7;
@@ -248,18 +274,11 @@ int gemm_digits(const Layout &g, const __half *Ad, const __half *Bd, int64_t m, 
         p.W[sft] = (int32_t)w;      // unused by EPI_EXACT_I64, whose N may exceed 32 bits
         w = (int64_t)(((__int128)w * (g.bits == 8 ? 256 : 128)) % N);
     }
-    // the read-modify-write fast path: odd N, one exact chunk, shift sums below 2^22
-    if (epi == EPI_SUB_I32 && (N & 1) && p.kblocks <= p.chunk_kb &&
+    // the read-modify-write fast path: odd N, one exact chunk, shift sums within 2^22, 7-bit
+    // digits (its drain reads the shifts in pairs)
+    if (epi == EPI_SUB_I32 && (N & 1) && g.bits == 7 && p.kblocks <= p.chunk_kb &&
         (int64_t)p.kblocks * BK * g.L * (int64_t(1) << (2 * g.bits - 2)) <= (int64_t(1) << 22)) {
-        uint32_t inv = 1;                         // N^-1 mod 2^32 by Newton's iteration
-        for (int it = 0; it < 5; it++) inv *= 2u - (uint32_t)N * inv;
-        p.ninv = 0u - inv;
-        int64_t wsum = 0;
-        for (int sft = 0; sft < MAX_SHIFTS; sft++) {
-            p.Wm[sft] = (int32_t)(((__int128)p.W[sft] << 32) % N);
-            if (sft < 2 * g.L - 1) wsum += p.Wm[sft];
-        }
-        p.fbias = N * (int64_t(1) << 25) - (int64_t)0x4B400000 * wsum;
+        fast_consts(N, g.L, g.bits, true, &p.ninv, p.Wm, &p.fbias);
         epi = EPI_SUB_I32M;
     }
     p.C = C;

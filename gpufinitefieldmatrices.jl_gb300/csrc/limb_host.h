@@ -39,6 +39,12 @@ int raw_limbs_for(int64_t N);
 Layout layout(int64_t m, int64_t n, int64_t k, int64_t N);
 Layout layout_bits(int64_t m, int64_t n, int64_t k, int64_t N, int bits);
 int chunk_kblocks(const Layout &g);        // k-blocks of 64 per exact accumulation chunk
+// The fast drain's constants (odd N, one exact chunk, shift sums within 2^22): ninv =
+// -N^-1 mod 2^32, Wm[s] = 2^(bits s) 2^32 mod N for s < MAX_SHIFTS, and the initial
+// value that takes out the magic-number bits and keeps the sum in (0, 2^32 N), for a
+// drain that reads the shifts in pairs (`paired`, 7-bit digits only; see fast_pair) or
+// one at a time.
+void fast_consts(int64_t N, int L, int bits, bool paired, uint32_t *ninv, int32_t *Wm, int64_t *fbias);
 // how the digit products of a limb GEMM are formed (gffm_limb_tuning.form)
 enum Form { FORM_DEFAULT = 0, FORM_SCHOOLBOOK = 1, FORM_KARATSUBA = 2 };
 // the default form is Karatsuba (kara_host.h) for four 7-bit digits from this inner dimension on
