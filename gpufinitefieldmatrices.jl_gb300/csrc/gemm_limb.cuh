@@ -354,6 +354,7 @@ __global__ void __launch_bounds__(gemm_threads(EPI), 1)
             int64_t acc[CW];
 #pragma unroll
             for (int j = 0; j < CW; j++) acc[j] = FAST ? p.fbias : 0;
+            int32_t dp[FAST ? (C_::NSHIFT + 1) / 2 : 1][FAST ? CW : 1];   // the fast drain's pairs
             bool ok = true;
             int chunk = 0;
             for (int kb0 = 0; kb0 < p.kblocks; kb0 += p.chunk_kb, chunk++) {
@@ -365,18 +366,21 @@ __global__ void __launch_bounds__(gemm_threads(EPI), 1)
                 }
                 gffm_dev::tc_fence_after();
                 if (FAST) {
-                    // shifts in pairs, one wide multiply-add per pair (fast_pair)
+                    // shifts in pairs (fast_pair), kept as int32 until the accumulator is
+                    // released; 8 columns of both shifts at a time
 #pragma unroll
                     for (int s = 0; s < C_::NSHIFT; s += 2) {
-                        uint32_t v[CW], u[CW];
-                        const uint32_t ta = accb + ((uint32_t)(quad * 32) << 16) + BNV * s;
-                        gffm_dev::tmem_ld_32x32b<CW>(ta, v);
-                        if (s + 1 < C_::NSHIFT) gffm_dev::tmem_ld_32x32b<CW>(ta + BNV, u);
-                        gffm_dev::tmem_ld_wait();
-                        const int w = p.Wm[s];
 #pragma unroll
-                        for (int j = 0; j < CW; j++)
-                            acc[j] += (int64_t)(s + 1 < C_::NSHIFT ? fast_pair(v[j], u[j]) : (int32_t)fast_bits(v[j])) * w;
+                        for (int h = 0; h < CW; h += 8) {
+                            uint32_t v[8], u[8];
+                            const uint32_t ta = accb + ((uint32_t)(quad * 32) << 16) + BNV * s + h;
+                            gffm_dev::tmem_ld_32x32b_x8(ta, v);
+                            if (s + 1 < C_::NSHIFT) gffm_dev::tmem_ld_32x32b_x8(ta + BNV, u);
+                            gffm_dev::tmem_ld_wait();
+#pragma unroll
+                            for (int j = 0; j < 8; j++)
+                                dp[s / 2][h + j] = s + 1 < C_::NSHIFT ? fast_pair(v[j], u[j]) : (int32_t)fast_bits(v[j]);
+                        }
                     }
                 }
 #pragma unroll
@@ -401,6 +405,15 @@ __global__ void __launch_bounds__(gemm_threads(EPI), 1)
                 __syncwarp();
                 if (lane == 0) gffm_dev::mbar_arrive(&acc_empty_bar[buf]);
                 acc_phase ^= 1;
+                if (FAST) {
+                    // the wide multiply-adds run while the next tile's mma's fill the accumulator
+#pragma unroll
+                    for (int i = 0; i < (C_::NSHIFT + 1) / 2; i++) {
+                        const int w = p.Wm[2 * i];
+#pragma unroll
+                        for (int j = 0; j < CW; j++) acc[j] += (int64_t)dp[i][j] * w;
+                    }
+                }
                 if (EPI == EPI_EXACT_I64) {
                     // acc < N < 2^52 before the chunk, so acc + chunk < 2^63: one Barrett step
 #pragma unroll
