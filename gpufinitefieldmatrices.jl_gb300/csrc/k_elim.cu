@@ -576,9 +576,11 @@ static int run_panel(Work &w, int m, int n, int R0, int C0, int nbw, const ModP 
 // one), the trailing update of the
 // columns past it runs beside it on the other SMs (a second stream).  The next
 // panel's own columns are updated first, on the whole GPU.
+// The panel beside a side update takes at least 64 rows a CTA and at most 48 CTAs unless
+// its rows need more (48 measured best on a 16384^2 factorization among caps 24 to 64).
 static int look_ctas(int rows) {
     const int gmin = (rows + PANEL_MAX_R - 1) / PANEL_MAX_R;   // the panel's rows per CTA
-    return std::max(gmin, std::min(32, (rows + 63) / 64));
+    return std::max(gmin, std::min(48, (rows + 63) / 64));
 }
 
 struct Lookahead {
