@@ -496,13 +496,31 @@ __global__ void __launch_bounds__(G_THREADS, 1)
                 break;
             }
             gffm_dev::tc_fence_after();
-            // one shift at a time: pairing the shifts (limb::fast_pair) spills registers here
-            // and measured slower
-            for (int q = 0; q < nshift; q++) {
-                uint32_t v[16];
-                gffm_dev::tmem_ld_32x32b_x16(tq + 64 * q, v);
-                gffm_dev::tmem_ld_wait();
+            // 7-bit digits: the shifts in pairs, one wide multiply-add each (limb::fast_pair),
+            // 8 columns of both shifts at a time
+#pragma unroll 1
+            for (int q = 0; q + 1 < nshift; q += 2) {
                 const int w = Wm[q];
+#pragma unroll 1
+                for (int h = 0; h < 16; h += 8) {
+                    uint32_t v[8], u[8];
+                    gffm_dev::tmem_ld_32x32b_x8(tq + 64 * q + h, v);
+                    gffm_dev::tmem_ld_32x32b_x8(tq + 64 * (q + 1) + h, u);
+                    gffm_dev::tmem_ld_wait();
+                    if (h == 0) {
+#pragma unroll
+                        for (int j = 0; j < 8; j++) acc[j] += (int64_t)fast_pair(v[j], u[j]) * w;
+                    } else {
+#pragma unroll
+                        for (int j = 0; j < 8; j++) acc[8 + j] += (int64_t)fast_pair(v[j], u[j]) * w;
+                    }
+                }
+            }
+            {
+                uint32_t v[16];
+                gffm_dev::tmem_ld_32x32b_x16(tq + 64 * (nshift - 1), v);
+                gffm_dev::tmem_ld_wait();
+                const int w = Wm[nshift - 1];
 #pragma unroll
                 for (int j = 0; j < 16; j++) acc[j] += (int64_t)(int32_t)fast_bits(v[j]) * w;
             }

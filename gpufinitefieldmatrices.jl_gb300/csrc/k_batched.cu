@@ -840,7 +840,7 @@ int create(const gffm_batch_desc *descs, int64_t count, const gffm_batch_tuning 
         J.L = limb::limbs_for(d.N);
         J.Mpad = (int)align_up((size_t)d.n - ST_NB, ST_BM);
         J.Npad = (int)align_up((size_t)d.n - ST_NB, ST_BN);
-        limb::fast_consts(d.N, J.L, 7, false, &J.ninv, J.Wm, &J.fbias);
+        limb::fast_consts(d.N, J.L, 7, true, &J.ninv, J.Wm, &J.fbias);
         o_src[j] = cv.take(sizeof(int) * d.n);
         o_id[j] = cv.take(sizeof(int) * d.n);
         o_u12[j] = cv.take(sizeof(int32_t) * ST_NB * d.n);
