@@ -9,7 +9,8 @@ the 129 MB L2, so no flush is needed between steps.
 Printed JSON line (one, from rank 0):
   value        whole-job Gop/s (2*m*n*k per step, all ranks)
   e2e          the same metric through the C ABI with host buffers: every step
-               copies A and B from pinned host memory and C back
+               copies A and B from pinned host memory and C back (the median of
+               three timed runs, all three listed)
   roofline     the tcgen05 GEMM kernel's tensor FLOP/s (digit products) vs the
                measured dense bf16/fp16 peak; traffic from an ncu capture (its
                source is named in the line: no run reads DRAM counters itself)
