@@ -34,9 +34,12 @@ constexpr int ST_KPAD = 32;                 // K of the digit planes: 64-byte ro
 constexpr int ST_MAX_GROUPS = 2;            // step chains run side by side (graph branches)
 constexpr int ST_GROUP_MIN = 64;            // step instances needed before a batch is split into groups
 constexpr int ST_A_TILE = ST_BM * ST_KPAD * 2, ST_B_TILE = ST_BN * ST_KPAD * 2;   // one digit's tile
-constexpr int ST_STAGES = 4;
+constexpr int ST_STAGES = 3;
 constexpr int ST_STAGE_BYTES = 4 * (ST_A_TILE + ST_B_TILE);
-constexpr int ST_SMEM_BYTES = ST_STAGES * ST_STAGE_BYTES + 1024;
+// after the stages: two slots of 64 bytes per epilogue thread for the next tile's old values
+constexpr int ST_PF_BYTES = 2 * 512 * 64;
+constexpr int ST_SMEM_BYTES = ST_STAGES * ST_STAGE_BYTES + ST_PF_BYTES + 1024;
+static_assert(ST_SMEM_BYTES <= 227 * 1024, "trail GEMM shared memory");
 static_assert(ST_BM == limb::BM && ST_BN == limb::BN, "the step GEMM's epilogue uses the limb tile shape");
 
 // Dynamic shared memory of k_pq_panel for panels of up to rcap rows: the panel (32 columns
@@ -433,7 +436,10 @@ __global__ void __launch_bounds__(G_THREADS, 1)
         // ---------------- epilogue ----------------
         // A thread owns one row and 16 columns of the tile.  The row's old values are loaded
         // before the accumulator is waited for (no tile of this launch writes a row another
-        // tile reads: sources are pivot rows or the row itself).
+        // tile reads: sources are pivot rows or the row itself): a tile's by cp.async into
+        // one of two shared slots while the previous tile drains, when both belong to the
+        // same instance, else directly.  Every iteration commits one (possibly empty)
+        // cp.async group, so waiting for all but the newest finds the current tile's.
         const int quad = warp & 3;
         const int part = (warp - 2) >> 2;   // which 16 of the tile's 64 columns
         const uint32_t tq = tmem + ((uint32_t)(quad * 32) << 16) + 16 * part;
@@ -447,6 +453,8 @@ __global__ void __launch_bounds__(G_THREADS, 1)
         const int *srcmap = nullptr;
         const int32_t *src_row = nullptr;
         int32_t *dst_row = nullptr;
+        uint8_t *pf_base = smem + ST_STAGES * ST_STAGE_BYTES + (threadIdx.x - 64) * 64;
+        bool have = false;   // this tile's old values were prefetched into slot t & 1
         WorkItem nx = t_begin < t_end ? items[t_begin] : WorkItem{0, 0, 0, 0};
         for (int t = t_begin; t < t_end; t++) {
             const WorkItem it = nx;
@@ -469,8 +477,7 @@ __global__ void __launch_bounds__(G_THREADS, 1)
                 n32 = I.M.n;
                 srcmap = J.srcmap;
             }
-            if (skip) continue;
-            if (it.tm != last_tm) {
+            if (!skip && it.tm != last_tm) {
                 last_tm = it.tm;
                 const int rt = it.tm * ST_BM + quad * 32 + lane;   // row within the trailing block
                 row_live = rt < n - r0 - ST_NB;
@@ -479,12 +486,35 @@ __global__ void __launch_bounds__(G_THREADS, 1)
                     dst_row = W + (int64_t)(r0 + ST_NB + rt) * ldw;
                 }
             }
+            // the next tile's old values, if it belongs to this instance and is live
+            const bool cur = have;
+            have = false;
+            if (!skip && t + 1 < t_end && nx.inst == it.inst) {
+                const int rtn = nx.tm * ST_BM + quad * 32 + lane;
+                const int coln = r0 + ST_NB + nx.tn * ST_BN + part * 16;
+                if (rtn < n - r0 - ST_NB && coln < n) {
+                    const int32_t *srcn = nx.tm == it.tm ? src_row : W + (int64_t)(r0 + srcmap[ST_NB + rtn]) * ldw;
+                    uint8_t *slot = pf_base + ((t + 1) & 1) * (512 * 64);
+#pragma unroll
+                    for (int q = 0; q < 4; q++) gffm_dev::cp_async16(slot + 16 * q, srcn + coln + 4 * q);
+                    have = true;
+                }
+            }
+            gffm_dev::cp_async_commit();
+            if (skip) continue;
             const int col = r0 + ST_NB + it.tn * ST_BN + part * 16;   // n - col is 0 or >= 16
             const bool live = row_live && col < n;
             int4 c4[4];
             if (live) {
+                if (cur) {
+                    gffm_dev::cp_async_wait<1>();
+                    const int4 *slot = reinterpret_cast<const int4 *>(pf_base + (t & 1) * (512 * 64));
 #pragma unroll
-                for (int q = 0; q < 4; q++) c4[q] = *reinterpret_cast<const int4 *>(src_row + col + 4 * q);
+                    for (int q = 0; q < 4; q++) c4[q] = slot[q];
+                } else {
+#pragma unroll
+                    for (int q = 0; q < 4; q++) c4[q] = *reinterpret_cast<const int4 *>(src_row + col + 4 * q);
+                }
             }
             const int nshift = 2 * L - 1;
             int64_t acc[16];
@@ -547,6 +577,7 @@ __global__ void __launch_bounds__(G_THREADS, 1)
                 }
             }
         }
+        gffm_dev::cp_async_wait<0>();   // no copy into shared memory outlives the CTA
     }
 
     gffm_dev::tc_fence_before();
